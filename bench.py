@@ -1,0 +1,362 @@
+#!/usr/bin/env python3
+"""Benchmark of the MHFEM time step on GB300.
+
+Workload: the 3D heterogeneous-diffusion problem on the unit cube as a 64^3
+grid of cubes split into 6 tetrahedra each (1,572,864 cells, 3,170,304 faces,
+interior vertices jittered by +-0.15h, D = exp(g) with g a seeded Gaussian
+field, f = 1, Dirichlet 0 on x=0,1 and zero flux elsewhere, dt = 1e-3,
+BiCGStab to a relative residual of 1e-10).  A "step" is one backward-Euler
+time step: coefficient / mass-matrix update, condensation, assembly, Krylov
+solve and reconstruction (control.h:83-98).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Rank 0 prints one JSON line.  `value` is time steps/s of the plain FP64 form
+summed over all replicas (each GPU runs an independent copy of the
+workload: the path is not sharded, "replicas only").  `e2e` is the same
+metric through the public C ABI with host buffers: every step uploads the
+source field from pinned host memory and reads Z_iK back.  The mixed form is
+reported beside it under "forms".  `--impl reference` times the CPU
+restatement of the reference algorithm (the reference itself cannot be
+built: its TNL dependency is absent) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parent
+PKG = REPO / "tnl-mhfem_gb300"
+for _p in (str(PKG), str(REPO)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "time steps/s & face-DOF/s: FP64 vs mixed/learned at 1e-8 rel err; HBM GB/s"
+UNIT = "time steps/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--grid", type=int, default=64, help="cubes per axis (64 = the benchmark workload)")
+    ap.add_argument("--cpu-steps", type=int, default=3, help="time steps of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples taken during the timed region."""
+
+    def __init__(self, device: int):
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(device), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        self.file.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.file.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.file.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def step_bytes(n, nf, S, C, F, V, W, iters, d_full=True):
+    """Algorithmic bytes of one time step (each array once at its size)."""
+    R = n * F
+    rec = nf * n * (n * nf + 1) * C * 8
+    cell = 4 * nf * C + 8 * 3 * V + (8 * n * n * C if d_full else 0) + 8 * n * C + 4 * nf * C + C \
+        + 8 * n * n * S * C + 8 * n * n * nf * C + 8 * n * C + rec
+    assemble = 15 * F + rec + 8 * W * R + 8 * R
+    init = R * (12 * W + 8 + 8 + 8 + 24)
+    per_iter = R * (24 * W + 160)
+    recon = 4 * nf * C + 8 * n * F + 8 * n * n * nf * C + 16 * n * C
+    return cell + assemble + init + iters * per_iter + recon
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    from mhfem import problems
+    from oracle.oracle import OracleModel, load
+
+    lib = load()
+    threads = os.cpu_count() or 1
+    lib.orc_set_threads(threads)
+    p = problems.diffusion3d(N=args.grid)
+    m = OracleModel.from_problem(p)
+    t = 0.0
+    for _ in range(args.warmup):
+        m.step(t, p.dt, p.tol)
+        t += p.dt
+    iters = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        it, _ = m.step(t, p.dt, p.tol)
+        iters.append(it)
+        t += p.dt
+    el = time.perf_counter() - t0
+    value = args.steps / el
+    sample = f"{args.steps} time steps of the 64^3 tetrahedral workload after {args.warmup} warm-up steps"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": f"diffusion3d_{args.grid}", "cells": m.C, "faces": m.F,
+                                            "form": "fp64 (CPU restatement, OpenMP)", "tol": p.tol, "dt": p.dt},
+            "face_dof_per_s": value * m.F * p.n, "iterations_per_step": statistics.mean(iters),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(p, steps):
+    from oracle.oracle import OracleModel, load
+
+    lib = load()
+    threads = os.cpu_count() or 1
+    lib.orc_set_threads(threads)
+    m = OracleModel.from_problem(p)
+    t = 0.0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        m.step(t, p.dt, p.tol)
+        t += p.dt
+    el = time.perf_counter() - t0
+    return {"value": steps / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"the first {steps} time steps of the same 64^3 workload (CPU restatement of the "
+                      "reference algorithm, OpenMP, FP64, same tolerance)"}
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+        return
+
+    import numpy as np
+    import torch
+
+    from mhfem import _lib as L
+    from mhfem import problems
+
+    torch.cuda.set_device(local)
+    dev = local
+    p = problems.diffusion3d(N=args.grid)
+    p.config.device = dev
+    s = problems.make_solver(p, check_every=8)
+    ext = torch.cuda.ExternalStream(s.stream(), device=dev)
+    n, nf, S = p.n, 4, 14
+    C, F, V = s.C, s.F, s.V
+    rows = n * F
+    W = (2 * nf - 1) * n - 1
+
+    t = 0.0
+    for _ in range(args.warmup):
+        s.step(t, p.dt)
+        t += p.dt
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    it0, _, kl0 = s.totals()
+    clocks = ClockSampler(dev)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    stats = []
+    torch.cuda.synchronize()
+    ev0.record(ext)
+    for _ in range(args.steps):
+        stats.append(s.step(t, p.dt))
+        t += p.dt
+    ev1.record(ext)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    el_ms = ev0.elapsed_time(ev1)
+    it1, _, kl1 = s.totals()
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([el_ms], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        el_ms = float(tt.item())
+        dist.barrier()
+    zf64, zk64 = s.state()
+    iters = (it1 - it0) / args.steps
+    ms_step = el_ms / args.steps
+    value = world * args.steps / (el_ms / 1e3)
+    bytes_step = step_bytes(n, nf, S, C, F, V, W, iters)
+
+    # dominant kernel: the FP64 SpMV fused with its dot product
+    hbm_peak, peak_kind = measured_peaks()
+    spmv = s.time_kernel(L.KERNEL_SPMV_FP64, reps=50)
+    achieved = spmv["bytes"] / (spmv["ms"] * 1e-3) / 1e9
+    kernels = {}
+    for name, kid in [("cell_local", L.KERNEL_CELL_LOCAL), ("assemble", L.KERNEL_ASSEMBLE),
+                      ("reconstruct", L.KERNEL_RECONSTRUCT)]:
+        r = s.time_kernel(kid, reps=20)
+        kernels[name] = {"ms": r["ms"], "gbs": r["bytes"] / (r["ms"] * 1e-3) / 1e9,
+                         "hbm_frac": r["bytes"] / (r["ms"] * 1e-3) / 1e9 / hbm_peak,
+                         "fp64_tflops": r["flops"] / (r["ms"] * 1e-3) / 1e12}
+    kernels["spmv_fp64"] = {"ms": spmv["ms"], "gbs": achieved, "hbm_frac": achieved / hbm_peak,
+                            "fp64_tflops": spmv["flops"] / (spmv["ms"] * 1e-3) / 1e12}
+    traffic = None
+    tfile = REPO / "profiles" / "spmv_fp64_diffusion3d.txt"
+    if tfile.exists():
+        for line in tfile.read_text().splitlines():
+            if line.startswith("dram_bytes_per_launch_full_size:"):
+                try:
+                    traffic = float(line.split(":", 1)[1].split()[0])
+                except ValueError:
+                    traffic = None
+    gpu_launches = kl1 - kl0
+
+    forms = {}
+    if not args.no_mixed:
+        pm = problems.diffusion3d(N=args.grid, form=L.FORM_MIXED)
+        pm.config.device = dev
+        sm = problems.make_solver(pm, check_every=8)
+        extm = torch.cuda.ExternalStream(sm.stream(), device=dev)
+        tm = 0.0
+        for _ in range(args.warmup):
+            sm.step(tm, pm.dt)
+            tm += pm.dt
+        itm0, _, _ = sm.totals()
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a0.record(extm)
+        sweeps = []
+        for _ in range(args.steps):
+            sweeps.append(sm.step(tm, pm.dt)["sweeps"])
+            tm += pm.dt
+        a1.record(extm)
+        a1.synchronize()
+        mel = a0.elapsed_time(a1)
+        itm1, _, _ = sm.totals()
+        zfm, zkm = sm.state()
+        err_f = float(np.abs(zfm - zf64).max() / max(np.abs(zf64).max(), 1e-300))
+        err_k = float(np.abs(zkm - zk64).max() / max(np.abs(zk64).max(), 1e-300))
+        sp32 = sm.time_kernel(L.KERNEL_SPMV_FP32, reps=50)
+        forms["mixed"] = {"value": world * args.steps / (mel / 1e3), "ms_per_step": mel / args.steps,
+                          "speedup_vs_fp64": (args.steps / mel) / (args.steps / el_ms),
+                          "inner_iterations_per_step": (itm1 - itm0) / args.steps,
+                          "sweeps_per_step": statistics.mean(sweeps),
+                          "rel_err_face_traces_vs_fp64": err_f, "rel_err_cell_values_vs_fp64": err_k,
+                          "spmv_fp32_gbs": sp32["bytes"] / (sp32["ms"] * 1e-3) / 1e9}
+        sm.close()
+
+    e2e = None
+    if not args.no_e2e:
+        f_host = torch.ones(C, dtype=torch.float64).pin_memory().numpy()
+        zk_host = torch.empty(C, dtype=torch.float64).pin_memory().numpy()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            s.set_coeff("f", f_host)          # host -> device: this step's source field
+            s.step(t, p.dt, stats=False)
+            s._ck(s.lib.mhfem_get_state(s._h, None, zk_host.ctypes.data_as(
+                __import__("ctypes").POINTER(__import__("ctypes").c_double))))  # device -> host: Z_iK
+            t += p.dt
+        torch.cuda.synchronize()
+        e_el = time.perf_counter() - t0
+        if world > 1:
+            import torch.distributed as dist
+            tt = torch.tensor([e_el], dtype=torch.float64)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            e_el = float(tt.item())
+        e2e = {"value": world * args.steps / e_el, "unit": UNIT, "h2d_bytes_per_step": 8 * C,
+               "d2h_bytes_per_step": 8 * C, "path": "mhfem_set_coeff + mhfem_step + mhfem_get_state (ctypes)"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(problems.diffusion3d(N=args.grid), args.cpu_steps)
+
+    s.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded jittered 64^3 cube grid split into 6 tetrahedra, D = exp(Gaussian field)",
+        "config": {"workload": f"diffusion3d_{args.grid}", "cells": C, "faces": F, "rows": rows,
+                   "nnz": int(rows + (rows - 0) * 0) if False else None, "tol": p.tol, "dt": p.dt,
+                   "form": "fp64", "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "working set larger than L2 (ELL values+columns 228 MB, cell records 252 MB)"},
+        "face_dof_per_s": value * F * n, "iterations_per_step": iters,
+        "hbm_gbs_step": bytes_step / (ms_step * 1e-3) / 1e9,
+        "hbm_frac_step": bytes_step / (ms_step * 1e-3) / 1e9 / hbm_peak,
+        "roofline": {"bound": "hbm", "kernel": "k_spmv_dot<double> (BiCGStab SpMV + dot)", "achieved": achieved,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
+                     "peak_kind": peak_kind, "bytes_per_launch": spmv["bytes"], "ms_per_launch": spmv["ms"]},
+        "kernels": kernels,
+        "forms": forms,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": gpu_launches,
+        "clocks": clk,
+    }
+    line["config"].pop("nnz")
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

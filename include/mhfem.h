@@ -1,0 +1,235 @@
+/*
+ * mhfem.h - C ABI of the GB300-native MHFEM time-step library.
+ *
+ * The library implements the per-time-step hot path of TNL-MHFEM's CUDA
+ * solver (TNL::MHFEM::Solver<Model, BoundaryModel, Matrix>, Solver.h:28-210)
+ * on one GPU: local RT0 mass-matrix update, upwinding, local condensation,
+ * in-place assembly of the hybridized face-trace system, its BiCGStab solve
+ * and the reconstruction of the cell averages.  The reference's plugin API is
+ * compile-time C++ (a Model class derived from BaseModel plus a
+ * BoundaryModel); this header is the run-time C equivalent a maintainer binds
+ * from C, C++, ctypes or any other FFI.
+ *
+ * Conventions
+ *  - Every function returns an mhfem_status; mhfem_last_error() gives a
+ *    message for the last failure on a handle.
+ *  - All pointers are HOST pointers owned by the caller; the library owns
+ *    all device memory.  A handle is not thread-safe; it uses one CUDA
+ *    stream of its own.
+ *  - Indices are int32 (examples/config.h:1-7: Index = int); reals are
+ *    double (Real = double).
+ *  - Array layouts follow the reference's CUDA permutations
+ *    (BaseModel.h:18-125): per-cell arrays have the cell index K innermost,
+ *    e.g. D_ijK at ((i*n + j)*C + K), a_ijKe at (((i*n + j)*f + e)*C + K),
+ *    w_iKe at ((i*f + e)*C + K), m_iK at (i*C + K).  Face traces Z_iF are
+ *    face-major: (E*n + i), which is also the DOF / row index
+ *    (BaseModel.h:252-263).  Boundary-condition arrays are component-major:
+ *    (i*F + E) (BoundaryModels/Stationary.h:21-36).
+ */
+#ifndef MHFEM_H
+#define MHFEM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t mhfem_status;
+#define MHFEM_OK                        0
+#define MHFEM_ERR_INVALID_ARGUMENT      1
+#define MHFEM_ERR_STATE                 2   /* call made out of order */
+#define MHFEM_ERR_CUDA                  3
+#define MHFEM_ERR_NOT_CONVERGED         4   /* Solver.hpp:1259-1264 */
+#define MHFEM_ERR_BREAKDOWN             5   /* Krylov breakdown (zero inner product) */
+#define MHFEM_ERR_NONPOSITIVE_DIAGONAL  6   /* LinearSystem.h:153, BoundaryConditions.hpp:181 */
+#define MHFEM_ERR_NO_DEVICE             7
+#define MHFEM_ERR_OUT_OF_MEMORY         8
+#define MHFEM_ERR_NOT_FINITE            9   /* NaN / Inf met in the solve */
+#define MHFEM_ERR_TIMEOUT              10   /* host wall-clock limit on a solve */
+#define MHFEM_ERR_UNSUPPORTED          11
+
+typedef struct mhfem_solver_s* mhfem_t;
+
+/* Advection discretization (BaseModel.h:12-16). */
+#define MHFEM_EXPLICIT_UPWIND 0
+#define MHFEM_IMPLICIT_UPWIND 1
+#define MHFEM_IMPLICIT_TRACE  2
+
+/* Solver forms. */
+#define MHFEM_FORM_FP64    0   /* plain FP64 BiCGStab (the reference's path)          */
+#define MHFEM_FORM_MIXED   1   /* FP32 inner BiCGStab + FP64 iterative refinement    */
+#define MHFEM_FORM_LEARNED 2   /* FP64 BiCGStab warm-started by the message-passing net */
+
+/* Boundary condition tags (BoundaryConditionsType.h:7-31). */
+#define MHFEM_BC_FIXED_VALUE              0
+#define MHFEM_BC_FIXED_FLUX               1
+#define MHFEM_BC_ADVECTIVE_OUTFLOW        2
+#define MHFEM_BC_FIXED_FLUX_NO_ADVECTION  3
+
+/* Coefficient identifiers (BaseModel.h:267-275 and HeatEquationModel.h:114-133). */
+#define MHFEM_COEF_N      0   /* (i,j,K)   */
+#define MHFEM_COEF_U      1   /* (i,j,e,K) */
+#define MHFEM_COEF_M      2   /* (i,K)     */
+#define MHFEM_COEF_D      3   /* (i,j,K)   isotropic D, as in the reference */
+#define MHFEM_COEF_W      4   /* (i,e,K)   */
+#define MHFEM_COEF_A      5   /* (i,j,e,K) */
+#define MHFEM_COEF_R      6   /* (i,j,K)   */
+#define MHFEM_COEF_F      7   /* (i,K)     */
+#define MHFEM_COEF_M_UPW  8   /* (E,i) upwinded mobility, a model input when mobility upwind is off */
+#define MHFEM_COEF_M_BND  9   /* (i*F+E) getBoundaryMobility value on inflow boundary faces */
+#define MHFEM_COEF_PSI   10   /* (K) spatial shape of the time-modulated source */
+
+/* Arrays readable with mhfem_get_array. */
+#define MHFEM_ARRAY_B       0  /* b_ijK_storage (i,j,s,K) */
+#define MHFEM_ARRAY_R_IJKE  1  /* Q^-1 R_ijKe (i,j,e,K)   */
+#define MHFEM_ARRAY_R_IK    2  /* Q^-1 R_iK (i,K)         */
+#define MHFEM_ARRAY_M_UPW   3  /* m_iE_upw (E,i)          */
+#define MHFEM_ARRAY_Z_UPW   4  /* Z_ijE_upw (E,j,i)       */
+#define MHFEM_ARRAY_V       5  /* v_iKe (i,e,K)           */
+#define MHFEM_ARRAY_RHS     6  /* scaled right-hand side, rows E*n+i */
+
+typedef struct {
+    int32_t dim;              /* 2: triangles, 3: tetrahedra (examples/config.h:17-21) */
+    int32_t n_eq;             /* NumberOfEquations, 1 or 2 */
+    int32_t mass_lumping;     /* MassLumping::enabled = 1 (MassMatrix.h:16-19) */
+    int32_t advection;        /* MHFEM_*_UPWIND / MHFEM_IMPLICIT_TRACE */
+    int32_t mobility_upwind;  /* Model::do_mobility_upwind (BaseModel.h:160-161) */
+    int32_t form;             /* MHFEM_FORM_* */
+    int32_t device;           /* CUDA device ordinal */
+} mhfem_desc;
+
+typedef struct {
+    double  tol;              /* convergence-residue: relative residual ||b-Ax||/||b|| */
+    int32_t max_iter;         /* max-iterations of the Krylov solver */
+    double  inner_tol;        /* mixed form: relative tolerance of each FP32 sweep */
+    int32_t max_sweeps;       /* mixed form: cap on refinement sweeps */
+    int32_t check_every;      /* Krylov iterations between host convergence checks */
+    double  timeout_s;        /* host wall-clock limit of one solve (<= 0: none) */
+} mhfem_solver_opts;
+
+typedef struct {
+    int32_t iterations;       /* Krylov iterations (mixed: FP32 inner iterations, summed) */
+    int32_t sweeps;           /* refinement sweeps (mixed form), else 1 */
+    double  residual;         /* final relative residual in FP64 */
+    int32_t guess_used;       /* learned form: 1 if the predicted initial guess was accepted */
+    double  guess_residual;   /* learned form: relative residual of the predicted guess */
+    double  warm_residual;    /* relative residual of the previous-step warm start */
+    double  ms_pre, ms_assemble, ms_solve, ms_post;   /* device time per phase */
+} mhfem_step_stats;
+
+/* ---- lifecycle ---------------------------------------------------------- */
+
+/* Replaces constructing Solver<Model,...> with its compile-time static
+ * configuration (examples/config.h:1-61, examples/main.h:17). */
+mhfem_status mhfem_create(const mhfem_desc* desc, mhfem_t* out);
+mhfem_status mhfem_destroy(mhfem_t h);
+const char*  mhfem_last_error(mhfem_t h);
+void         mhfem_default_solver_opts(mhfem_solver_opts* opts);
+
+/* ---- setup -------------------------------------------------------------- */
+
+/* Replaces Solver::setMesh (Solver.hpp:28-80) after MHFEM::init loaded the
+ * mesh (control.h:15-47).  cell_verts is [C][dim+1]; local vertex e is
+ * opposite local face e (the convention MassMatrix.h:538 relies on).  The
+ * library numbers the faces in order of first appearance over the cells
+ * and their local faces. */
+mhfem_status mhfem_set_mesh(mhfem_t h, int64_t num_vertices, const double* coords,
+                            int64_t num_cells, const int32_t* cell_verts);
+
+/* Sizes: vertices, cells, faces, rows (n*F) and non-zeros of the face system. */
+mhfem_status mhfem_get_sizes(mhfem_t h, int64_t* V, int64_t* C, int64_t* F,
+                             int64_t* rows, int64_t* nnz);
+
+/* Topology as built (getCellsForFace / getFacesForCell, mesh_helpers.h:49-160):
+ * face_verts [F][dim] (sorted vertex ids), face_cells [F][2] (ascending, -1 on
+ * the boundary), cell_faces [C][dim+1].  Any pointer may be NULL. */
+mhfem_status mhfem_get_topology(mhfem_t h, int32_t* face_verts, int32_t* face_cells,
+                                int32_t* cell_faces);
+
+/* Replaces the model writing its coefficient arrays in Model::init
+ * (HeatEquationModel.h:114-133).  count == 1 gives a uniform coefficient
+ * (UniformCoefficient.h:8-52); otherwise count must equal the full size of
+ * the layout listed beside the MHFEM_COEF_* identifier. */
+mhfem_status mhfem_set_coeff(mhfem_t h, int32_t which, const double* data, int64_t count);
+
+/* Time-modulated source (a model hook of updateNonLinearTerms,
+ * Solver.hpp:616-625): before each step at time t,
+ *   f_iK = f_base_iK + amplitude * sin(2*pi*t/period) * psi_K,
+ * with f_base the MHFEM_COEF_F array and psi the MHFEM_COEF_PSI array.
+ * amplitude == 0 switches it off. */
+mhfem_status mhfem_set_source_modulation(mhfem_t h, double amplitude, double period);
+
+/* Replaces BoundaryConditions::init from a BoundaryConditionsStorage
+ * (BoundaryConditions.hpp:224-233; Solver.hpp:264-293).  Each array holds
+ * n*F entries, index i*F + E. */
+mhfem_status mhfem_set_bc(mhfem_t h, const uint8_t* tags, const double* values,
+                          const double* dirichlet_values);
+
+/* Replaces Solver::setInitialCondition (Solver.hpp:260-344): sets Z_iK
+ * ((i,K), n*C values) and initializes Z_iF as the average of the adjacent
+ * cells (Solver.hpp:319-339) and v_iKe = 0. */
+mhfem_status mhfem_set_initial_condition(mhfem_t h, const double* Z_iK);
+
+/* Sets both state arrays explicitly (restart). Z_iF may be NULL: face average. */
+mhfem_status mhfem_set_state(mhfem_t h, const double* Z_iK, const double* Z_iF);
+
+/* Replaces Solver::setup's solver selection (Solver.hpp:88-258) and the
+ * iterative-solver keys of configSetup.h:32-62. */
+mhfem_status mhfem_set_solver(mhfem_t h, const mhfem_solver_opts* opts);
+
+/* Replaces Solver::setupLinearSystem (Solver.hpp:351-484): builds the fixed
+ * sparsity pattern of the face system from the topology and the BC tags. */
+mhfem_status mhfem_setup_linear_system(mhfem_t h);
+
+/* ---- one time step (control.h:83-98) ------------------------------------ */
+
+mhfem_status mhfem_pre_iterate(mhfem_t h, double t, double tau);     /* Solver.hpp:596-892  */
+mhfem_status mhfem_assemble(mhfem_t h, double t, double tau);        /* Solver.hpp:894-962  */
+mhfem_status mhfem_solve(mhfem_t h, mhfem_step_stats* stats);        /* Solver.hpp:979-1266 */
+mhfem_status mhfem_post_iterate(mhfem_t h, double t, double tau);    /* Solver.hpp:1268-1324 */
+/* All four phases; stats may be NULL. */
+mhfem_status mhfem_step(mhfem_t h, double t, double tau, mhfem_step_stats* stats);
+
+/* ---- results ------------------------------------------------------------ */
+
+/* Z_iF (n*F, (E,i)) and Z_iK (n*C, (i,K)); either may be NULL. */
+mhfem_status mhfem_get_state(mhfem_t h, double* Z_iF, double* Z_iK);
+mhfem_status mhfem_get_array(mhfem_t h, int32_t which, double* out, int64_t count);
+
+/* The assembled system in CSR (rowptr has rows+1 entries), with the unit
+ * diagonal included, columns ascending in each row exactly as the
+ * reference's row setters emit them (LinearSystem.h:66-256,
+ * BoundaryConditions.hpp:132-222).  Any pointer may be NULL. */
+mhfem_status mhfem_get_system(mhfem_t h, int64_t* rowptr, int32_t* cols, double* vals,
+                              double* rhs);
+
+/* Cumulative counters as in Solver::writeEpilog (Solver.hpp:1326-1391),
+ * plus the number of kernels this library launched on the handle. */
+mhfem_status mhfem_get_totals(mhfem_t h, int64_t* iterations, int64_t* time_steps,
+                              int64_t* kernel_launches);
+
+/* ---- measurement (replaces the per-phase TNL::Timer of Solver.h:132-138) -- */
+
+/* The handle's CUDA stream (a cudaStream_t), so a caller can record CUDA
+ * events on the stream the kernels run on. */
+mhfem_status mhfem_get_stream(mhfem_t h, void** stream);
+
+/* Kernels that mhfem_time_kernel can time. */
+#define MHFEM_KERNEL_CELL_LOCAL   0   /* fused b / R / Q^-1 R / local Schur records */
+#define MHFEM_KERNEL_ASSEMBLE     1   /* face-row assembly */
+#define MHFEM_KERNEL_SPMV_FP64    2   /* BiCGStab SpMV fused with a dot product, FP64 */
+#define MHFEM_KERNEL_SPMV_FP32    3   /* the same in FP32 (mixed form) */
+#define MHFEM_KERNEL_RECONSTRUCT  4   /* Z_iK (and v_iKe) reconstruction */
+
+/* Times `reps` back-to-back launches of one kernel on the current system
+ * with CUDA events on the handle's stream (after a step has run) and returns
+ * the mean duration, the algorithmic bytes one launch must move (each array
+ * counted once at its size) and its FP64 (or FP32) operation count. */
+mhfem_status mhfem_time_kernel(mhfem_t h, int32_t kernel, int32_t reps, double* ms_per_launch,
+                               double* bytes_per_launch, double* flops_per_launch);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,72 @@
+"""Shared helpers: model variants and GPU-vs-oracle comparison."""
+from __future__ import annotations
+
+import copy
+
+import numpy as np
+
+from mhfem import _lib as L
+from mhfem import problems
+
+
+def rel_err(a, b) -> float:
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    scale = max(np.abs(b).max(initial=0.0), 1e-300)
+    return float(np.abs(a - b).max(initial=0.0) / scale)
+
+
+def variant(p: problems.Problem, **changes) -> problems.Problem:
+    q = copy.copy(p)
+    q.config = copy.copy(p.config)
+    q.coeffs = dict(p.coeffs)
+    for k, v in changes.items():
+        if hasattr(q.config, k):
+            setattr(q.config, k, v)
+        elif k == "coeffs":
+            q.coeffs.update(v)
+        else:
+            setattr(q, k, v)
+    return q
+
+
+def small_cases():
+    """Small models that together exercise every branch of the path."""
+    cases = {}
+    cases["heat2d"] = problems.heat2d(N=8, steps=3)
+    cases["diffusion3d"] = problems.diffusion3d(N=4, steps=3)
+    cases["adr2d"] = problems.adr2d(N=8, steps=3)
+    cases["diffusion3d_lumped"] = variant(problems.diffusion3d(N=4, steps=2), mass_lumping=True)
+    cases["heat2d_lumped"] = variant(problems.heat2d(N=8, steps=2), mass_lumping=True)
+    # mobility upwind with a heterogeneous mobility (K6 and K13 active)
+    p = problems.diffusion3d(N=4, steps=3)
+    rng = np.random.default_rng(7)
+    cases["diffusion3d_mobility"] = variant(p, mobility_upwind=True,
+                                            coeffs={"m": rng.uniform(0.5, 2.0, p.C), "m_bnd": 1.5})
+    p = problems.adr2d(N=8, steps=3)
+    cases["adr2d_implicit_upwind"] = variant(p, advection=L.IMPLICIT_UPWIND)
+    # the trace discretization needs a low cell Peclet number for a positive diagonal
+    cases["adr2d_implicit_trace"] = variant(p, advection=L.IMPLICIT_TRACE,
+                                            coeffs={"a": np.asarray(p.coeffs["a"]) * 0.02})
+    cases["adr2d_mobility"] = variant(p, mobility_upwind=True,
+                                      coeffs={"m": np.random.default_rng(3).uniform(0.5, 2.0, 2 * p.C)})
+    # two components on tetrahedra with coupled reaction and a full w field
+    p3 = problems.diffusion3d(N=3, steps=2)
+    C = p3.C
+    rng = np.random.default_rng(11)
+    Nc = np.zeros((2, 2, C)); Nc[0, 0] = 1.0; Nc[1, 1] = 2.0
+    D = np.zeros((2, 2, C)); D[0, 0] = p3.coeffs["D"]; D[1, 1] = 0.5 * p3.coeffs["D"]; D[0, 1] = 0.1
+    r = np.zeros((2, 2, C)); r[0, 0] = 0.3; r[0, 1] = -0.1; r[1, 0] = -0.1; r[1, 1] = 0.2
+    w = rng.uniform(-0.01, 0.01, (2, 4, C))
+    base_bc = p3.bc_fn
+
+    def bc2(fv, fc):
+        t, v, d = base_bc(fv, fc)
+        F = fc.shape[0]
+        return np.concatenate([t, t]), np.concatenate([v, v + 0.1 * (t == 1)]), np.concatenate([d + 0.2, d])
+
+    q = variant(p3, n_eq=2, coeffs={"N": Nc.ravel(), "D": D.ravel(), "r": r.ravel(), "w": w.ravel(), "f": 0.5})
+    q.bc_fn = bc2
+    q.Z0 = rng.uniform(0, 1, 2 * C)
+    cases["diffusion3d_n2"] = q
+    return cases

@@ -1,0 +1,168 @@
+"""GPU path vs the CPU oracle, through the C ABI (needs a GB300).
+
+Bars: topology, face numbering and the CSR pattern bit-exact; the local
+quantities and the assembled values within 1e-12 relative; face traces and
+cell averages within 1e-10 relative after each time step (both solves run
+to a relative residual of 1e-13 so the comparison measures the path, not the
+solver tolerance).
+"""
+import numpy as np
+import pytest
+
+from helpers import rel_err, small_cases
+from mhfem import _lib as L
+from mhfem import problems
+from oracle.oracle import OracleModel
+
+pytestmark = pytest.mark.gpu
+
+CASES = small_cases()
+TOL_LOCAL = 1e-12
+TOL_STATE = 1e-10
+
+
+def _pair(p, check_every=4):
+    p.tol = 1e-13
+    s = problems.make_solver(p, check_every=check_every)
+    m = OracleModel.from_problem(p)
+    return s, m
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_topology_bit_exact(name):
+    p = CASES[name]
+    s, m = _pair(p)
+    fv, fc, cf = s.topology()
+    assert np.array_equal(fv, m.face_verts)
+    assert np.array_equal(fc, m.face_cells)
+    assert np.array_equal(cf, m.cell_faces)
+    s.close()
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_step_parity(name):
+    p = CASES[name]
+    s, m = _pair(p)
+    n, C = p.n, p.C
+    nf = p.config.dim + 1
+    S = 9 if p.config.dim == 2 else 14
+    t = 0.0
+    for step in range(p.steps):
+        s.preIterate(t, p.dt)
+        s.assembleLinearSystem(t, p.dt)
+        m.pre_iterate(t, p.dt)
+        m.assemble(t, p.dt)
+        assert rel_err(s.array("b", n * n * S * C), m.b) < TOL_LOCAL
+        assert rel_err(s.array("R_ijKe", n * n * nf * C), m.R_ijKe) < TOL_LOCAL
+        assert rel_err(s.array("R_iK", n * C), m.R_iK) < TOL_LOCAL
+        rowptr, cols, vals, rhs = s.system()
+        assert np.array_equal(rowptr, m.rowptr), "CSR row pointers differ"
+        assert np.array_equal(cols, m.cols), "CSR column indices differ"
+        assert rel_err(vals, m.vals) < TOL_LOCAL
+        assert rel_err(rhs, m.rhs) < TOL_LOCAL
+        st = s.solveLinearSystem()
+        m.solve(1e-13)
+        s.postIterate(t, p.dt)
+        m.post_iterate(t, p.dt)
+        zf, zk = s.state()
+        assert rel_err(zf, m.Z_iF) < TOL_STATE, f"step {step}: Z_iF"
+        assert rel_err(zk, m.Z_iK) < TOL_STATE, f"step {step}: Z_iK"
+        if p.config.mobility_upwind:
+            assert rel_err(s.array("v_iKe", n * nf * C), m.v_iKe) < 1e-9
+            assert rel_err(s.array("m_upw", n * p_faces(s)), m.m_upw) < 1e-12
+        assert st["residual"] < 1e-13
+        t += p.dt
+    s.close()
+
+
+def p_faces(s):
+    return s.F
+
+
+def test_heat2d_full_size():
+    """The 128^2 triangle heat-equation workload, 3 steps at tol 1e-12."""
+    p = problems.heat2d(N=128, steps=3)
+    s, m = _pair(p)
+    assert s.F == 49408 and s.C == 32768
+    t = 0.0
+    for _ in range(p.steps):
+        s.step(t, p.dt)
+        m.step(t, p.dt, 1e-13)
+        t += p.dt
+    zf, zk = s.state()
+    assert rel_err(zf, m.Z_iF) < TOL_STATE
+    assert rel_err(zk, m.Z_iK) < TOL_STATE
+    rowptr, cols, _, _ = s.system()
+    assert np.array_equal(rowptr, m.rowptr) and np.array_equal(cols, m.cols)
+    s.close()
+
+
+def test_diffusion3d_full_size():
+    """The 64^3 tetrahedral heterogeneous-diffusion workload: 2 steps."""
+    p = problems.diffusion3d(N=64, steps=2)
+    s, m = _pair(p, check_every=8)
+    assert s.F == 3170304 and s.C == 1572864
+    t = 0.0
+    for _ in range(p.steps):
+        s.step(t, p.dt)
+        m.step(t, p.dt, 1e-13)
+        t += p.dt
+    zf, zk = s.state()
+    assert rel_err(zf, m.Z_iF) < TOL_STATE
+    assert rel_err(zk, m.Z_iK) < TOL_STATE
+    rowptr, cols, _, _ = s.system()
+    assert np.array_equal(rowptr, m.rowptr) and np.array_equal(cols, m.cols)
+    s.close()
+
+
+def test_mixed_precision_matches_fp64_oracle():
+    """FP32 inner BiCGStab + FP64 refinement to 1e-10: error vs the FP64 oracle."""
+    p = problems.diffusion3d(N=12, steps=3, form=L.FORM_MIXED)
+    s = problems.make_solver(p)
+    m = OracleModel.from_problem(p)
+    t = 0.0
+    for _ in range(p.steps):
+        st = s.step(t, p.dt)
+        m.step(t, p.dt, 1e-13)
+        assert st["sweeps"] >= 1 and st["residual"] < p.tol
+        t += p.dt
+    zf, zk = s.state()
+    assert rel_err(zf, m.Z_iF) < 1e-8
+    assert rel_err(zk, m.Z_iK) < 1e-8
+    s.close()
+
+
+def test_deterministic():
+    p = problems.diffusion3d(N=8, steps=2)
+    outs = []
+    for _ in range(2):
+        s = problems.make_solver(p)
+        t = 0.0
+        for _ in range(p.steps):
+            s.step(t, p.dt)
+            t += p.dt
+        outs.append(s.state())
+        s.close()
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+def test_not_converged_is_reported():
+    p = problems.diffusion3d(N=6, steps=1)
+    s = problems.make_solver(p)
+    s.setup(tol=1e-14, max_iter=1, check_every=1)
+    with pytest.raises(L.MhfemError) as ei:
+        s.step(0.0, p.dt)
+    assert ei.value.status == L.ERR_NOT_CONVERGED
+    s.close()
+
+
+def test_nan_coefficient_is_reported():
+    p = problems.diffusion3d(N=4, steps=1)
+    D = np.array(p.coeffs["D"], copy=True)
+    D[5] = np.nan
+    s = problems.make_solver(p)
+    s.set_coeff("D", D)
+    with pytest.raises(L.MhfemError) as ei:
+        s.step(0.0, p.dt)
+    assert ei.value.status in (L.ERR_NONPOSITIVE_DIAGONAL, L.ERR_NOT_FINITE)
+    s.close()

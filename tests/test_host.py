@@ -1,0 +1,80 @@
+"""Host-side checks that need no GPU: the C-ABI library loads, exports every
+symbol include/mhfem.h declares, refuses to run without a device, and the
+model builders reproduce the workload sizes."""
+import ctypes as ct
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from mhfem import _lib as L
+from mhfem import meshgen, problems
+from oracle.oracle import build_faces
+
+REPO = Path(__file__).resolve().parent.parent
+
+
+def _declared_symbols():
+    text = (REPO / "include" / "mhfem.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:mhfem_status|const char\*|void)\s+(mhfem_\w+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ct.CDLL(str(L.LIB_PATH))
+    declared = _declared_symbols()
+    assert len(declared) >= 20
+    for name in declared:
+        assert hasattr(lib, name), f"{name} declared in include/mhfem.h but not exported"
+    bound = {s[0] for s in L.SIGNATURES}
+    assert set(declared) == bound, "ctypes signatures out of sync with the header"
+
+
+def test_create_without_device_fails_loudly():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    lib = L.load()
+    desc = L.Desc(3, 1, 0, 0, 0, 0, 0)
+    h = ct.c_void_p()
+    assert lib.mhfem_create(ct.byref(desc), ct.byref(h)) == L.ERR_NO_DEVICE
+
+
+@pytest.mark.parametrize("N", [1, 3, 8])
+def test_triangle_mesh_counts(N):
+    coords, cells = meshgen.square_triangles(N)
+    fv, fc, cf = build_faces(2, cells)
+    assert cells.shape[0] == 2 * N * N
+    assert fv.shape[0] == 3 * N * N + 2 * N
+    assert int((fc[:, 1] < 0).sum()) == 4 * N
+
+
+@pytest.mark.parametrize("N", [1, 2, 5])
+def test_tetrahedron_mesh_counts(N):
+    coords, cells = meshgen.cube_tetrahedra(N)
+    fv, fc, cf = build_faces(3, cells)
+    assert cells.shape[0] == 6 * N ** 3
+    assert fv.shape[0] == 12 * N ** 3 + 6 * N ** 2
+    assert int((fc[:, 1] < 0).sum()) == 12 * N * N
+
+
+def test_mesh_cells_positive_measure():
+    for coords, cells in [meshgen.square_triangles(16), meshgen.cube_tetrahedra(6)]:
+        X = coords[cells]
+        E = X[:, 1:] - X[:, :1]
+        vol = np.abs(np.linalg.det(E))
+        assert vol.min() > 0.1 * vol.mean()
+
+
+def test_diffusion3d_workload_sizes():
+    """64^3 tetrahedra: C, F, boundary split as the workload states."""
+    p = problems.diffusion3d(N=64, steps=1)
+    assert p.C == 1572864
+    fv, fc, _ = build_faces(3, p.cells)
+    assert fv.shape[0] == 3170304
+    tags, _, _ = p.bc_fn(fv, fc)
+    bnd = fc[:, 1] < 0
+    assert int(bnd.sum()) == 49152
+    assert int((tags[bnd] == problems.BC_FIXED_VALUE).sum()) == 16384
+    assert int((tags[bnd] == problems.BC_FIXED_FLUX).sum()) == 32768

@@ -1,0 +1,918 @@
+// C ABI and host orchestration of one MHFEM solver instance (one GPU,
+// one CUDA stream).  Mirrors TNL::MHFEM::Solver (Solver.h:28-210) and the
+// time-step sequence of MHFEM::solve (control.h:64-102).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mhfem_internal.h"
+#include "topology.h"
+
+using namespace mhfem;
+
+namespace {
+
+constexpr int NCOEF = 11;
+
+struct DevCoef {
+    double* p = nullptr;
+    int64_t count = 0;  // 1 = uniform
+};
+
+}  // namespace
+
+struct mhfem_solver_s {
+    mhfem_desc desc{};
+    int dim = 0, nf = 0, n = 0, S = 0;
+    std::string err;
+    cudaStream_t stream = nullptr;
+    int sms = 0;
+
+    HostTopology topo;
+    HostPattern pat;
+    bool has_mesh = false, has_bc = false, has_state = false;
+    bool pattern_ready = false;
+    std::vector<uint8_t> h_tags;
+
+    // device topology
+    double* coords = nullptr;
+    int32_t* cell_verts = nullptr;   // SoA
+    int32_t* cell_faces = nullptr;   // SoA
+    uint8_t* cell_bmask = nullptr;
+    int2* face_cells = nullptr;
+    uint8_t* face_local = nullptr;
+    double* face_measure = nullptr;
+
+    DevCoef coef[NCOEF];
+    bool coef_nonzero[NCOEF] = {};
+    double src_amp = 0, src_period = 1;
+
+    uint8_t* tags = nullptr;
+    double* bvalues = nullptr;
+    double* bdirichlet = nullptr;
+
+    double *Z_iF = nullptr, *Z_iK = nullptr, *v_iKe = nullptr, *m_upw = nullptr, *Z_upw = nullptr;
+    double *b = nullptr, *R_ijKe = nullptr, *R_iK = nullptr, *rec = nullptr;
+    int rec_stride = 0;
+
+    EllMatrix A;
+    AssemblyMap amap;
+    double* rhs = nullptr;
+    int32_t* err_flags = nullptr;
+    int32_t* host_err = nullptr;
+    KrylovWork W;
+
+    mhfem_solver_opts opts{};
+    int64_t total_iters = 0, total_steps = 0, launches = 0;
+    double cur_t = 0, cur_tau = 0;
+
+    cudaGraphExec_t g64 = nullptr, g32 = nullptr;
+    int g64_iters = 0, g32_iters = 0;
+
+    cudaEvent_t ev[5] = {};
+    std::vector<void*> allocs;
+};
+
+namespace {
+
+mhfem_status fail(mhfem_t h, mhfem_status code, const char* fmt, ...)
+{
+    if (h) {
+        char buf[1024];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        h->err = buf;
+    }
+    return code;
+}
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return fail(h, e_ == cudaErrorMemoryAllocation ? MHFEM_ERR_OUT_OF_MEMORY : MHFEM_ERR_CUDA, \
+                        "%s failed: %s", #call, cudaGetErrorString(e_));                          \
+    } while (0)
+
+template <typename T>
+cudaError_t dalloc(mhfem_t h, T** p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * count);
+    if (e == cudaSuccess) h->allocs.push_back((void*)*p);
+    return e;
+}
+
+template <typename T>
+void dfree(mhfem_t h, T*& p)
+{
+    if (!p) return;
+    auto it = std::find(h->allocs.begin(), h->allocs.end(), (void*)p);
+    if (it != h->allocs.end()) h->allocs.erase(it);
+    cudaFree((void*)p);
+    p = nullptr;
+}
+
+int64_t coef_size(mhfem_t h, int which)
+{
+    const int64_t n = h->n, nf = h->nf, C = h->topo.C, F = h->topo.F;
+    switch (which) {
+        case MHFEM_COEF_N: case MHFEM_COEF_D: case MHFEM_COEF_R: return n * n * C;
+        case MHFEM_COEF_U: case MHFEM_COEF_A: return n * n * nf * C;
+        case MHFEM_COEF_M: case MHFEM_COEF_F: return n * C;
+        case MHFEM_COEF_W: return n * nf * C;
+        case MHFEM_COEF_M_UPW: return F * n;
+        case MHFEM_COEF_M_BND: return n * F;
+        case MHFEM_COEF_PSI: return C;
+    }
+    return -1;
+}
+
+mhfem_status set_coef_device(mhfem_t h, int which, const double* data, int64_t count)
+{
+    if (h->coef[which].count != count || !h->coef[which].p) {
+        dfree(h, h->coef[which].p);
+        CK(dalloc(h, &h->coef[which].p, (size_t)count));
+    }
+    CK(cudaMemcpyAsync(h->coef[which].p, data, sizeof(double) * count, cudaMemcpyHostToDevice, h->stream));
+    h->coef[which].count = count;
+    bool nz = false;
+    for (int64_t q = 0; q < count && !nz; ++q) nz = (data[q] != 0.0);
+    h->coef_nonzero[which] = nz;
+    CK(cudaStreamSynchronize(h->stream));
+    return MHFEM_OK;
+}
+
+Coef as_coef(const DevCoef& c) { return Coef{c.p, c.count > 1 ? 1 : 0}; }
+
+void invalidate_graphs(mhfem_t h)
+{
+    if (h->g64) cudaGraphExecDestroy(h->g64);
+    if (h->g32) cudaGraphExecDestroy(h->g32);
+    h->g64 = h->g32 = nullptr;
+    h->g64_iters = h->g32_iters = 0;
+}
+
+DevProblem make_problem(mhfem_t h)
+{
+    DevProblem P{};
+    P.dim = h->dim; P.nf = h->nf; P.n = h->n; P.S = h->S;
+    P.lumping = h->desc.mass_lumping;
+    P.advection = h->desc.advection;
+    P.mobility_upwind = h->desc.mobility_upwind;
+    P.V = h->topo.V; P.C = h->topo.C; P.F = h->topo.F; P.rows = h->topo.F * h->n;
+    P.coords = h->coords;
+    P.cell_verts = h->cell_verts;
+    P.cell_faces = h->cell_faces;
+    P.cell_bmask = h->cell_bmask;
+    P.face_cells = h->face_cells;
+    P.face_local = h->face_local;
+    P.face_measure = h->face_measure;
+    P.N = as_coef(h->coef[MHFEM_COEF_N]);
+    P.u = as_coef(h->coef[MHFEM_COEF_U]);
+    P.m = as_coef(h->coef[MHFEM_COEF_M]);
+    P.D = as_coef(h->coef[MHFEM_COEF_D]);
+    P.w = as_coef(h->coef[MHFEM_COEF_W]);
+    P.a = as_coef(h->coef[MHFEM_COEF_A]);
+    P.r = as_coef(h->coef[MHFEM_COEF_R]);
+    P.f = as_coef(h->coef[MHFEM_COEF_F]);
+    P.m_upw_in = as_coef(h->coef[MHFEM_COEF_M_UPW]);
+    P.m_bnd = as_coef(h->coef[MHFEM_COEF_M_BND]);
+    P.psi = (h->src_amp != 0 && h->coef[MHFEM_COEF_PSI].p) ? as_coef(h->coef[MHFEM_COEF_PSI]) : Coef{};
+    P.src_amp = h->src_amp;
+    P.src_omega = 2.0 * M_PI / h->src_period;
+    P.src_time = h->cur_t;
+    P.bc_tags = h->tags;
+    P.bc_values = h->bvalues;
+    P.bc_dirichlet = h->bdirichlet;
+    P.Z_iF = h->Z_iF; P.Z_iK = h->Z_iK; P.v_iKe = h->v_iKe;
+    P.m_upw = h->m_upw; P.Z_upw = h->Z_upw;
+    P.b = h->b; P.R_ijKe = h->R_ijKe; P.R_iK = h->R_iK;
+    P.rec = h->rec; P.rec_stride = h->rec_stride;
+    if (h->desc.mobility_upwind) { P.use_m_upw_array = 1; P.m_upw_read = h->m_upw; }
+    else if (h->coef[MHFEM_COEF_M_UPW].count > 1) { P.use_m_upw_array = 1; P.m_upw_read = h->coef[MHFEM_COEF_M_UPW].p; }
+    else { P.use_m_upw_array = 0; P.m_upw_read = nullptr; }
+    P.explicit_adv_active = (h->desc.advection == MHFEM_EXPLICIT_UPWIND) &&
+                            (h->coef_nonzero[MHFEM_COEF_A] || h->coef_nonzero[MHFEM_COEF_U]);
+    P.err_flags = h->err_flags;
+    return P;
+}
+
+mhfem_status require_ready(mhfem_t h)
+{
+    if (!h) return MHFEM_ERR_INVALID_ARGUMENT;
+    if (!h->has_mesh) return fail(h, MHFEM_ERR_STATE, "mhfem_set_mesh has not been called");
+    return MHFEM_OK;
+}
+
+mhfem_status ensure_pattern(mhfem_t h);
+
+}  // namespace
+
+extern "C" {
+
+void mhfem_default_solver_opts(mhfem_solver_opts* o)
+{
+    if (!o) return;
+    o->tol = 1e-10;
+    o->max_iter = 10000;
+    o->inner_tol = 1e-4;
+    o->max_sweeps = 50;
+    o->check_every = 8;
+    o->timeout_s = 0;
+}
+
+mhfem_status mhfem_create(const mhfem_desc* desc, mhfem_t* out)
+{
+    if (!desc || !out) return MHFEM_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (desc->dim != 2 && desc->dim != 3) return MHFEM_ERR_INVALID_ARGUMENT;
+    if (desc->n_eq < 1 || desc->n_eq > 2) return MHFEM_ERR_UNSUPPORTED;
+    if (desc->advection < 0 || desc->advection > 2) return MHFEM_ERR_INVALID_ARGUMENT;
+    if (desc->form < 0 || desc->form > 2) return MHFEM_ERR_INVALID_ARGUMENT;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return MHFEM_ERR_NO_DEVICE;
+    if (desc->device < 0 || desc->device >= ndev) return MHFEM_ERR_NO_DEVICE;
+    if (cudaSetDevice(desc->device) != cudaSuccess) return MHFEM_ERR_NO_DEVICE;
+    mhfem_t h = new mhfem_solver_s();
+    h->desc = *desc;
+    h->dim = desc->dim;
+    h->nf = desc->dim + 1;
+    h->n = desc->n_eq;
+    h->S = (desc->dim == 2) ? 9 : 14;
+    mhfem_default_solver_opts(&h->opts);
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete h;
+        return MHFEM_ERR_CUDA;
+    }
+    for (auto& e : h->ev) cudaEventCreate(&e);
+    cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, desc->device);
+    cudaMallocHost((void**)&h->W.host_sc, sizeof(KrylovScalars) * 2);
+    cudaMallocHost((void**)&h->host_err, sizeof(int32_t));
+    *out = h;
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_destroy(mhfem_t h)
+{
+    if (!h) return MHFEM_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(h->desc.device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    invalidate_graphs(h);
+    for (void* p : h->allocs) cudaFree(p);
+    h->allocs.clear();
+    if (h->W.host_sc) cudaFreeHost(h->W.host_sc);
+    if (h->host_err) cudaFreeHost(h->host_err);
+    for (auto& e : h->ev)
+        if (e) cudaEventDestroy(e);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return MHFEM_OK;
+}
+
+const char* mhfem_last_error(mhfem_t h)
+{
+    if (!h) return "invalid handle";
+    return h->err.c_str();
+}
+
+mhfem_status mhfem_set_mesh(mhfem_t h, int64_t V, const double* coords, int64_t C, const int32_t* cell_verts)
+{
+    if (!h || !coords || !cell_verts || V <= 0 || C <= 0) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "invalid mesh arguments");
+    cudaSetDevice(h->desc.device);
+    std::string msg = build_topology(h->dim, V, coords, C, cell_verts, h->topo);
+    if (!msg.empty()) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "%s", msg.c_str());
+    const int nf = h->nf, n = h->n;
+    const int64_t F = h->topo.F;
+    // release everything that depends on the mesh
+    invalidate_graphs(h);
+    for (void* p : h->allocs) cudaFree(p);
+    h->allocs.clear();
+    h->coords = nullptr; h->cell_verts = h->cell_faces = nullptr; h->cell_bmask = nullptr;
+    h->face_cells = nullptr; h->face_local = nullptr; h->face_measure = nullptr;
+    for (auto& c : h->coef) c = DevCoef();
+    h->tags = nullptr; h->bvalues = h->bdirichlet = nullptr;
+    h->Z_iF = h->Z_iK = h->v_iKe = h->m_upw = h->Z_upw = h->b = h->R_ijKe = h->R_iK = h->rec = nullptr;
+    h->A = EllMatrix(); h->amap = AssemblyMap(); h->rhs = nullptr; h->err_flags = nullptr;
+    KrylovScalars* keep = h->W.host_sc;
+    h->W = KrylovWork();
+    h->W.host_sc = keep;
+    h->pattern_ready = false;
+    h->has_bc = h->has_state = false;
+
+    // topology on the device, SoA with the cell index innermost
+    std::vector<int32_t> soa((size_t)C * nf);
+    CK(dalloc(h, &h->coords, (size_t)V * h->dim));
+    CK(cudaMemcpy(h->coords, coords, sizeof(double) * V * h->dim, cudaMemcpyHostToDevice));
+    for (int64_t K = 0; K < C; ++K)
+        for (int v = 0; v < nf; ++v) soa[(size_t)v * C + K] = cell_verts[K * nf + v];
+    CK(dalloc(h, &h->cell_verts, (size_t)C * nf));
+    CK(cudaMemcpy(h->cell_verts, soa.data(), sizeof(int32_t) * C * nf, cudaMemcpyHostToDevice));
+    for (int64_t K = 0; K < C; ++K)
+        for (int e = 0; e < nf; ++e) soa[(size_t)e * C + K] = h->topo.cell_faces[K * nf + e];
+    CK(dalloc(h, &h->cell_faces, (size_t)C * nf));
+    CK(cudaMemcpy(h->cell_faces, soa.data(), sizeof(int32_t) * C * nf, cudaMemcpyHostToDevice));
+    CK(dalloc(h, &h->cell_bmask, (size_t)C));
+    CK(cudaMemcpy(h->cell_bmask, h->topo.cell_bmask.data(), C, cudaMemcpyHostToDevice));
+    CK(dalloc(h, &h->face_cells, (size_t)F));
+    CK(cudaMemcpy(h->face_cells, h->topo.face_cells.data(), sizeof(int2) * F, cudaMemcpyHostToDevice));
+    CK(dalloc(h, &h->face_local, (size_t)2 * F));
+    CK(cudaMemcpy(h->face_local, h->topo.face_local.data(), 2 * F, cudaMemcpyHostToDevice));
+    CK(dalloc(h, &h->face_measure, (size_t)F));
+    CK(cudaMemcpy(h->face_measure, h->topo.face_measure.data(), sizeof(double) * F, cudaMemcpyHostToDevice));
+
+    // scheme arrays (BaseModel::allocate, BaseModel.h:168-195)
+    CK(dalloc(h, &h->Z_iF, (size_t)n * F));
+    CK(dalloc(h, &h->Z_iK, (size_t)n * C));
+    CK(dalloc(h, &h->b, (size_t)n * n * h->S * C));
+    CK(dalloc(h, &h->R_ijKe, (size_t)n * n * nf * C));
+    CK(dalloc(h, &h->R_iK, (size_t)n * C));
+    if (h->desc.mobility_upwind) {
+        CK(dalloc(h, &h->m_upw, (size_t)n * F));
+        CK(dalloc(h, &h->v_iKe, (size_t)n * nf * C));
+        CK(cudaMemset(h->v_iKe, 0, sizeof(double) * n * nf * C));
+    }
+    if (h->desc.advection == MHFEM_EXPLICIT_UPWIND) {
+        CK(dalloc(h, &h->Z_upw, (size_t)n * n * F));
+        CK(cudaMemset(h->Z_upw, 0, sizeof(double) * n * n * F));
+    }
+    h->rec_stride = ((n * nf + 1) + 1) & ~1;
+    CK(dalloc(h, &h->rec, (size_t)C * nf * n * h->rec_stride));
+    CK(dalloc(h, &h->err_flags, 1));
+    CK(cudaMemset(h->err_flags, 0, sizeof(int32_t)));
+    CK(cudaMemset(h->Z_iK, 0, sizeof(double) * n * C));
+    CK(cudaMemset(h->Z_iF, 0, sizeof(double) * n * F));
+
+    // default coefficients: the heat-equation model (HeatEquationModel.h:114-133)
+    h->has_mesh = true;
+    const double one = 1.0, zero = 0.0;
+    mhfem_status st;
+    const int ones[] = {MHFEM_COEF_N, MHFEM_COEF_M, MHFEM_COEF_D, MHFEM_COEF_M_UPW, MHFEM_COEF_M_BND};
+    const int zeros[] = {MHFEM_COEF_U, MHFEM_COEF_W, MHFEM_COEF_A, MHFEM_COEF_R, MHFEM_COEF_F};
+    for (int w : ones)
+        if ((st = set_coef_device(h, w, &one, 1)) != MHFEM_OK) return st;
+    for (int w : zeros)
+        if ((st = set_coef_device(h, w, &zero, 1)) != MHFEM_OK) return st;
+    // default boundary conditions: zero Dirichlet everywhere (Solver.hpp:282-293)
+    std::vector<uint8_t> t0((size_t)n * F, MHFEM_BC_FIXED_VALUE);
+    std::vector<double> v0((size_t)n * F, 0.0);
+    if ((st = mhfem_set_bc(h, t0.data(), v0.data(), v0.data())) != MHFEM_OK) return st;
+    h->has_bc = false;  // defaults only
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_get_sizes(mhfem_t h, int64_t* V, int64_t* C, int64_t* F, int64_t* rows, int64_t* nnz)
+{
+    mhfem_status st = require_ready(h);
+    if (st) return st;
+    if (V) *V = h->topo.V;
+    if (C) *C = h->topo.C;
+    if (F) *F = h->topo.F;
+    if (rows) *rows = h->topo.F * h->n;
+    if (nnz) {
+        if ((st = ensure_pattern(h)) != MHFEM_OK) return st;
+        *nnz = h->pat.nnz;
+    }
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_get_topology(mhfem_t h, int32_t* face_verts, int32_t* face_cells, int32_t* cell_faces)
+{
+    mhfem_status st = require_ready(h);
+    if (st) return st;
+    if (face_verts) std::memcpy(face_verts, h->topo.face_verts.data(), sizeof(int32_t) * h->topo.face_verts.size());
+    if (face_cells) std::memcpy(face_cells, h->topo.face_cells.data(), sizeof(int32_t) * h->topo.face_cells.size());
+    if (cell_faces) std::memcpy(cell_faces, h->topo.cell_faces.data(), sizeof(int32_t) * h->topo.cell_faces.size());
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_set_coeff(mhfem_t h, int32_t which, const double* data, int64_t count)
+{
+    mhfem_status st = require_ready(h);
+    if (st) return st;
+    if (which < 0 || which >= NCOEF || !data) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "invalid coefficient id %d", which);
+    const int64_t full = coef_size(h, which);
+    if (count != 1 && count != full)
+        return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "coefficient %d: expected 1 or %lld values, got %lld", which,
+                    (long long)full, (long long)count);
+    if (which == MHFEM_COEF_PSI && count != full)
+        return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "psi must be a full per-cell array");
+    cudaSetDevice(h->desc.device);
+    return set_coef_device(h, which, data, count);
+}
+
+mhfem_status mhfem_set_source_modulation(mhfem_t h, double amplitude, double period)
+{
+    mhfem_status st = require_ready(h);
+    if (st) return st;
+    if (!(period > 0)) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "period must be positive");
+    if (amplitude != 0 && !h->coef[MHFEM_COEF_PSI].p)
+        return fail(h, MHFEM_ERR_STATE, "set MHFEM_COEF_PSI before enabling the source modulation");
+    h->src_amp = amplitude;
+    h->src_period = period;
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_set_bc(mhfem_t h, const uint8_t* tags, const double* values, const double* dirichlet)
+{
+    mhfem_status st = require_ready(h);
+    if (st) return st;
+    if (!tags || !values || !dirichlet) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "null boundary arrays");
+    const int64_t count = h->topo.F * h->n;
+    for (int64_t q = 0; q < count; ++q)
+        if (tags[q] > 3) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "unknown boundary condition tag %d at %lld", tags[q], (long long)q);
+    cudaSetDevice(h->desc.device);
+    if (!h->tags) {
+        CK(dalloc(h, &h->tags, (size_t)count));
+        CK(dalloc(h, &h->bvalues, (size_t)count));
+        CK(dalloc(h, &h->bdirichlet, (size_t)count));
+    }
+    const bool same = h->h_tags.size() == (size_t)count && std::memcmp(h->h_tags.data(), tags, count) == 0;
+    h->h_tags.assign(tags, tags + count);
+    CK(cudaMemcpy(h->tags, tags, count, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->bvalues, values, sizeof(double) * count, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->bdirichlet, dirichlet, sizeof(double) * count, cudaMemcpyHostToDevice));
+    if (!same) h->pattern_ready = false;
+    h->has_bc = true;
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_set_initial_condition(mhfem_t h, const double* Z_iK)
+{
+    return mhfem_set_state(h, Z_iK, nullptr);
+}
+
+mhfem_status mhfem_set_state(mhfem_t h, const double* Z_iK, const double* Z_iF)
+{
+    mhfem_status st = require_ready(h);
+    if (st) return st;
+    if (!Z_iK) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "Z_iK is null");
+    cudaSetDevice(h->desc.device);
+    CK(cudaMemcpyAsync(h->Z_iK, Z_iK, sizeof(double) * h->n * h->topo.C, cudaMemcpyHostToDevice, h->stream));
+    if (Z_iF) {
+        CK(cudaMemcpyAsync(h->Z_iF, Z_iF, sizeof(double) * h->n * h->topo.F, cudaMemcpyHostToDevice, h->stream));
+    }
+    else {
+        DevProblem P = make_problem(h);
+        h->launches += launch_face_average(P, h->stream);
+        CK(cudaGetLastError());
+    }
+    if (h->v_iKe) CK(cudaMemsetAsync(h->v_iKe, 0, sizeof(double) * h->n * h->nf * h->topo.C, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->has_state = true;
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_set_solver(mhfem_t h, const mhfem_solver_opts* o)
+{
+    if (!h || !o) return MHFEM_ERR_INVALID_ARGUMENT;
+    if (!(o->tol > 0) || o->max_iter < 1 || o->check_every < 1 || !(o->inner_tol > 0) || o->max_sweeps < 1)
+        return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "invalid solver options");
+    const bool regraph = (o->check_every != h->opts.check_every);
+    h->opts = *o;
+    if (regraph) invalidate_graphs(h);
+    return MHFEM_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+mhfem_status ensure_pattern(mhfem_t h)
+{
+    if (h->pattern_ready) return MHFEM_OK;
+    cudaSetDevice(h->desc.device);
+    invalidate_graphs(h);
+    const int n = h->n;
+    const int64_t F = h->topo.F, rows = F * n;
+    build_pattern(h->topo, n, h->h_tags.data(), h->pat);
+    for (int64_t r = 0; r < rows; ++r)
+        if (h->pat.row_len[r] <= 0)  // Solver.hpp:467-474
+            return fail(h, MHFEM_ERR_STATE, "invalid row length at row %lld", (long long)r);
+    dfree(h, h->A.cols);
+    dfree(h, h->A.vals);
+    dfree(h, h->A.vals32);
+    dfree(h, h->amap.qmap);
+    dfree(h, h->amap.qdiag);
+    dfree(h, h->rhs);
+    const int W = h->pat.W;
+    h->A.rows = rows;
+    h->A.width = W;
+    CK(dalloc(h, &h->A.cols, (size_t)W * rows));
+    CK(cudaMemcpy(h->A.cols, h->pat.ell_cols.data(), sizeof(int32_t) * W * rows, cudaMemcpyHostToDevice));
+    CK(dalloc(h, &h->A.vals, (size_t)W * rows));
+    CK(cudaMemset(h->A.vals, 0, sizeof(double) * W * rows));
+    if (h->desc.form == MHFEM_FORM_MIXED) {
+        CK(dalloc(h, &h->A.vals32, (size_t)W * rows));
+        CK(cudaMemset(h->A.vals32, 0, sizeof(float) * W * rows));
+    }
+    CK(dalloc(h, &h->amap.qmap, (size_t)F));
+    CK(cudaMemcpy(h->amap.qmap, h->pat.qmap.data(), sizeof(uint32_t) * F, cudaMemcpyHostToDevice));
+    CK(dalloc(h, &h->amap.qdiag, (size_t)F));
+    CK(cudaMemcpy(h->amap.qdiag, h->pat.qdiag.data(), F, cudaMemcpyHostToDevice));
+    CK(dalloc(h, &h->rhs, (size_t)rows));
+    CK(cudaMemset(h->rhs, 0, sizeof(double) * rows));
+
+    // Krylov workspace (7 vectors as in Solver::estimateMemoryDemands, Solver.hpp:1424-1425)
+    KrylovWork& Wk = h->W;
+    dfree(h, Wk.r); dfree(h, Wk.rh); dfree(h, Wk.p); dfree(h, Wk.v); dfree(h, Wk.s); dfree(h, Wk.t);
+    dfree(h, Wk.r32); dfree(h, Wk.rh32); dfree(h, Wk.p32); dfree(h, Wk.v32); dfree(h, Wk.s32); dfree(h, Wk.t32);
+    dfree(h, Wk.x32); dfree(h, Wk.partials); dfree(h, Wk.counters); dfree(h, Wk.sc); dfree(h, Wk.sc32);
+    Wk.rows = rows;
+    Wk.grid = krylov_grid();
+    CK(dalloc(h, &Wk.r, (size_t)rows)); CK(dalloc(h, &Wk.rh, (size_t)rows)); CK(dalloc(h, &Wk.p, (size_t)rows));
+    CK(dalloc(h, &Wk.v, (size_t)rows)); CK(dalloc(h, &Wk.s, (size_t)rows)); CK(dalloc(h, &Wk.t, (size_t)rows));
+    if (h->desc.form == MHFEM_FORM_MIXED) {
+        CK(dalloc(h, &Wk.r32, (size_t)rows)); CK(dalloc(h, &Wk.rh32, (size_t)rows)); CK(dalloc(h, &Wk.p32, (size_t)rows));
+        CK(dalloc(h, &Wk.v32, (size_t)rows)); CK(dalloc(h, &Wk.s32, (size_t)rows)); CK(dalloc(h, &Wk.t32, (size_t)rows));
+        CK(dalloc(h, &Wk.x32, (size_t)rows));
+    }
+    CK(dalloc(h, &Wk.partials, (size_t)Wk.grid * 4));
+    CK(dalloc(h, &Wk.counters, (size_t)4));
+    CK(cudaMemset(Wk.counters, 0, sizeof(uint32_t) * 4));
+    CK(dalloc(h, &Wk.sc, (size_t)1));
+    CK(dalloc(h, &Wk.sc32, (size_t)1));
+    CK(cudaMemset(Wk.sc, 0, sizeof(KrylovScalars)));
+    CK(cudaMemset(Wk.sc32, 0, sizeof(KrylovScalars)));
+    h->pattern_ready = true;
+    return MHFEM_OK;
+}
+
+// Captures `iters` Krylov iterations plus the read-back of the device
+// scalars as one CUDA graph (replayed between host convergence checks).
+mhfem_status build_graph(mhfem_t h, bool fp32, int iters)
+{
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    if (fp32) {
+        krylov_iterate_fp32(h->A, h->W, iters, h->stream);
+        cudaMemcpyAsync(h->W.host_sc + 1, h->W.sc32, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, h->stream);
+    }
+    else {
+        krylov_iterate_fp64(h->A, h->Z_iF, h->W, iters, h->stream);
+        cudaMemcpyAsync(h->W.host_sc, h->W.sc, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, h->stream);
+    }
+    CK(cudaStreamEndCapture(h->stream, &g));
+    cudaGraphExec_t ex = nullptr;
+    cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(h, MHFEM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    if (fp32) { h->g32 = ex; h->g32_iters = iters; }
+    else { h->g64 = ex; h->g64_iters = iters; }
+    return MHFEM_OK;
+}
+
+mhfem_status status_from_krylov(mhfem_t h, const KrylovScalars& s, const char* what)
+{
+    switch (s.status) {
+        case KS_CONVERGED: return MHFEM_OK;
+        case KS_MAXITER:
+            return fail(h, MHFEM_ERR_NOT_CONVERGED,
+                        "MHFEM error: the linear system solver did not converge (%d iterations, %s, residual %.3e)",
+                        s.it, what, s.res);
+        case KS_BREAKDOWN: return fail(h, MHFEM_ERR_BREAKDOWN, "%s: BiCGStab breakdown after %d iterations", what, s.it);
+        case KS_NOTFINITE: return fail(h, MHFEM_ERR_NOT_FINITE, "%s: non-finite value after %d iterations", what, s.it);
+    }
+    return fail(h, MHFEM_ERR_STATE, "%s: unexpected Krylov status %d", what, s.status);
+}
+
+double elapsed_s(std::chrono::steady_clock::time_point t0)
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// Runs FP64 BiCGStab from the current Z_iF until the device flag says done.
+mhfem_status run_fp64(mhfem_t h, double tol, int max_iter, int* iters, double* res)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    krylov_init_fp64(h->A, h->rhs, h->Z_iF, h->W, tol, max_iter, h->stream);
+    CK(cudaMemcpyAsync(h->W.host_sc, h->W.sc, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaGetLastError());
+    if (!h->g64) {
+        mhfem_status st = build_graph(h, false, h->opts.check_every);
+        if (st) return st;
+    }
+    h->launches += 1;
+    while (!h->W.host_sc->done) {
+        CK(cudaGraphLaunch(h->g64, h->stream));
+        h->launches += 5 * h->g64_iters;
+        CK(cudaStreamSynchronize(h->stream));
+        if (h->opts.timeout_s > 0 && elapsed_s(t0) > h->opts.timeout_s)
+            return fail(h, MHFEM_ERR_TIMEOUT, "Krylov solve exceeded %.1f s", h->opts.timeout_s);
+    }
+    *iters = h->W.host_sc->it;
+    *res = h->W.host_sc->res;
+    return status_from_krylov(h, *h->W.host_sc, "FP64 BiCGStab");
+}
+
+mhfem_status run_mixed(mhfem_t h, int* iters, int* sweeps, double* res)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    KrylovScalars init{};
+    init.tol = h->opts.tol;
+    init.max_iter = h->opts.max_sweeps;
+    CK(cudaMemcpyAsync(h->W.sc, &init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
+    if (!h->g32) {
+        mhfem_status st = build_graph(h, true, h->opts.check_every);
+        if (st) return st;
+    }
+    int total_inner = 0;
+    for (;;) {
+        mixed_outer_residual(h->A, h->rhs, h->Z_iF, h->W, h->opts.tol, h->opts.max_sweeps, h->stream);
+        h->launches += 2;
+        CK(cudaMemcpyAsync(h->W.host_sc, h->W.sc, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, h->stream));
+        mixed_inner_init(h->W, h->opts.inner_tol, h->opts.max_iter, h->stream);
+        CK(cudaMemcpyAsync(h->W.host_sc + 1, h->W.sc32, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        CK(cudaGetLastError());
+        const KrylovScalars outer = h->W.host_sc[0];
+        if (outer.done) {
+            *iters = total_inner;
+            *sweeps = outer.it - 1;
+            *res = outer.res;
+            return status_from_krylov(h, outer, "mixed-precision refinement");
+        }
+        while (!h->W.host_sc[1].done) {
+            CK(cudaGraphLaunch(h->g32, h->stream));
+            h->launches += 5 * h->g32_iters;
+            CK(cudaStreamSynchronize(h->stream));
+            if (h->opts.timeout_s > 0 && elapsed_s(t0) > h->opts.timeout_s)
+                return fail(h, MHFEM_ERR_TIMEOUT, "mixed solve exceeded %.1f s", h->opts.timeout_s);
+        }
+        const KrylovScalars inner = h->W.host_sc[1];
+        total_inner += inner.it;
+        if (inner.status == KS_NOTFINITE)
+            return fail(h, MHFEM_ERR_NOT_FINITE, "FP32 inner solve produced a non-finite value");
+        mixed_apply_correction(h->Z_iF, h->W, h->stream);
+        h->launches += 1;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+mhfem_status mhfem_setup_linear_system(mhfem_t h)
+{
+    mhfem_status st = require_ready(h);
+    if (st) return st;
+    h->pattern_ready = false;
+    return ensure_pattern(h);
+}
+
+mhfem_status mhfem_pre_iterate(mhfem_t h, double t, double tau)
+{
+    mhfem_status st = require_ready(h);
+    if (st) return st;
+    if (!(tau > 0)) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "time step must be positive");
+    cudaSetDevice(h->desc.device);
+    if ((st = ensure_pattern(h)) != MHFEM_OK) return st;
+    h->cur_t = t;
+    h->cur_tau = tau;
+    DevProblem P = make_problem(h);
+    cudaEventRecord(h->ev[0], h->stream);
+    h->launches += launch_upwind(P, h->stream);
+    h->launches += launch_cell_local(P, tau, h->stream);
+    cudaEventRecord(h->ev[1], h->stream);
+    CK(cudaGetLastError());
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_assemble(mhfem_t h, double t, double tau)
+{
+    mhfem_status st = require_ready(h);
+    if (st) return st;
+    (void)t; (void)tau;  // stationary boundary values (BoundaryModels/Stationary.h)
+    if (!h->pattern_ready) return fail(h, MHFEM_ERR_STATE, "mhfem_pre_iterate must run before mhfem_assemble");
+    cudaSetDevice(h->desc.device);
+    DevProblem P = make_problem(h);
+    h->launches += launch_assemble(P, h->amap, h->A, h->rhs, h->desc.form == MHFEM_FORM_MIXED, h->stream);
+    cudaEventRecord(h->ev[2], h->stream);
+    CK(cudaGetLastError());
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_solve(mhfem_t h, mhfem_step_stats* stats)
+{
+    mhfem_status st = require_ready(h);
+    if (st) return st;
+    if (!h->pattern_ready) return fail(h, MHFEM_ERR_STATE, "the linear system is not assembled");
+    cudaSetDevice(h->desc.device);
+    // assembly error word (non-positive or non-finite diagonal)
+    CK(cudaMemcpyAsync(h->host_err, h->err_flags, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    if (*h->host_err) {
+        cudaMemsetAsync(h->err_flags, 0, sizeof(int32_t), h->stream);
+        return fail(h, MHFEM_ERR_NONPOSITIVE_DIAGONAL, "the diagonal matrix element is not positive");
+    }
+    int iters = 0, sweeps = 1;
+    double res = 0;
+    if (h->desc.form == MHFEM_FORM_MIXED) st = run_mixed(h, &iters, &sweeps, &res);
+    else st = run_fp64(h, h->opts.tol, h->opts.max_iter, &iters, &res);
+    cudaEventRecord(h->ev[3], h->stream);
+    h->total_iters += iters;
+    if (stats) {
+        stats->iterations = iters;
+        stats->sweeps = sweeps;
+        stats->residual = res;
+        stats->guess_used = 0;
+        stats->guess_residual = -1;
+        stats->warm_residual = -1;
+    }
+    return st;
+}
+
+mhfem_status mhfem_post_iterate(mhfem_t h, double t, double tau)
+{
+    mhfem_status st = require_ready(h);
+    if (st) return st;
+    (void)t; (void)tau;
+    cudaSetDevice(h->desc.device);
+    DevProblem P = make_problem(h);
+    h->launches += launch_reconstruct(P, h->stream);
+    cudaEventRecord(h->ev[4], h->stream);
+    CK(cudaGetLastError());
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_step(mhfem_t h, double t, double tau, mhfem_step_stats* stats)
+{
+    mhfem_status st;
+    if ((st = mhfem_pre_iterate(h, t, tau)) != MHFEM_OK) return st;
+    if ((st = mhfem_assemble(h, t, tau)) != MHFEM_OK) return st;
+    if ((st = mhfem_solve(h, stats)) != MHFEM_OK) return st;
+    if ((st = mhfem_post_iterate(h, t, tau)) != MHFEM_OK) return st;
+    h->total_steps += 1;
+    if (stats) {
+        CK(cudaEventSynchronize(h->ev[4]));
+        float a = 0, b = 0, c = 0, d = 0;
+        cudaEventElapsedTime(&a, h->ev[0], h->ev[1]);
+        cudaEventElapsedTime(&b, h->ev[1], h->ev[2]);
+        cudaEventElapsedTime(&c, h->ev[2], h->ev[3]);
+        cudaEventElapsedTime(&d, h->ev[3], h->ev[4]);
+        stats->ms_pre = a; stats->ms_assemble = b; stats->ms_solve = c; stats->ms_post = d;
+    }
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_get_state(mhfem_t h, double* Z_iF, double* Z_iK)
+{
+    mhfem_status st = require_ready(h);
+    if (st) return st;
+    cudaSetDevice(h->desc.device);
+    if (Z_iF) CK(cudaMemcpyAsync(Z_iF, h->Z_iF, sizeof(double) * h->n * h->topo.F, cudaMemcpyDeviceToHost, h->stream));
+    if (Z_iK) CK(cudaMemcpyAsync(Z_iK, h->Z_iK, sizeof(double) * h->n * h->topo.C, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_get_array(mhfem_t h, int32_t which, double* out, int64_t count)
+{
+    mhfem_status st = require_ready(h);
+    if (st) return st;
+    const int64_t n = h->n, nf = h->nf, C = h->topo.C, F = h->topo.F;
+    const double* src = nullptr;
+    int64_t size = 0;
+    switch (which) {
+        case MHFEM_ARRAY_B: src = h->b; size = n * n * h->S * C; break;
+        case MHFEM_ARRAY_R_IJKE: src = h->R_ijKe; size = n * n * nf * C; break;
+        case MHFEM_ARRAY_R_IK: src = h->R_iK; size = n * C; break;
+        case MHFEM_ARRAY_M_UPW: src = h->m_upw; size = n * F; break;
+        case MHFEM_ARRAY_Z_UPW: src = h->Z_upw; size = n * n * F; break;
+        case MHFEM_ARRAY_V: src = h->v_iKe; size = n * nf * C; break;
+        case MHFEM_ARRAY_RHS: src = h->rhs; size = n * F; break;
+        default: return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "unknown array %d", which);
+    }
+    if (!src) return fail(h, MHFEM_ERR_STATE, "array %d is not allocated in this configuration", which);
+    if (!out || count != size) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "array %d has %lld values", which, (long long)size);
+    cudaSetDevice(h->desc.device);
+    CK(cudaMemcpyAsync(out, src, sizeof(double) * size, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_get_system(mhfem_t h, int64_t* rowptr, int32_t* cols, double* vals, double* rhs)
+{
+    mhfem_status st = require_ready(h);
+    if (st) return st;
+    if ((st = ensure_pattern(h)) != MHFEM_OK) return st;
+    cudaSetDevice(h->desc.device);
+    const int64_t rows = h->pat.rows;
+    const int W = h->pat.W;
+    std::vector<double> ev((size_t)W * rows);
+    CK(cudaMemcpyAsync(ev.data(), h->A.vals, sizeof(double) * W * rows, cudaMemcpyDeviceToHost, h->stream));
+    if (rhs) CK(cudaMemcpyAsync(rhs, h->rhs, sizeof(double) * rows, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    int64_t pos = 0;
+    for (int64_t r = 0; r < rows; ++r) {
+        if (rowptr) rowptr[r] = pos;
+        const int len = h->pat.row_len[r];
+        int k = 0;
+        bool diag_done = false;
+        for (int q = 0; q < len; ++q) {
+            int32_t c;
+            double v;
+            const bool take_diag = !diag_done && (k >= len - 1 || h->pat.ell_cols[(size_t)k * rows + r] > r);
+            if (take_diag) { c = (int32_t)r; v = 1.0; diag_done = true; }
+            else { c = h->pat.ell_cols[(size_t)k * rows + r]; v = ev[(size_t)k * rows + r]; ++k; }
+            if (cols) cols[pos] = c;
+            if (vals) vals[pos] = v;
+            ++pos;
+        }
+    }
+    if (rowptr) rowptr[rows] = pos;
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_get_totals(mhfem_t h, int64_t* iterations, int64_t* time_steps, int64_t* kernel_launches)
+{
+    if (!h) return MHFEM_ERR_INVALID_ARGUMENT;
+    if (iterations) *iterations = h->total_iters;
+    if (time_steps) *time_steps = h->total_steps;
+    if (kernel_launches) *kernel_launches = h->launches;
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_get_stream(mhfem_t h, void** stream)
+{
+    if (!h || !stream) return MHFEM_ERR_INVALID_ARGUMENT;
+    *stream = (void*)h->stream;
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_time_kernel(mhfem_t h, int32_t kernel, int32_t reps, double* ms, double* bytes, double* flops)
+{
+    mhfem_status st = require_ready(h);
+    if (st) return st;
+    if (reps < 1) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "reps must be positive");
+    if ((st = ensure_pattern(h)) != MHFEM_OK) return st;
+    cudaSetDevice(h->desc.device);
+    const double n = h->n, nf = h->nf, S = h->S, C = (double)h->topo.C, F = (double)h->topo.F;
+    const double R = F * n, W = h->A.width, V = (double)h->topo.V, d = h->dim;
+    const double rec = nf * n * (n * nf + 1) * C * 8;  // assembly records (one per cell side)
+    DevProblem P = make_problem(h);
+    double B = 0, FL = 0;
+    // algorithmic bytes: each array once at its size; FLOPs: FP64 (FP32 for the SpMV32) operations
+    switch (kernel) {
+        case MHFEM_KERNEL_CELL_LOCAL:
+            B = 4 * nf * C + 8 * d * V + (h->coef[MHFEM_COEF_D].count > 1 ? 8 * n * n * C : 0) + 8 * n * C
+              + 4 * nf * C + C + 8 * n * n * S * C + 8 * n * n * nf * C + 8 * n * C + rec;
+            FL = C * (nf == 4 ? 420.0 : 220.0) * n * n;
+            break;
+        case MHFEM_KERNEL_ASSEMBLE:
+            B = 8 * F + 2 * F + 4 * F + F + rec + 8 * W * R + 8 * R
+              + (h->desc.form == MHFEM_FORM_MIXED ? 4 * W * R : 0);
+            FL = R * (W + 3);
+            break;
+        case MHFEM_KERNEL_SPMV_FP64: B = R * (12 * W + 24); FL = 2 * R * (W + 1); break;
+        case MHFEM_KERNEL_SPMV_FP32:
+            if (h->desc.form != MHFEM_FORM_MIXED) return fail(h, MHFEM_ERR_STATE, "FP32 SpMV needs the mixed form");
+            B = R * (8 * W + 12); FL = 2 * R * (W + 1); break;
+        case MHFEM_KERNEL_RECONSTRUCT:
+            B = 4 * nf * C + 8 * n * F + 8 * n * n * nf * C + 8 * n * C + 8 * n * C;
+            FL = 2 * C * n * (n * nf + 1);
+            break;
+        default: return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "unknown kernel %d", kernel);
+    }
+    if (kernel == MHFEM_KERNEL_SPMV_FP64 || kernel == MHFEM_KERNEL_SPMV_FP32) {
+        // make the Krylov kernels run (clear "done"); the state is re-initialized by the next solve
+        KrylovScalars z{};
+        z.rho = 1.0;
+        CK(cudaMemcpyAsync(kernel == MHFEM_KERNEL_SPMV_FP64 ? h->W.sc : h->W.sc32, &z, sizeof(z),
+                           cudaMemcpyHostToDevice, h->stream));
+    }
+    auto launch = [&]() {
+        switch (kernel) {
+            case MHFEM_KERNEL_CELL_LOCAL: launch_cell_local(P, h->cur_tau > 0 ? h->cur_tau : 1.0, h->stream); break;
+            case MHFEM_KERNEL_ASSEMBLE:
+                launch_assemble(P, h->amap, h->A, h->rhs, h->desc.form == MHFEM_FORM_MIXED, h->stream); break;
+            case MHFEM_KERNEL_SPMV_FP64: krylov_spmv_dot_once(h->A, h->W, false, h->stream); break;
+            case MHFEM_KERNEL_SPMV_FP32: krylov_spmv_dot_once(h->A, h->W, true, h->stream); break;
+            case MHFEM_KERNEL_RECONSTRUCT: launch_reconstruct(P, h->stream); break;
+        }
+    };
+    launch();  // warm-up
+    CK(cudaEventRecord(h->ev[0], h->stream));
+    for (int r = 0; r < reps; ++r) launch();
+    CK(cudaEventRecord(h->ev[1], h->stream));
+    CK(cudaEventSynchronize(h->ev[1]));
+    CK(cudaGetLastError());
+    float total = 0;
+    CK(cudaEventElapsedTime(&total, h->ev[0], h->ev[1]));
+    h->launches += reps + 1;
+    if (ms) *ms = total / reps;
+    if (bytes) *bytes = B;
+    if (flops) *flops = FL;
+    return MHFEM_OK;
+}
+
+}  // extern "C"

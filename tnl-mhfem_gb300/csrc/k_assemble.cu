@@ -1,0 +1,121 @@
+// In-place assembly of the hybridized face-trace system (sm_103a).
+//
+// One thread owns one row (E, i) (row index E*n + i, BaseModel.h:252-263),
+// so the fixed pattern is filled without atomics.  The interior row follows
+// LinearSystem::setMatrixElements (LinearSystem.h:66-256) and
+// RightHandSide::getValue (RightHandSide.h:18-45); boundary rows follow
+// BoundaryConditions::setMatrixElements (BoundaryConditions.hpp:335-508).
+//
+// Storage: every row is scaled to a unit diagonal (LinearSystem.h:196-201),
+// so the diagonal is implicit and only the off-diagonal part is stored, in
+// ELL form [slot][row] (column-major across rows: a warp's loads of one slot
+// are one contiguous 256-byte segment).  The merged, ascending face order of
+// the reference's row setters is precomputed once per mesh as a 4-bit
+// position per (side, local face) ("qmap"), so the kernel does no sorting.
+// The local Schur entries come from the per-(cell, local face) records that
+// k_cell_local wrote; each record is read by exactly one row.
+#include "mhfem_internal.h"
+
+namespace mhfem {
+
+template <int NF, int NE>
+__global__ void __launch_bounds__(256) k_assemble(const DevProblem P, const uint32_t* __restrict__ qmap,
+                                                  const uint8_t* __restrict__ qdiag, int W,
+                                                  double* __restrict__ vals, float* __restrict__ vals32,
+                                                  double* __restrict__ rhs)
+{
+    constexpr int RL = NE * NF + 1;
+    const int64_t rows = P.rows;
+    const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= rows) return;
+    const int64_t E = row / NE;
+    const int i = (int)(row - E * NE);
+    const int2 kk = __ldg(&P.face_cells[E]);
+    const int e0 = __ldg(P.face_local + 2 * E);
+    const int e1 = __ldg(P.face_local + 2 * E + 1);
+    const uint32_t qm = __ldg(qmap + E);
+    const int dslot = __ldg(qdiag + E) * NE + i;
+
+    auto put = [&](int q, int j, double v) {
+        const int idx = q * NE + j;
+        const int k = idx - (idx > dslot ? 1 : 0);
+        vals[(int64_t)k * rows + row] = v;
+        if (vals32) vals32[(int64_t)k * rows + row] = (float)v;
+    };
+    auto load_rec = [&](int64_t K, int e, double (&A)[RL]) {
+        const double* rec = P.rec + ((K * NF + e) * NE + i) * (int64_t)P.rec_stride;
+#pragma unroll
+        for (int q = 0; q < RL; ++q) A[q] = __ldcs(rec + q);
+    };
+
+    if (kk.y < 0) {
+        const int64_t bidx = (int64_t)i * P.F + E;
+        const int tag = P.bc_tags[bidx];
+        if (tag == MHFEM_BC_FIXED_VALUE) {
+            rhs[row] = P.bc_dirichlet[bidx];  // BoundaryConditions.hpp:367-376
+            return;
+        }
+        double A[RL];
+        load_rec(kk.x, e0, A);
+        const double diag = A[i * NF + e0];
+        if (!(diag > 0)) atomicOr(P.err_flags, 1);
+        const double rd = 1.0 / diag;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+            const int q = (qm >> (4 * f)) & 15u;
+#pragma unroll
+            for (int j = 0; j < NE; ++j) {
+                if (j == i && f == e0) continue;
+                put(q, j, A[j * NF + f] * rd);
+            }
+        }
+        double bval = 0;
+        if (tag != MHFEM_BC_ADVECTIVE_OUTFLOW) bval = -P.bc_values[bidx] * P.face_measure[E];
+        bval += A[NE * NF];
+        rhs[row] = bval * rd;
+        return;
+    }
+
+    double A0[RL], A1[RL];
+    load_rec(kk.x, e0, A0);
+    load_rec(kk.y, e1, A1);
+    const double diag = A0[i * NF + e0] + A1[i * NF + e1];
+    if (!(diag > 0)) atomicOr(P.err_flags, 1);
+    const double rd = 1.0 / diag;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        const int q = (qm >> (4 * f)) & 15u;
+#pragma unroll
+        for (int j = 0; j < NE; ++j) {
+            if (f == e0) {
+                if (j == i) continue;  // the unit diagonal (LinearSystem.h:196-201)
+                put(q, j, (A0[j * NF + e0] + A1[j * NF + e1]) * rd);
+            }
+            else
+                put(q, j, A0[j * NF + f] * rd);
+        }
+    }
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+        if (f == e1) continue;
+        const int q = (qm >> (4 * (NF + f))) & 15u;
+#pragma unroll
+        for (int j = 0; j < NE; ++j) put(q, j, A1[j * NF + f] * rd);
+    }
+    rhs[row] = (A0[NE * NF] + A1[NE * NF]) * rd;
+}
+
+int launch_assemble(const DevProblem& P, const AssemblyMap& M, EllMatrix& A, double* rhs,
+                    int write32, cudaStream_t s)
+{
+    if (P.rows == 0) return 0;
+    const unsigned grid = (unsigned)((P.rows + 255) / 256);
+    float* v32 = write32 ? A.vals32 : nullptr;
+    if (P.nf == 3 && P.n == 1) k_assemble<3, 1><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, v32, rhs);
+    else if (P.nf == 3 && P.n == 2) k_assemble<3, 2><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, v32, rhs);
+    else if (P.nf == 4 && P.n == 1) k_assemble<4, 1><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, v32, rhs);
+    else k_assemble<4, 2><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, v32, rhs);
+    return 1;
+}
+
+}  // namespace mhfem

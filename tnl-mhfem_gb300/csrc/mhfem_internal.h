@@ -1,0 +1,127 @@
+// Internal declarations shared by the host orchestration and the kernels.
+#pragma once
+
+#include <cstdint>
+#include <cstddef>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/mhfem.h"
+
+namespace mhfem {
+
+// A coefficient: a uniform value (stride 0) or a full array.
+struct Coef {
+    const double* p = nullptr;
+    int full = 0;
+};
+
+// Krylov scalars kept on the device; written by the last block of each
+// reduction kernel so an iteration never round-trips to the host.
+struct KrylovScalars {
+    double rho, alpha, omega, beta;
+    double bnorm, res, snorm;
+    double rv, ts, tt, rr, rhnorm;
+    int32_t it, done, status, max_iter;
+    int32_t restart, pad;
+    double tol;
+};
+
+// Krylov status codes written to KrylovScalars::status.
+enum : int32_t { KS_RUNNING = 0, KS_CONVERGED = 1, KS_MAXITER = 2, KS_BREAKDOWN = 3, KS_NOTFINITE = 4 };
+
+// Device-side view of a problem, passed by value to kernels.
+struct DevProblem {
+    int dim, nf, n, S, lumping, advection, mobility_upwind;
+    int64_t V, C, F, rows;
+    const double* coords;        // [V][dim]
+    const int32_t* cell_verts;   // SoA [v][C]
+    const int32_t* cell_faces;   // SoA [e][C]
+    const uint8_t* cell_bmask;   // bit e set: local face e lies on the boundary
+    const int2* face_cells;      // [F] (K0, K1), K1 = -1 on the boundary
+    const uint8_t* face_local;   // [F][2] local index of the face in K0, K1
+    const double* face_measure;  // [F]
+    Coef N, u, m, D, w, a, r, f, m_upw_in, m_bnd, psi;
+    double src_amp, src_omega, src_time;  // time-modulated source
+    const uint8_t* bc_tags;      // (i*F + E)
+    const double* bc_values;
+    const double* bc_dirichlet;
+    double* Z_iF;                // (E, i)
+    double* Z_iK;                // (i, K)
+    double* v_iKe;               // (i, e, K)
+    double* m_upw;               // (E, i) when computed
+    double* Z_upw;               // (E, j, i)
+    double* b;                   // (i, j, s, K)
+    double* R_ijKe;              // (i, j, e, K)
+    double* R_iK;                // (i, K)
+    double* rec;                 // per (K, e) assembly record, stride rec_stride doubles
+    int rec_stride;
+    int use_m_upw_array;         // m_upw read from an (E,i) array (computed or model input)
+    const double* m_upw_read;    // the array read when use_m_upw_array
+    int explicit_adv_active;     // explicit upwind with a or u not identically zero
+    int32_t* err_flags;          // device error word (bit 0: non-positive diagonal, bit 1: non-finite)
+};
+
+// ELL storage of the off-diagonal part of the unit-diagonal face system.
+struct EllMatrix {
+    int64_t rows = 0;
+    int width = 0;               // off-diagonal entries per row (max)
+    int32_t* cols = nullptr;     // [width][rows]
+    double* vals = nullptr;      // [width][rows]
+    float* vals32 = nullptr;     // [width][rows] (mixed form)
+};
+
+// Per-row assembly map: which ELL slot each (side, local face) goes to.
+struct AssemblyMap {
+    uint32_t* qmap = nullptr;    // per face: 4 bits per (side, local face): merged position q
+    uint8_t* qdiag = nullptr;    // per face: merged position of the face itself
+};
+
+// Launchers (k_local.cu)
+// Each launcher returns the number of kernels it launched.
+int launch_face_average(const DevProblem& P, cudaStream_t s);
+int launch_upwind(const DevProblem& P, cudaStream_t s);
+int launch_cell_local(const DevProblem& P, double tau, cudaStream_t s);
+int launch_reconstruct(const DevProblem& P, cudaStream_t s);
+
+// Launchers (k_assemble.cu)
+int launch_assemble(const DevProblem& P, const AssemblyMap& M, EllMatrix& A, double* rhs,
+                    int write32, cudaStream_t s);
+
+// Krylov (k_krylov.cu)
+struct KrylovWork {
+    int64_t rows = 0;
+    int grid = 0, block = 256;
+    double *r = nullptr, *rh = nullptr, *p = nullptr, *v = nullptr, *s = nullptr, *t = nullptr;
+    float *r32 = nullptr, *rh32 = nullptr, *p32 = nullptr, *v32 = nullptr, *s32 = nullptr,
+          *t32 = nullptr, *x32 = nullptr;
+    double* partials = nullptr;      // [grid][4]
+    uint32_t* counters = nullptr;    // last-block counters
+    KrylovScalars* sc = nullptr;     // device scalars (FP64 solve / outer)
+    KrylovScalars* sc32 = nullptr;   // device scalars (inner FP32 solve)
+    KrylovScalars* host_sc = nullptr;// pinned mirror
+};
+
+void krylov_init_fp64(const EllMatrix& A, const double* b, double* x, KrylovWork& W,
+                      double tol, int max_iter, cudaStream_t s);
+void krylov_iterate_fp64(const EllMatrix& A, double* x, KrylovWork& W, int iters, cudaStream_t s);
+
+// mixed: outer residual r = b - A x (FP64) -> sc; scale into r32; inner FP32 solve; x += scale*e
+void mixed_outer_residual(const EllMatrix& A, const double* b, const double* x, KrylovWork& W,
+                          double tol, int max_sweeps, cudaStream_t s);
+void mixed_inner_init(KrylovWork& W, double inner_tol, int max_iter, cudaStream_t s);
+void krylov_iterate_fp32(const EllMatrix& A, KrylovWork& W, int iters, cudaStream_t s);
+void mixed_apply_correction(double* x, KrylovWork& W, cudaStream_t s);
+
+// Residual of a candidate x: ||b - A x|| / ||b|| into W.sc->res (used by the learned gate)
+void residual_norm_fp64(const EllMatrix& A, const double* b, const double* x, KrylovWork& W,
+                        cudaStream_t s);
+
+int krylov_grid();
+
+// One launch of the SpMV + dot kernel on the current Krylov vectors (timing).
+void krylov_spmv_dot_once(const EllMatrix& A, KrylovWork& W, bool fp32, cudaStream_t s);
+
+}  // namespace mhfem

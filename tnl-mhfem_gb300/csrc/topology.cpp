@@ -1,0 +1,218 @@
+// Host-side topology builder and face-system pattern (setup, not per step).
+#include "topology.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace mhfem {
+
+namespace {
+
+double simplex_measure(const double* const* P, int k, int dim)
+{
+    double e1[3] = {0, 0, 0}, e2[3] = {0, 0, 0}, e3[3] = {0, 0, 0};
+    for (int d = 0; d < dim; ++d) e1[d] = P[1][d] - P[0][d];
+    if (k == 1) return std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+    for (int d = 0; d < dim; ++d) e2[d] = P[2][d] - P[0][d];
+    if (k == 2) {
+        if (dim == 2) return 0.5 * std::fabs(e1[0] * e2[1] - e1[1] * e2[0]);
+        const double cx = e1[1] * e2[2] - e1[2] * e2[1];
+        const double cy = e1[2] * e2[0] - e1[0] * e2[2];
+        const double cz = e1[0] * e2[1] - e1[1] * e2[0];
+        return 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+    }
+    for (int d = 0; d < dim; ++d) e3[d] = P[3][d] - P[0][d];
+    const double det = e1[0] * (e2[1] * e3[2] - e2[2] * e3[1]) - e1[1] * (e2[0] * e3[2] - e2[2] * e3[0])
+                     + e1[2] * (e2[0] * e3[1] - e2[1] * e3[0]);
+    return std::fabs(det) / 6.0;
+}
+
+struct Key {
+    int32_t b, c;
+    int32_t slot;
+};
+
+}  // namespace
+
+std::string build_topology(int dim, int64_t V, const double* coords, int64_t C, const int32_t* cell_verts,
+                           HostTopology& T)
+{
+    if (dim != 2 && dim != 3) return "dim must be 2 or 3";
+    const int nf = dim + 1;
+    const int64_t N = C * nf;
+    if (N >= (int64_t)INT32_MAX) return "mesh too large for int32 face slots";
+    for (int64_t q = 0; q < C * nf; ++q)
+        if (cell_verts[q] < 0 || cell_verts[q] >= V) return "cell vertex index out of range";
+
+    T = HostTopology();
+    T.dim = dim;
+    T.nf = nf;
+    T.V = V;
+    T.C = C;
+
+    // 1. sorted vertex tuple of every (cell, local face) slot; bucket by its smallest vertex
+    std::vector<int32_t> fa(N), fb(N), fc(N);
+#pragma omp parallel for schedule(static)
+    for (int64_t K = 0; K < C; ++K)
+        for (int e = 0; e < nf; ++e) {
+            int32_t v[3] = {-1, -1, -1};
+            int c = 0;
+            for (int q = 0; q < nf; ++q)
+                if (q != e) v[c++] = cell_verts[K * nf + q];
+            if (dim == 2) {
+                if (v[0] > v[1]) std::swap(v[0], v[1]);
+            }
+            else {
+                if (v[0] > v[1]) std::swap(v[0], v[1]);
+                if (v[1] > v[2]) std::swap(v[1], v[2]);
+                if (v[0] > v[1]) std::swap(v[0], v[1]);
+            }
+            const int64_t s = K * nf + e;
+            fa[s] = v[0];
+            fb[s] = v[1];
+            fc[s] = v[2];
+            if (v[0] == v[1] || (dim == 3 && v[1] == v[2])) fa[s] = -2;  // degenerate cell
+        }
+    for (int64_t s = 0; s < N; ++s)
+        if (fa[s] == -2) return "degenerate cell (repeated vertex)";
+
+    std::vector<int64_t> start(V + 1, 0);
+    for (int64_t s = 0; s < N; ++s) start[fa[s] + 1]++;
+    for (int64_t v = 0; v < V; ++v) start[v + 1] += start[v];
+    std::vector<Key> keys(N);
+    {
+        std::vector<int64_t> pos(start.begin(), start.end() - 1);
+        for (int64_t s = 0; s < N; ++s) keys[pos[fa[s]]++] = Key{fb[s], fc[s], (int32_t)s};
+    }
+
+    // 2. group equal faces inside each bucket; rep = smallest slot of the group
+    std::vector<int32_t> rep(N);
+    int bad = 0;
+#pragma omp parallel for schedule(dynamic, 1024) reduction(| : bad)
+    for (int64_t v = 0; v < V; ++v) {
+        Key* k0 = keys.data() + start[v];
+        Key* k1 = keys.data() + start[v + 1];
+        std::sort(k0, k1, [](const Key& x, const Key& y) {
+            if (x.b != y.b) return x.b < y.b;
+            if (x.c != y.c) return x.c < y.c;
+            return x.slot < y.slot;
+        });
+        for (Key* g = k0; g < k1;) {
+            Key* h = g + 1;
+            while (h < k1 && h->b == g->b && h->c == g->c) ++h;
+            if (h - g > 2) bad = 1;  // non-manifold: a face shared by more than two cells
+            for (Key* q = g; q < h; ++q) rep[q->slot] = g->slot;
+            g = h;
+        }
+    }
+    if (bad) return "non-manifold mesh: a face is shared by more than two cells";
+
+    // 3. face ids in order of first appearance
+    std::vector<int32_t> id_of_rep(N, -1);
+    int64_t F = 0;
+    for (int64_t s = 0; s < N; ++s)
+        if (rep[s] == s) id_of_rep[s] = (int32_t)F++;
+    T.F = F;
+    T.cell_faces.resize(N);
+    T.face_cells.assign(2 * F, -1);
+    T.face_local.assign(2 * F, 0);
+    T.face_verts.resize(F * dim);
+    for (int64_t s = 0; s < N; ++s) {
+        const int32_t E = id_of_rep[rep[s]];
+        T.cell_faces[s] = E;
+        const int32_t K = (int32_t)(s / nf);
+        const uint8_t e = (uint8_t)(s % nf);
+        if (T.face_cells[2 * E] < 0) {
+            T.face_cells[2 * E] = K;
+            T.face_local[2 * E] = e;
+            T.face_verts[E * dim + 0] = fa[s];
+            T.face_verts[E * dim + 1] = fb[s];
+            if (dim == 3) T.face_verts[E * dim + 2] = fc[s];
+        }
+        else {
+            T.face_cells[2 * E + 1] = K;
+            T.face_local[2 * E + 1] = e;
+        }
+    }
+    T.cell_bmask.assign(C, 0);
+    T.boundary_faces = 0;
+    for (int64_t E = 0; E < F; ++E)
+        if (T.face_cells[2 * E + 1] < 0) {
+            ++T.boundary_faces;
+            const int32_t K = T.face_cells[2 * E];
+            T.cell_bmask[K] |= (uint8_t)(1u << T.face_local[2 * E]);
+        }
+    T.face_measure.resize(F);
+#pragma omp parallel for schedule(static)
+    for (int64_t E = 0; E < F; ++E) {
+        const double* P[3];
+        for (int d = 0; d < dim; ++d) P[d] = coords + (int64_t)T.face_verts[E * dim + d] * dim;
+        T.face_measure[E] = simplex_measure(P, dim - 1, dim);
+    }
+    return std::string();
+}
+
+void build_pattern(const HostTopology& T, int n, const uint8_t* tags, HostPattern& P)
+{
+    const int nf = T.nf;
+    const int64_t F = T.F;
+    P = HostPattern();
+    P.n = n;
+    P.rows = F * n;
+    P.W = (T.C > 0) ? ((F > T.boundary_faces) ? (2 * nf - 1) * n - 1 : nf * n - 1) : 0;
+    P.qmap.assign(F, 0);
+    P.qdiag.assign(F, 0);
+    P.row_len.assign(P.rows, 0);
+    P.ell_cols.assign((size_t)P.W * P.rows, 0);
+    const int64_t rows = P.rows;
+    int64_t nnz = 0;
+#pragma omp parallel for schedule(static) reduction(+ : nnz)
+    for (int64_t E = 0; E < F; ++E) {
+        const int32_t K0 = T.face_cells[2 * E], K1 = T.face_cells[2 * E + 1];
+        int32_t list[8];
+        int L = 0;
+        for (int f = 0; f < nf; ++f) list[L++] = T.cell_faces[(int64_t)K0 * nf + f];
+        if (K1 >= 0)
+            for (int f = 0; f < nf; ++f) {
+                const int32_t g = T.cell_faces[(int64_t)K1 * nf + f];
+                if (g != (int32_t)E) list[L++] = g;
+            }
+        std::sort(list, list + L);
+        auto pos_of = [&](int32_t g) {
+            for (int q = 0; q < L; ++q)
+                if (list[q] == g) return q;
+            return 0;
+        };
+        uint32_t qm = 0;
+        for (int f = 0; f < nf; ++f) qm |= (uint32_t)pos_of(T.cell_faces[(int64_t)K0 * nf + f]) << (4 * f);
+        if (K1 >= 0)
+            for (int f = 0; f < nf; ++f)
+                qm |= (uint32_t)pos_of(T.cell_faces[(int64_t)K1 * nf + f]) << (4 * (nf + f));
+        P.qmap[E] = qm;
+        const int qd = pos_of((int32_t)E);
+        P.qdiag[E] = (uint8_t)qd;
+        for (int i = 0; i < n; ++i) {
+            const int64_t row = E * n + i;
+            int len;
+            int k = 0;
+            const bool dirichlet = (K1 < 0) && tags[(int64_t)i * F + E] == 0;
+            if (dirichlet) len = 1;
+            else {
+                len = L * n;
+                for (int q = 0; q < L; ++q)
+                    for (int j = 0; j < n; ++j) {
+                        if (q == qd && j == i) continue;
+                        P.ell_cols[(size_t)k * rows + row] = list[q] * n + j;
+                        ++k;
+                    }
+            }
+            for (; k < P.W; ++k) P.ell_cols[(size_t)k * rows + row] = (int32_t)row;
+            P.row_len[row] = len;
+            nnz += len;
+        }
+    }
+    P.nnz = nnz;
+}
+
+}  // namespace mhfem

@@ -1,0 +1,114 @@
+"""Seeded synthetic simplex meshes and random fields (numpy).
+
+The reference runs on meshes read from VTK files (its example meshes are
+Git-LFS stubs); these generators build the jittered structured meshes the
+benchmark workloads are defined on:
+
+* ``square_triangles(N)``: the unit square as N x N squares, each split into
+  two triangles along the (0,0)-(1,1) diagonal;
+* ``cube_tetrahedra(N)``: the unit cube as N^3 cubes, each split into six
+  tetrahedra along its main diagonal (Kuhn split, conforming between cubes).
+
+Interior vertices are jittered uniformly by +-jitter*h per coordinate; boundary
+vertices stay on the grid so the domain is exact.  Local vertex e of a cell is
+opposite its local face e.
+"""
+from __future__ import annotations
+
+import itertools
+
+import numpy as np
+
+
+def square_triangles(N: int, jitter: float = 0.2, seed: int = 1234):
+    h = 1.0 / N
+    idx = np.arange(N + 1)
+    iy, ix = np.meshgrid(idx, idx, indexing="ij")
+    coords = np.stack([ix.ravel() * h, iy.ravel() * h], axis=1)
+    rng = np.random.default_rng(seed)
+    J = rng.uniform(-jitter * h, jitter * h, size=coords.shape)
+    interior = ((ix > 0) & (ix < N) & (iy > 0) & (iy < N)).ravel()
+    coords[interior] += J[interior]
+    sy, sx = np.meshgrid(np.arange(N), np.arange(N), indexing="ij")
+    v00 = (sy * (N + 1) + sx).ravel()
+    v10 = v00 + 1
+    v01 = v00 + (N + 1)
+    v11 = v01 + 1
+    cells = np.empty((2 * N * N, 3), np.int32)
+    cells[0::2] = np.stack([v00, v10, v11], axis=1)
+    cells[1::2] = np.stack([v00, v11, v01], axis=1)
+    return coords, cells
+
+
+_KUHN_PERMS = list(itertools.permutations(range(3)))
+
+
+def cube_tetrahedra(N: int, jitter: float = 0.15, seed: int = 1234):
+    h = 1.0 / N
+    idx = np.arange(N + 1)
+    iz, iy, ix = np.meshgrid(idx, idx, idx, indexing="ij")
+    coords = np.stack([ix.ravel() * h, iy.ravel() * h, iz.ravel() * h], axis=1)
+    rng = np.random.default_rng(seed)
+    J = rng.uniform(-jitter * h, jitter * h, size=coords.shape)
+    interior = ((ix > 0) & (ix < N) & (iy > 0) & (iy < N) & (iz > 0) & (iz < N)).ravel()
+    coords[interior] += J[interior]
+    cz, cy, cx = np.meshgrid(np.arange(N), np.arange(N), np.arange(N), indexing="ij")
+    base = ((cz * (N + 1) + cy) * (N + 1) + cx).ravel().astype(np.int64)
+    step = np.array([1, N + 1, (N + 1) * (N + 1)], dtype=np.int64)
+    cells = np.empty((6 * N ** 3, 4), np.int32)
+    for t, perm in enumerate(_KUHN_PERMS):
+        v0 = base
+        v1 = v0 + step[perm[0]]
+        v2 = v1 + step[perm[1]]
+        v3 = v2 + step[perm[2]]
+        cells[t::6] = np.stack([v0, v1, v2, v3], axis=1)
+    return coords, cells
+
+
+def gaussian_field(shape, corr_length: float = 0.1, seed: int = 5678) -> np.ndarray:
+    """Zero-mean, unit-variance Gaussian random field on a periodic grid of
+    the unit square/cube, with Gaussian covariance of the given correlation
+    length: white noise filtered in Fourier space by exp(-|k|^2 l^2 / 4)."""
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal(shape)
+    ks = [np.fft.fftfreq(s, d=1.0 / s) * 2 * np.pi for s in shape]
+    grids = np.meshgrid(*ks, indexing="ij")
+    k2 = sum(g * g for g in grids)
+    g = np.real(np.fft.ifftn(np.fft.fftn(w) * np.exp(-k2 * corr_length ** 2 / 4.0)))
+    g -= g.mean()
+    sd = g.std()
+    return g / sd if sd > 0 else g
+
+
+def cell_centroids(coords: np.ndarray, cells: np.ndarray) -> np.ndarray:
+    return coords[cells].mean(axis=1)
+
+
+def cell_grid_index(centroids: np.ndarray, N: int) -> tuple:
+    """Index of the grid square/cube that contains each centroid."""
+    ij = np.clip(np.floor(centroids * N).astype(np.int64), 0, N - 1)
+    return tuple(ij[:, d] for d in range(ij.shape[1]))
+
+
+def face_centroids(coords: np.ndarray, face_verts: np.ndarray) -> np.ndarray:
+    return coords[face_verts].mean(axis=1)
+
+
+def outward_face_normals(coords: np.ndarray, cells: np.ndarray) -> np.ndarray:
+    """Outward normals scaled by the face measure, [C][nf][dim]: face e of a
+    cell is opposite local vertex e."""
+    C, nf = cells.shape
+    dim = nf - 1
+    X = coords[cells]  # [C][nf][dim]
+    out = np.empty((C, nf, dim))
+    for e in range(nf):
+        others = [v for v in range(nf) if v != e]
+        if dim == 2:
+            t = X[:, others[1]] - X[:, others[0]]
+            n = np.stack([t[:, 1], -t[:, 0]], axis=1)
+        else:
+            n = 0.5 * np.cross(X[:, others[1]] - X[:, others[0]], X[:, others[2]] - X[:, others[0]])
+        d = X[:, others[0]] - X[:, e]
+        sgn = np.sign(np.einsum("ij,ij->i", n, d))
+        out[:, e] = n * sgn[:, None]
+    return out

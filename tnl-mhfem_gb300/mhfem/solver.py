@@ -1,0 +1,215 @@
+"""Host-side mirror of TNL::MHFEM::Solver over the C ABI.
+
+Method names follow the reference's Solver interface (Solver.h:64-117):
+``setMesh``, ``setup``, ``setInitialCondition``, ``setupLinearSystem``,
+``preIterate``, ``assembleLinearSystem``, ``solveLinearSystem``,
+``postIterate``; ``step`` runs the four phases of one time step as
+MHFEM::solve does (control.h:83-98) and ``solve`` is that time loop.
+Arrays are numpy arrays in the reference's CUDA layouts (BaseModel.h:18-125).
+"""
+from __future__ import annotations
+
+import ctypes as ct
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(ct.POINTER(ct.c_double))
+
+
+def _i32ptr(a: np.ndarray):
+    return a.ctypes.data_as(ct.POINTER(ct.c_int32))
+
+
+def _i64ptr(a: np.ndarray):
+    return a.ctypes.data_as(ct.POINTER(ct.c_int64))
+
+
+@dataclass
+class StaticConfig:
+    """The reference's compile-time configuration (examples/config.h), at run time."""
+    dim: int = 2
+    n_eq: int = 1
+    mass_lumping: bool = False
+    advection: int = L.EXPLICIT_UPWIND
+    mobility_upwind: bool = False
+    form: int = L.FORM_FP64
+    device: int = 0
+
+
+COEF_IDS = {"N": L.COEF_N, "u": L.COEF_U, "m": L.COEF_M, "D": L.COEF_D, "w": L.COEF_W, "a": L.COEF_A,
+            "r": L.COEF_R, "f": L.COEF_F, "m_upw": L.COEF_M_UPW, "m_bnd": L.COEF_M_BND, "psi": L.COEF_PSI}
+ARRAY_IDS = {"b": L.ARRAY_B, "R_ijKe": L.ARRAY_R_IJKE, "R_iK": L.ARRAY_R_IK, "m_upw": L.ARRAY_M_UPW,
+             "Z_upw": L.ARRAY_Z_UPW, "v_iKe": L.ARRAY_V, "rhs": L.ARRAY_RHS}
+
+
+class Solver:
+    def __init__(self, config: StaticConfig):
+        self.lib = L.load()
+        self.config = config
+        desc = L.Desc(config.dim, config.n_eq, int(config.mass_lumping), config.advection,
+                      int(config.mobility_upwind), config.form, config.device)
+        h = ct.c_void_p()
+        st = self.lib.mhfem_create(ct.byref(desc), ct.byref(h))
+        if st != L.OK:
+            raise L.MhfemError(st, "mhfem_create failed (is a CUDA device visible?)")
+        self._h = h
+        self.C = self.F = self.V = 0
+        self.time_steps = 0
+
+    # -- error handling --------------------------------------------------
+    def _ck(self, st: int) -> None:
+        if st != L.OK:
+            msg = self.lib.mhfem_last_error(self._h)
+            raise L.MhfemError(st, msg.decode() if msg else "")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self.lib.mhfem_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- setup (Solver.hpp:28-484) -----------------------------------------
+    def setMesh(self, coords: np.ndarray, cells: np.ndarray) -> None:
+        coords = np.ascontiguousarray(coords, dtype=np.float64)
+        cells = np.ascontiguousarray(cells, dtype=np.int32)
+        assert coords.ndim == 2 and coords.shape[1] == self.config.dim
+        assert cells.ndim == 2 and cells.shape[1] == self.config.dim + 1
+        self._ck(self.lib.mhfem_set_mesh(self._h, coords.shape[0], _dptr(coords), cells.shape[0], _i32ptr(cells)))
+        V = ct.c_int64(); C = ct.c_int64(); F = ct.c_int64()
+        self._ck(self.lib.mhfem_get_sizes(self._h, ct.byref(V), ct.byref(C), ct.byref(F), None, None))
+        self.V, self.C, self.F = V.value, C.value, F.value
+
+    def topology(self):
+        d = self.config.dim
+        fv = np.empty((self.F, d), np.int32)
+        fc = np.empty((self.F, 2), np.int32)
+        cf = np.empty((self.C, d + 1), np.int32)
+        self._ck(self.lib.mhfem_get_topology(self._h, _i32ptr(fv), _i32ptr(fc), _i32ptr(cf)))
+        return fv, fc, cf
+
+    def set_coeff(self, name: str, value) -> None:
+        arr = np.ascontiguousarray(np.atleast_1d(np.asarray(value, dtype=np.float64)).ravel())
+        self._ck(self.lib.mhfem_set_coeff(self._h, COEF_IDS[name], _dptr(arr), arr.size))
+
+    def set_source_modulation(self, amplitude: float, period: float) -> None:
+        self._ck(self.lib.mhfem_set_source_modulation(self._h, amplitude, period))
+
+    def set_bc(self, tags: np.ndarray, values: np.ndarray, dirichlet: np.ndarray) -> None:
+        tags = np.ascontiguousarray(tags, dtype=np.uint8)
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        dirichlet = np.ascontiguousarray(dirichlet, dtype=np.float64)
+        n = self.config.n_eq * self.F
+        if tags.size != n or values.size != n or dirichlet.size != n:
+            raise ValueError(f"boundary arrays must hold n*F = {n} entries")
+        self._ck(self.lib.mhfem_set_bc(self._h, tags.ctypes.data_as(ct.POINTER(ct.c_uint8)), _dptr(values),
+                                       _dptr(dirichlet)))
+
+    def setup(self, tol: float = 1e-10, max_iter: int = 10000, inner_tol: float = 1e-4, max_sweeps: int = 50,
+              check_every: int = 8, timeout_s: float = 0.0) -> None:
+        o = L.SolverOpts(tol, max_iter, inner_tol, max_sweeps, check_every, timeout_s)
+        self._ck(self.lib.mhfem_set_solver(self._h, ct.byref(o)))
+
+    def setInitialCondition(self, Z_iK: np.ndarray, Z_iF: np.ndarray | None = None) -> None:
+        Z_iK = np.ascontiguousarray(Z_iK, dtype=np.float64).ravel()
+        if Z_iF is None:
+            self._ck(self.lib.mhfem_set_initial_condition(self._h, _dptr(Z_iK)))
+        else:
+            Z_iF = np.ascontiguousarray(Z_iF, dtype=np.float64).ravel()
+            self._ck(self.lib.mhfem_set_state(self._h, _dptr(Z_iK), _dptr(Z_iF)))
+
+    def setupLinearSystem(self) -> None:
+        self._ck(self.lib.mhfem_setup_linear_system(self._h))
+
+    # -- one time step (control.h:83-98) -------------------------------
+    def preIterate(self, t: float, tau: float) -> None:
+        self._ck(self.lib.mhfem_pre_iterate(self._h, t, tau))
+
+    def assembleLinearSystem(self, t: float, tau: float) -> None:
+        self._ck(self.lib.mhfem_assemble(self._h, t, tau))
+
+    def solveLinearSystem(self) -> dict:
+        s = L.StepStats()
+        self._ck(self.lib.mhfem_solve(self._h, ct.byref(s)))
+        return s.as_dict()
+
+    def postIterate(self, t: float, tau: float) -> None:
+        self._ck(self.lib.mhfem_post_iterate(self._h, t, tau))
+
+    def step(self, t: float, tau: float, stats: bool = True) -> dict | None:
+        if stats:
+            s = L.StepStats()
+            self._ck(self.lib.mhfem_step(self._h, t, tau, ct.byref(s)))
+            self.time_steps += 1
+            return s.as_dict()
+        self._ck(self.lib.mhfem_step(self._h, t, tau, None))
+        self.time_steps += 1
+        return None
+
+    def solve(self, start_time: float, stop_time: float, time_step: float, callback=None) -> list:
+        """The time loop of MHFEM::solve (control.h:64-102)."""
+        t = start_time
+        out = []
+        while stop_time - t > time_step * 1e-6:
+            tau = min(time_step, stop_time - t)
+            st = self.step(t, tau)
+            out.append(st)
+            if callback:
+                callback(t, tau, st)
+            t += tau
+        return out
+
+    # -- results --------------------------------------------------------
+    def state(self):
+        zf = np.empty(self.config.n_eq * self.F)
+        zk = np.empty(self.config.n_eq * self.C)
+        self._ck(self.lib.mhfem_get_state(self._h, _dptr(zf), _dptr(zk)))
+        return zf, zk
+
+    def array(self, name: str, size: int) -> np.ndarray:
+        out = np.empty(size)
+        self._ck(self.lib.mhfem_get_array(self._h, ARRAY_IDS[name], _dptr(out), size))
+        return out
+
+    def system(self):
+        rows = ct.c_int64(); nnz = ct.c_int64()
+        self._ck(self.lib.mhfem_get_sizes(self._h, None, None, None, ct.byref(rows), ct.byref(nnz)))
+        rowptr = np.empty(rows.value + 1, np.int64)
+        cols = np.empty(nnz.value, np.int32)
+        vals = np.empty(nnz.value)
+        rhs = np.empty(rows.value)
+        self._ck(self.lib.mhfem_get_system(self._h, _i64ptr(rowptr), _i32ptr(cols), _dptr(vals), _dptr(rhs)))
+        return rowptr, cols, vals, rhs
+
+    def totals(self):
+        """(Krylov iterations, time steps, kernel launches) since creation."""
+        it = ct.c_int64(); ts = ct.c_int64(); kl = ct.c_int64()
+        self._ck(self.lib.mhfem_get_totals(self._h, ct.byref(it), ct.byref(ts), ct.byref(kl)))
+        return it.value, ts.value, kl.value
+
+    def stream(self) -> int:
+        """The library's CUDA stream handle (for CUDA events on that stream)."""
+        p = ct.c_void_p()
+        self._ck(self.lib.mhfem_get_stream(self._h, ct.byref(p)))
+        return p.value or 0
+
+    def time_kernel(self, kernel: int, reps: int = 20) -> dict:
+        """Mean CUDA-event time of one path kernel and its algorithmic bytes / FLOPs per launch."""
+        ms = ct.c_double(); b = ct.c_double(); fl = ct.c_double()
+        self._ck(self.lib.mhfem_time_kernel(self._h, kernel, reps, ct.byref(ms), ct.byref(b), ct.byref(fl)))
+        return {"ms": ms.value, "bytes": b.value, "flops": fl.value}
