@@ -53,6 +53,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile-run", action="store_true",
+                    help="only the warm-up and timed steps (for an ncu launch list)")
     return ap.parse_args()
 
 
@@ -240,6 +242,11 @@ def main():
         dist.barrier()
     zf64, zk64 = s.state()
     iters = (it1 - it0) / args.steps
+    if args.profile_run:
+        if rank == 0:
+            print(json.dumps({"profile_run": True, "ms_per_step": el_ms / args.steps, "iterations_per_step": iters}))
+        s.close()
+        return
     ms_step = el_ms / args.steps
     value = world * args.steps / (el_ms / 1e3)
     bytes_step = step_bytes(n, nf, S, C, F, V, W, iters)

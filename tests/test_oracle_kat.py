@@ -1,0 +1,187 @@
+"""Known-answer tests that pin the CPU oracle (no GPU needed).
+
+The reference ships no tests or golden vectors and cannot be built here, so
+the oracle is pinned to answers that follow from mathematics and from the
+reference's own definitions:
+
+1. the stored b_ijK is the inverse of the RT0 mass matrix
+   int_K phi_e . phi_f dx with the basis of BasisFunctions_RTN0.h:32-51,
+   phi_e(x) = (x - v_e) / (d |K|), integrated exactly (degree-2 rules);
+2. linear patch test: a linear field with matching Dirichlet data is
+   reproduced exactly (to rounding) by the hybridized RT0 scheme;
+3. local conservation: sum_e v_Ke = |K| f - |K| N (Z_K^new - Z_K^old) / tau;
+4. row structure: unit diagonal, ascending columns, row lengths (2f-1)n /
+   1 / f n (LinearSystem.h:26-34, BoundaryConditions.hpp:283-299);
+5. the oracle's BiCGStab agrees with a direct sparse solve.
+"""
+import numpy as np
+import pytest
+import scipy.sparse.linalg as spla
+
+from helpers import rel_err, small_cases, variant
+from mhfem import meshgen, problems
+from oracle.oracle import OracleModel
+
+pytestmark = []
+
+
+def _quad_mass(X):
+    """Exact int_K phi_e . phi_f for a simplex with vertices X [nf][d]."""
+    nf, d = X.shape
+    if d == 2:
+        area = 0.5 * abs(np.linalg.det(X[1:] - X[0]))
+        pts = [(X[a] + X[b]) / 2 for a, b in [(0, 1), (1, 2), (0, 2)]]
+        wts = [area / 3] * 3
+        meas = area
+    else:
+        vol = abs(np.linalg.det(X[1:] - X[0])) / 6
+        al, be = 0.5854101966249685, 0.1381966011250105
+        pts = []
+        for k in range(4):
+            lam = np.full(4, be)
+            lam[k] = al
+            pts.append(lam @ X)
+        wts = [vol / 4] * 4
+        meas = vol
+    M = np.zeros((nf, nf))
+    for x, w in zip(pts, wts):
+        phi = [(x - X[e]) / (d * meas) for e in range(nf)]
+        for e in range(nf):
+            for f in range(nf):
+                M[e, f] += w * phi[e] @ phi[f]
+    return M
+
+
+def _unpack(bK, nf):
+    B = np.zeros((nf, nf))
+    for f in range(nf):
+        for e in range(f + 1):
+            B[e, f] = B[f, e] = bK[e + f * (f + 1) // 2]
+    return B
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_mass_matrix_is_inverse_of_rt0_quadrature(dim):
+    p = problems.heat2d(N=4) if dim == 2 else problems.diffusion3d(N=2)
+    p.coeffs["D"] = 1.0
+    m = OracleModel.from_problem(p)
+    m.pre_iterate(0.0, p.dt)
+    nf, S, C = dim + 1, m.S, m.C
+    b = m.b.reshape(S, C)
+    for K in range(0, C, max(1, C // 7)):
+        X = p.coords[p.cells[K]]
+        Binv = _unpack(b[:, K], nf)
+        M = _quad_mass(X)
+        assert np.abs(Binv @ M - np.eye(nf)).max() < 1e-11
+        # stored row sums (MassMatrix.h:594-597)
+        assert np.allclose(b[S - nf:, K], Binv.sum(axis=1), rtol=1e-14, atol=0)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_lumped_mass_matrix_is_spd(dim):
+    p = problems.heat2d(N=4) if dim == 2 else problems.diffusion3d(N=2)
+    p.config.mass_lumping = True
+    m = OracleModel.from_problem(p)
+    m.pre_iterate(0.0, p.dt)
+    nf, S, C = dim + 1, m.S, m.C
+    b = m.b.reshape(S, C)
+    for K in range(C):
+        B = _unpack(b[:, K], nf)
+        assert np.linalg.eigvalsh(B).min() > 0
+
+
+def _linear_problem(dim, neumann_sign=None):
+    c = np.array([0.7, -0.4, 0.25][:dim])
+    c0 = 0.3
+    Dval = 2.5
+    if dim == 2:
+        coords, cells = meshgen.square_triangles(6, 0.2, 99)
+    else:
+        coords, cells = meshgen.cube_tetrahedra(3, 0.15, 99)
+    cen = meshgen.cell_centroids(coords, cells)
+    Z0 = cen @ c + c0
+
+    def bc_fn(fv, fc):
+        F = fc.shape[0]
+        fcen = meshgen.face_centroids(coords, fv)
+        tags = np.zeros(F, np.uint8)
+        vals = np.zeros(F)
+        bnd = fc[:, 1] < 0
+        if neumann_sign is not None:
+            right = bnd & (np.abs(fcen[:, 0] - 1.0) < 1e-12)
+            tags[right] = problems.BC_FIXED_FLUX
+            # outward normal of the face x = 1 is +e_x
+            vals[right] = neumann_sign * Dval * c[0]
+        return tags, vals, fcen @ c + c0
+
+    cfg = problems.StaticConfig(dim=dim, n_eq=1)
+    coeffs = {"N": 1.0, "u": 0.0, "m": 1.0, "D": Dval, "w": 0.0, "a": 0.0, "r": 0.0, "f": 0.0, "m_upw": 1.0,
+              "m_bnd": 1.0}
+    p = problems.Problem("linear", cfg, coords, cells, coeffs, Z0, 1e-2, 3, 1e-13, bc_fn, 0)
+    return p, c, c0
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_linear_patch_dirichlet(dim):
+    p, c, c0 = _linear_problem(dim)
+    m = OracleModel.from_problem(p)
+    t = 0.0
+    for _ in range(p.steps):
+        m.step(t, p.dt, 1e-14)
+        t += p.dt
+    fcen = meshgen.face_centroids(p.coords, m.face_verts)
+    assert rel_err(m.Z_iF, fcen @ c + c0) < 1e-11
+    assert rel_err(m.Z_iK, meshgen.cell_centroids(p.coords, p.cells) @ c + c0) < 1e-11
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_linear_patch_neumann(dim):
+    """FixedFlux J on x = 1.  With the right-hand side -J |E| of the reference's
+    row setter (BoundaryConditions.hpp:413-418) the prescribed J is the outward
+    normal component of the velocity v = -D grad Z: J = -D grad Z . n."""
+    p, c, c0 = _linear_problem(dim, neumann_sign=-1.0)
+    m = OracleModel.from_problem(p)
+    t = 0.0
+    for _ in range(p.steps):
+        m.step(t, p.dt, 1e-14)
+        t += p.dt
+    fcen = meshgen.face_centroids(p.coords, m.face_verts)
+    assert rel_err(m.Z_iF, fcen @ c + c0) < 1e-10
+
+
+def test_local_conservation():
+    p = problems.diffusion3d(N=3, steps=1)
+    p = variant(p, mobility_upwind=True, coeffs={"f": 0.7})
+    m = OracleModel.from_problem(p)
+    z_old = m.Z_iK.copy()
+    m.step(0.0, p.dt, 1e-14)
+    C, nf = m.C, 4
+    v = m.v_iKe.reshape(nf, C)
+    X = p.coords[p.cells]
+    vol = np.abs(np.linalg.det(X[:, 1:] - X[:, :1])) / 6
+    balance = v.sum(axis=0) - (vol * 0.7 - vol * (m.Z_iK - z_old) / p.dt)
+    assert np.abs(balance).max() < 1e-10 * max(1.0, np.abs(v).max())
+
+
+@pytest.mark.parametrize("name", sorted(small_cases()))
+def test_row_structure_and_direct_solve(name):
+    p = small_cases()[name]
+    m = OracleModel.from_problem(p)
+    m.pre_iterate(0.0, p.dt)
+    m.assemble(0.0, p.dt)
+    A = m.csr()
+    n, nf = p.n, p.config.dim + 1
+    lens = np.diff(A.indptr)
+    interior = np.repeat(m.face_cells[:, 1] >= 0, n)
+    assert np.all(lens[interior] == (2 * nf - 1) * n)
+    tags = m.tags.reshape(n, m.F).T.ravel()  # row order E*n + i
+    bnd = ~interior
+    assert np.all(lens[bnd & (tags == 0)] == 1)
+    assert np.all(lens[bnd & (tags != 0)] == nf * n)
+    for r in range(A.shape[0]):
+        cols = A.indices[A.indptr[r]:A.indptr[r + 1]]
+        assert np.all(np.diff(cols) > 0)
+    assert np.all(A.diagonal() == 1.0)
+    x = spla.spsolve(A.tocsc(), m.rhs)
+    m.solve(1e-14)
+    assert rel_err(m.Z_iF, x) < 1e-10
