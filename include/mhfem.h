@@ -106,6 +106,8 @@ typedef struct {
     int32_t max_sweeps;       /* mixed form: cap on refinement sweeps */
     int32_t check_every;      /* Krylov iterations between host convergence checks */
     double  timeout_s;        /* host wall-clock limit of one solve (<= 0: none) */
+    int32_t inner_adaptive;   /* mixed form: relax the last sweeps' inner tolerance to what the outer
+                                 tolerance still needs (never tighter than inner_tol) */
 } mhfem_solver_opts;
 
 typedef struct {
@@ -228,6 +230,36 @@ mhfem_status mhfem_get_stream(mhfem_t h, void** stream);
  * counted once at its size) and its FP64 (or FP32) operation count. */
 mhfem_status mhfem_time_kernel(mhfem_t h, int32_t kernel, int32_t reps, double* ms_per_launch,
                                double* bytes_per_launch, double* flops_per_launch);
+
+/* ---- learned warm start (MHFEM_FORM_LEARNED) ----------------------------
+ * No counterpart in the reference: a message-passing network over the face
+ * adjacency graph (3 layers, hidden width 64, BF16 weights, FP32
+ * accumulation on the tensor cores) predicts the initial guess of each
+ * FP64 BiCGStab solve.  The guess is used only when its relative residual is
+ * below the previous-step warm start's; the solve always runs to the same
+ * tolerance.  The network is trained online on the first `train_steps`
+ * steps.  Only n_eq = 1 is supported. */
+typedef struct {
+    int32_t train_steps;          /* online training steps (default 200)            */
+    int32_t train_iters;          /* Adam iterations per training step (default 2)  */
+    double  learning_rate;        /* Adam step size (default 1e-3)                  */
+    int32_t use_during_training;  /* 1: also try the guess while still training     */
+    uint64_t seed;                /* initial weights (0 keeps the current ones)     */
+} mhfem_learned_opts;
+
+#define MHFEM_LEARNED_FEATURES 16
+mhfem_status mhfem_learned_set_options(mhfem_t h, const mhfem_learned_opts* opts);
+/* FP32 master parameters, flat: W0 [16][64], b0 [64], then W_l [128][64], b_l [64]
+ * for l = 1..3, then wd [64], bd [1]. */
+mhfem_status mhfem_learned_get_params(mhfem_t h, float* params, int64_t count);
+mhfem_status mhfem_learned_set_params(mhfem_t h, const float* params, int64_t count);
+/* Network output for given features [F][16] on the handle's face graph. */
+mhfem_status mhfem_learned_forward(mhfem_t h, const float* features, float* out);
+/* Loss mean((out - target)^2) over the non-Dirichlet faces and its gradient
+ * with respect to every parameter (layout as mhfem_learned_get_params). */
+mhfem_status mhfem_learned_gradients(mhfem_t h, const float* features, const double* target, float* grads,
+                                     double* loss);
+mhfem_status mhfem_learned_status(mhfem_t h, int32_t* trained_steps, double* last_loss, int32_t* num_params);
 
 #ifdef __cplusplus
 }

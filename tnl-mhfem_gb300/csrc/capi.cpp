@@ -15,111 +15,9 @@
 
 using namespace mhfem;
 
-namespace {
-
-constexpr int NCOEF = 11;
-
-struct DevCoef {
-    double* p = nullptr;
-    int64_t count = 0;  // 1 = uniform
-};
-
-}  // namespace
-
-struct mhfem_solver_s {
-    mhfem_desc desc{};
-    int dim = 0, nf = 0, n = 0, S = 0;
-    std::string err;
-    cudaStream_t stream = nullptr;
-    int sms = 0;
-
-    HostTopology topo;
-    HostPattern pat;
-    bool has_mesh = false, has_bc = false, has_state = false;
-    bool pattern_ready = false;
-    std::vector<uint8_t> h_tags;
-
-    // device topology
-    double* coords = nullptr;
-    int32_t* cell_verts = nullptr;   // SoA
-    int32_t* cell_faces = nullptr;   // SoA
-    uint8_t* cell_bmask = nullptr;
-    int2* face_cells = nullptr;
-    uint8_t* face_local = nullptr;
-    double* face_measure = nullptr;
-
-    DevCoef coef[NCOEF];
-    bool coef_nonzero[NCOEF] = {};
-    double src_amp = 0, src_period = 1;
-
-    uint8_t* tags = nullptr;
-    double* bvalues = nullptr;
-    double* bdirichlet = nullptr;
-
-    double *Z_iF = nullptr, *Z_iK = nullptr, *v_iKe = nullptr, *m_upw = nullptr, *Z_upw = nullptr;
-    double *b = nullptr, *R_ijKe = nullptr, *R_iK = nullptr, *rec = nullptr;
-    int rec_stride = 0;
-
-    EllMatrix A;
-    AssemblyMap amap;
-    double* rhs = nullptr;
-    int32_t* err_flags = nullptr;
-    int32_t* host_err = nullptr;
-    KrylovWork W;
-
-    mhfem_solver_opts opts{};
-    int64_t total_iters = 0, total_steps = 0, launches = 0;
-    double cur_t = 0, cur_tau = 0;
-
-    cudaGraphExec_t g64 = nullptr, g32 = nullptr;
-    int g64_iters = 0, g32_iters = 0;
-
-    cudaEvent_t ev[5] = {};
-    std::vector<void*> allocs;
-};
+#include "handle.h"
 
 namespace {
-
-mhfem_status fail(mhfem_t h, mhfem_status code, const char* fmt, ...)
-{
-    if (h) {
-        char buf[1024];
-        va_list ap;
-        va_start(ap, fmt);
-        vsnprintf(buf, sizeof(buf), fmt, ap);
-        va_end(ap);
-        h->err = buf;
-    }
-    return code;
-}
-
-#define CK(call)                                                                                  \
-    do {                                                                                          \
-        cudaError_t e_ = (call);                                                                  \
-        if (e_ != cudaSuccess)                                                                    \
-            return fail(h, e_ == cudaErrorMemoryAllocation ? MHFEM_ERR_OUT_OF_MEMORY : MHFEM_ERR_CUDA, \
-                        "%s failed: %s", #call, cudaGetErrorString(e_));                          \
-    } while (0)
-
-template <typename T>
-cudaError_t dalloc(mhfem_t h, T** p, size_t count)
-{
-    *p = nullptr;
-    if (count == 0) count = 1;
-    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * count);
-    if (e == cudaSuccess) h->allocs.push_back((void*)*p);
-    return e;
-}
-
-template <typename T>
-void dfree(mhfem_t h, T*& p)
-{
-    if (!p) return;
-    auto it = std::find(h->allocs.begin(), h->allocs.end(), (void*)p);
-    if (it != h->allocs.end()) h->allocs.erase(it);
-    cudaFree((void*)p);
-    p = nullptr;
-}
 
 int64_t coef_size(mhfem_t h, int which)
 {
@@ -144,6 +42,7 @@ mhfem_status set_coef_device(mhfem_t h, int which, const double* data, int64_t c
     }
     CK(cudaMemcpyAsync(h->coef[which].p, data, sizeof(double) * count, cudaMemcpyHostToDevice, h->stream));
     h->coef[which].count = count;
+    h->h_coef[which].assign(data, data + count);
     bool nz = false;
     for (int64_t q = 0; q < count && !nz; ++q) nz = (data[q] != 0.0);
     h->coef_nonzero[which] = nz;
@@ -228,6 +127,7 @@ void mhfem_default_solver_opts(mhfem_solver_opts* o)
     o->max_sweeps = 50;
     o->check_every = 8;
     o->timeout_s = 0;
+    o->inner_adaptive = 1;
 }
 
 mhfem_status mhfem_create(const mhfem_desc* desc, mhfem_t* out)
@@ -267,6 +167,7 @@ mhfem_status mhfem_destroy(mhfem_t h)
     cudaSetDevice(h->desc.device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     invalidate_graphs(h);
+    learned_release(h);
     for (void* p : h->allocs) cudaFree(p);
     h->allocs.clear();
     if (h->W.host_sc) cudaFreeHost(h->W.host_sc);
@@ -294,6 +195,7 @@ mhfem_status mhfem_set_mesh(mhfem_t h, int64_t V, const double* coords, int64_t 
     const int64_t F = h->topo.F;
     // release everything that depends on the mesh
     invalidate_graphs(h);
+    learned_release(h);
     for (void* p : h->allocs) cudaFree(p);
     h->allocs.clear();
     h->coords = nullptr; h->cell_verts = h->cell_faces = nullptr; h->cell_bmask = nullptr;
@@ -308,6 +210,7 @@ mhfem_status mhfem_set_mesh(mhfem_t h, int64_t V, const double* coords, int64_t 
     h->pattern_ready = false;
     h->has_bc = h->has_state = false;
 
+    h->h_coords.assign(coords, coords + V * h->dim);
     // topology on the device, SoA with the cell index innermost
     std::vector<int32_t> soa((size_t)C * nf);
     CK(dalloc(h, &h->coords, (size_t)V * h->dim));
@@ -491,6 +394,7 @@ mhfem_status ensure_pattern(mhfem_t h)
     if (h->pattern_ready) return MHFEM_OK;
     cudaSetDevice(h->desc.device);
     invalidate_graphs(h);
+    learned_invalidate(h);  // the face graph follows the pattern
     const int n = h->n;
     const int64_t F = h->topo.F, rows = F * n;
     build_pattern(h->topo, n, h->h_tags.data(), h->pat);
@@ -589,8 +493,10 @@ double elapsed_s(std::chrono::steady_clock::time_point t0)
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
 
+}  // namespace
+
 // Runs FP64 BiCGStab from the current Z_iF until the device flag says done.
-mhfem_status run_fp64(mhfem_t h, double tol, int max_iter, int* iters, double* res)
+mhfem_status mhfem::run_fp64(mhfem_t h, double tol, int max_iter, int* iters, double* res)
 {
     const auto t0 = std::chrono::steady_clock::now();
     krylov_init_fp64(h->A, h->rhs, h->Z_iF, h->W, tol, max_iter, h->stream);
@@ -614,6 +520,8 @@ mhfem_status run_fp64(mhfem_t h, double tol, int max_iter, int* iters, double* r
     return status_from_krylov(h, *h->W.host_sc, "FP64 BiCGStab");
 }
 
+namespace {
+
 mhfem_status run_mixed(mhfem_t h, int* iters, int* sweeps, double* res)
 {
     const auto t0 = std::chrono::steady_clock::now();
@@ -630,7 +538,7 @@ mhfem_status run_mixed(mhfem_t h, int* iters, int* sweeps, double* res)
         mixed_outer_residual(h->A, h->rhs, h->Z_iF, h->W, h->opts.tol, h->opts.max_sweeps, h->stream);
         h->launches += 2;
         CK(cudaMemcpyAsync(h->W.host_sc, h->W.sc, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, h->stream));
-        mixed_inner_init(h->W, h->opts.inner_tol, h->opts.max_iter, h->stream);
+        mixed_inner_init(h->W, h->opts.inner_tol, h->opts.inner_adaptive, h->opts.max_iter, h->stream);
         CK(cudaMemcpyAsync(h->W.host_sc + 1, h->W.sc32, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
         CK(cudaGetLastError());
@@ -716,7 +624,13 @@ mhfem_status mhfem_solve(mhfem_t h, mhfem_step_stats* stats)
     }
     int iters = 0, sweeps = 1;
     double res = 0;
+    if (stats) {
+        stats->guess_used = 0;
+        stats->guess_residual = -1;
+        stats->warm_residual = -1;
+    }
     if (h->desc.form == MHFEM_FORM_MIXED) st = run_mixed(h, &iters, &sweeps, &res);
+    else if (h->desc.form == MHFEM_FORM_LEARNED) st = learned_solve(h, &iters, &res, stats);
     else st = run_fp64(h, h->opts.tol, h->opts.max_iter, &iters, &res);
     cudaEventRecord(h->ev[3], h->stream);
     h->total_iters += iters;
@@ -724,9 +638,6 @@ mhfem_status mhfem_solve(mhfem_t h, mhfem_step_stats* stats)
         stats->iterations = iters;
         stats->sweeps = sweeps;
         stats->residual = res;
-        stats->guess_used = 0;
-        stats->guess_residual = -1;
-        stats->warm_residual = -1;
     }
     return st;
 }

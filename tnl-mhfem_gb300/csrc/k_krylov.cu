@@ -18,6 +18,9 @@
 //    convergence checks;
 //  - FP32 kernels accumulate per-thread sums in FP32 and block sums in FP64:
 //    GB300 issues FP64 at 1/57 of the FP32 rate.
+#include <mutex>
+#include <unordered_map>
+
 #include "mhfem_internal.h"
 
 namespace mhfem {
@@ -30,12 +33,51 @@ int krylov_grid()
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        g_grid = (sms > 0 ? sms : 152) * 4;
+        g_grid = (sms > 0 ? sms : 152) * 8;  // 8 x 256 threads = full occupancy
     }
     return g_grid;
 }
 
 constexpr int KB = 256;
+
+// Grid of a grid-stride kernel: as many CTAs of KB threads as can be resident
+// at once on every SM (fixed per kernel and device, so reductions stay
+// deterministic).
+template <typename Kern>
+static int occ_grid(Kern kernel)
+{
+    static std::mutex mu;
+    static std::unordered_map<const void*, int> cache;
+    static int sms = 0;
+    std::lock_guard<std::mutex> lock(mu);
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 152;
+    }
+    auto it = cache.find((const void*)kernel);
+    if (it != cache.end()) return it->second;
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, KB, 0);
+    const int g = sms * (nb > 0 ? (nb < 8 ? nb : 8) : 1);
+    cache[(const void*)kernel] = g;
+    return g;
+}
+
+// Compile-time ELL widths of the supported cell types: (2f - 1) n - 1 for
+// triangles / tetrahedra with one or two components; other widths (meshes
+// without interior faces) take the run-time loop.
+#define MHFEM_WIDTH_DISPATCH(W, CALL)                                   \
+    do {                                                                \
+        switch (W) {                                                    \
+            case 4: { constexpr int WW = 4; CALL; } break;              \
+            case 6: { constexpr int WW = 6; CALL; } break;              \
+            case 9: { constexpr int WW = 9; CALL; } break;              \
+            case 13: { constexpr int WW = 13; CALL; } break;            \
+            default: { constexpr int WW = 0; CALL; } break;             \
+        }                                                               \
+    } while (0)
 // restart threshold of |(rh, r)| relative to ||r|| ||rh|| (same as the oracle)
 constexpr double kRestartEps = 1e-14;
 
@@ -100,30 +142,50 @@ __device__ __forceinline__ void final_sums(const double* partials, double (&out)
     for (int q = 0; q < NV; ++q) out[q] = sh[0][q];
 }
 
-template <typename T>
+// y_r = x_r + sum_k vals[k][r] x[cols[k][r]] (unit diagonal).  With a
+// compile-time width WW every column and value load of the row is issued
+// before the gathers, so all of a row's memory accesses are in flight at once.
+template <typename T, int WW>
 __device__ __forceinline__ T spmv_row(const int32_t* __restrict__ cols, const T* __restrict__ vals, int W,
                                       int64_t rows, int64_t r, const T* __restrict__ x)
 {
-    T y = x[r];
-#pragma unroll 8
-    for (int k = 0; k < W; ++k) {
-        const int64_t o = (int64_t)k * rows + r;
-        y = fma(__ldg(vals + o), x[__ldg(cols + o)], y);
+    if constexpr (WW > 0) {
+        int32_t c[WW];
+        T v[WW];
+#pragma unroll
+        for (int k = 0; k < WW; ++k) {
+            c[k] = __ldg(cols + (int64_t)k * rows + r);
+            v[k] = __ldg(vals + (int64_t)k * rows + r);
+        }
+        T xg[WW];
+#pragma unroll
+        for (int k = 0; k < WW; ++k) xg[k] = x[c[k]];
+        T y = x[r];
+#pragma unroll
+        for (int k = 0; k < WW; ++k) y = fma(v[k], xg[k], y);
+        return y;
     }
-    return y;
+    else {
+        T y = x[r];
+        for (int k = 0; k < W; ++k) {
+            const int64_t o = (int64_t)k * rows + r;
+            y = fma(__ldg(vals + o), x[__ldg(cols + o)], y);
+        }
+        return y;
+    }
 }
 
 __device__ __forceinline__ bool finite(double v) { return isfinite(v); }
 
 // r = b - A x ; rh = r ; p = r ; partials: r.r, b.b
-template <typename T>
+template <typename T, int WW>
 __global__ void __launch_bounds__(KB) k_init(const int32_t* cols, const T* vals, int W, int64_t rows,
                                              const T* b, const T* x, T* r, T* rh, T* p,
                                              KrylovScalars* sc, double* partials, uint32_t* counter)
 {
     T acc[2] = {0, 0};
     for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB) {
-        const T rv = b[q] - spmv_row<T>(cols, vals, W, rows, q, x);
+        const T rv = b[q] - spmv_row<T, WW>(cols, vals, W, rows, q, x);
         r[q] = rv; rh[q] = rv; p[q] = rv;
         acc[0] = fma(rv, rv, acc[0]);
         acc[1] = fma(b[q], b[q], acc[1]);
@@ -150,7 +212,7 @@ __global__ void __launch_bounds__(KB) k_init(const int32_t* cols, const T* vals,
 }
 
 // v = A p ; alpha = rho / (rh . v)
-template <typename T>
+template <typename T, int WW>
 __global__ void __launch_bounds__(KB) k_spmv_dot(const int32_t* cols, const T* vals, int W, int64_t rows,
                                                  const T* p, const T* rh, T* v,
                                                  KrylovScalars* sc, double* partials, uint32_t* counter)
@@ -158,7 +220,7 @@ __global__ void __launch_bounds__(KB) k_spmv_dot(const int32_t* cols, const T* v
     if (*(volatile int32_t*)&sc->done) return;
     T acc[1] = {0};
     for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB) {
-        const T y = spmv_row<T>(cols, vals, W, rows, q, p);
+        const T y = spmv_row<T, WW>(cols, vals, W, rows, q, p);
         v[q] = y;
         acc[0] = fma(rh[q], y, acc[0]);
     }
@@ -195,7 +257,7 @@ __global__ void __launch_bounds__(KB) k_update_s(int64_t rows, const T* r, const
 }
 
 // t = A s ; omega = (t.s)/(t.t)  (skipped when ||s|| already meets the tolerance)
-template <typename T>
+template <typename T, int WW>
 __global__ void __launch_bounds__(KB) k_spmv_dots2(const int32_t* cols, const T* vals, int W, int64_t rows,
                                                    const T* s, T* t,
                                                    KrylovScalars* sc, double* partials, uint32_t* counter)
@@ -204,7 +266,7 @@ __global__ void __launch_bounds__(KB) k_spmv_dots2(const int32_t* cols, const T*
     if (sc->snorm < sc->tol) return;
     T acc[2] = {0, 0};
     for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB) {
-        const T y = spmv_row<T>(cols, vals, W, rows, q, s);
+        const T y = spmv_row<T, WW>(cols, vals, W, rows, q, s);
         t[q] = y;
         acc[0] = fma(y, s[q], acc[0]);
         acc[1] = fma(y, y, acc[1]);
@@ -308,33 +370,34 @@ void krylov_init_fp64(const EllMatrix& A, const double* b, double* x, KrylovWork
     h.tol = tol;
     h.max_iter = max_iter;
     cudaMemcpyAsync(W.sc, &h, sizeof(h), cudaMemcpyHostToDevice, s);
-    k_init<double><<<W.grid, KB, 0, s>>>(A.cols, A.vals, A.width, A.rows, b, x, W.r, W.rh, W.p, W.sc,
-                                         W.partials, W.counters);
+    MHFEM_WIDTH_DISPATCH(A.width, (k_init<double, WW><<<occ_grid(k_init<double, WW>), KB, 0, s>>>(A.cols, A.vals, A.width, A.rows, b, x,
+                                              W.r, W.rh, W.p, W.sc, W.partials, W.counters)));
 }
 
 void krylov_iterate_fp64(const EllMatrix& A, double* x, KrylovWork& W, int iters, cudaStream_t s)
 {
     for (int it = 0; it < iters; ++it) {
-        k_spmv_dot<double><<<W.grid, KB, 0, s>>>(A.cols, A.vals, A.width, A.rows, W.p, W.rh, W.v, W.sc,
-                                                 W.partials, W.counters);
-        k_update_s<double><<<W.grid, KB, 0, s>>>(A.rows, W.r, W.v, W.s, W.sc, W.partials, W.counters);
-        k_spmv_dots2<double><<<W.grid, KB, 0, s>>>(A.cols, A.vals, A.width, A.rows, W.s, W.t, W.sc,
-                                                   W.partials, W.counters);
-        k_update_xr<double><<<W.grid, KB, 0, s>>>(A.rows, x, W.p, W.s, W.t, W.r, W.rh, W.sc, W.partials,
+        MHFEM_WIDTH_DISPATCH(A.width, (k_spmv_dot<double, WW><<<occ_grid(k_spmv_dot<double, WW>), KB, 0, s>>>(A.cols, A.vals, A.width, A.rows,
+                                                  W.p, W.rh, W.v, W.sc, W.partials, W.counters)));
+        k_update_s<double><<<occ_grid(k_update_s<double>), KB, 0, s>>>(A.rows, W.r, W.v, W.s, W.sc, W.partials, W.counters);
+        MHFEM_WIDTH_DISPATCH(A.width, (k_spmv_dots2<double, WW><<<occ_grid(k_spmv_dots2<double, WW>), KB, 0, s>>>(A.cols, A.vals, A.width,
+                                                    A.rows, W.s, W.t, W.sc, W.partials, W.counters)));
+        k_update_xr<double><<<occ_grid(k_update_xr<double>), KB, 0, s>>>(A.rows, x, W.p, W.s, W.t, W.r, W.rh, W.sc, W.partials,
                                                   W.counters);
-        k_update_p<double><<<W.grid, KB, 0, s>>>(A.rows, W.p, W.r, W.v, W.rh, W.sc);
+        k_update_p<double><<<occ_grid(k_update_p<double>), KB, 0, s>>>(A.rows, W.p, W.r, W.v, W.rh, W.sc);
     }
 }
 
 // ---- residual of a candidate (learned gate) ------------------------------------
 
+template <int WW>
 __global__ void __launch_bounds__(KB) k_residual_norm(const int32_t* cols, const double* vals, int W,
                                                       int64_t rows, const double* b, const double* x,
                                                       KrylovScalars* sc, double* partials, uint32_t* counter)
 {
     double acc[2] = {0, 0};
     for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB) {
-        const double rv = b[q] - spmv_row<double>(cols, vals, W, rows, q, x);
+        const double rv = b[q] - spmv_row<double, WW>(cols, vals, W, rows, q, x);
         acc[0] = fma(rv, rv, acc[0]);
         acc[1] = fma(b[q], b[q], acc[1]);
     }
@@ -352,13 +415,15 @@ __global__ void __launch_bounds__(KB) k_residual_norm(const int32_t* cols, const
 
 void residual_norm_fp64(const EllMatrix& A, const double* b, const double* x, KrylovWork& W, cudaStream_t s)
 {
-    k_residual_norm<<<W.grid, KB, 0, s>>>(A.cols, A.vals, A.width, A.rows, b, x, W.sc, W.partials, W.counters);
+    MHFEM_WIDTH_DISPATCH(A.width, (k_residual_norm<WW><<<occ_grid(k_residual_norm<WW>), KB, 0, s>>>(A.cols, A.vals, A.width, A.rows, b, x,
+                                                W.sc, W.partials, W.counters)));
 }
 
 // ---- mixed precision: FP64 outer residual, FP32 inner BiCGStab ------------------
 
 // r = b - A x (FP64) and its norm; sc->res is the outer relative residual,
 // sc->snorm carries ||r|| (the scale of the FP32 right-hand side).
+template <int WW>
 __global__ void __launch_bounds__(KB) k_outer_residual(const int32_t* cols, const double* vals, int W,
                                                        int64_t rows, const double* b, const double* x,
                                                        double* r, KrylovScalars* sc, double* partials,
@@ -366,7 +431,7 @@ __global__ void __launch_bounds__(KB) k_outer_residual(const int32_t* cols, cons
 {
     double acc[2] = {0, 0};
     for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB) {
-        const double rv = b[q] - spmv_row<double>(cols, vals, W, rows, q, x);
+        const double rv = b[q] - spmv_row<double, WW>(cols, vals, W, rows, q, x);
         r[q] = rv;
         acc[0] = fma(rv, rv, acc[0]);
         acc[1] = fma(b[q], b[q], acc[1]);
@@ -392,7 +457,7 @@ __global__ void __launch_bounds__(KB) k_outer_residual(const int32_t* cols, cons
 // r32 = r / ||r|| ; rh32 = p32 = r32 ; x32 = 0 ; inner scalars
 __global__ void __launch_bounds__(KB) k_inner_init(int64_t rows, const double* r, float* r32, float* rh32,
                                                    float* p32, float* x32, const KrylovScalars* outer,
-                                                   KrylovScalars* sc, double inner_tol, int max_iter,
+                                                   KrylovScalars* sc, double inner_tol, int adaptive, int max_iter,
                                                    double* partials, uint32_t* counter)
 {
     const double scale = (outer->snorm > 0) ? 1.0 / outer->snorm : 0.0;
@@ -407,7 +472,12 @@ __global__ void __launch_bounds__(KB) k_inner_init(int64_t rows, const double* r
     double s[1];
     final_sums<1>(partials, s);
     if (threadIdx.x == 0) {
-        sc->tol = inner_tol;
+        // The last sweeps only need to close the remaining gap to the outer
+        // tolerance: with adaptivity on, the inner tolerance is relaxed to
+        // 0.3 tol / res (never tighter than inner_tol).
+        double itol = inner_tol;
+        if (adaptive && outer->res > 0) itol = fmax(inner_tol, fmin(0.5, 0.3 * outer->tol / outer->res));
+        sc->tol = itol;
         sc->max_iter = max_iter;
         sc->bnorm = sqrt(s[0]) > 0 ? sqrt(s[0]) : 1.0;
         sc->rho = s[0];
@@ -434,43 +504,43 @@ void mixed_outer_residual(const EllMatrix& A, const double* b, const double* x, 
                           double tol, int max_sweeps, cudaStream_t s)
 {
     (void)tol; (void)max_sweeps;
-    k_outer_residual<<<W.grid, KB, 0, s>>>(A.cols, A.vals, A.width, A.rows, b, x, W.r, W.sc, W.partials,
-                                           W.counters);
+    MHFEM_WIDTH_DISPATCH(A.width, (k_outer_residual<WW><<<occ_grid(k_outer_residual<WW>), KB, 0, s>>>(A.cols, A.vals, A.width, A.rows, b,
+                                                 x, W.r, W.sc, W.partials, W.counters)));
 }
 
-void mixed_inner_init(KrylovWork& W, double inner_tol, int max_iter, cudaStream_t s)
+void mixed_inner_init(KrylovWork& W, double inner_tol, int adaptive, int max_iter, cudaStream_t s)
 {
-    k_inner_init<<<W.grid, KB, 0, s>>>(W.rows, W.r, W.r32, W.rh32, W.p32, W.x32, W.sc, W.sc32, inner_tol,
-                                       max_iter, W.partials, W.counters);
+    k_inner_init<<<occ_grid(k_inner_init), KB, 0, s>>>(W.rows, W.r, W.r32, W.rh32, W.p32, W.x32, W.sc, W.sc32, inner_tol,
+                                       adaptive, max_iter, W.partials, W.counters);
 }
 
 void krylov_iterate_fp32(const EllMatrix& A, KrylovWork& W, int iters, cudaStream_t s)
 {
     for (int it = 0; it < iters; ++it) {
-        k_spmv_dot<float><<<W.grid, KB, 0, s>>>(A.cols, A.vals32, A.width, A.rows, W.p32, W.rh32, W.v32, W.sc32,
-                                                W.partials, W.counters);
-        k_update_s<float><<<W.grid, KB, 0, s>>>(A.rows, W.r32, W.v32, W.s32, W.sc32, W.partials, W.counters);
-        k_spmv_dots2<float><<<W.grid, KB, 0, s>>>(A.cols, A.vals32, A.width, A.rows, W.s32, W.t32, W.sc32,
-                                                  W.partials, W.counters);
-        k_update_xr<float><<<W.grid, KB, 0, s>>>(A.rows, W.x32, W.p32, W.s32, W.t32, W.r32, W.rh32, W.sc32,
+        MHFEM_WIDTH_DISPATCH(A.width, (k_spmv_dot<float, WW><<<occ_grid(k_spmv_dot<float, WW>), KB, 0, s>>>(A.cols, A.vals32, A.width, A.rows,
+                                                 W.p32, W.rh32, W.v32, W.sc32, W.partials, W.counters)));
+        k_update_s<float><<<occ_grid(k_update_s<float>), KB, 0, s>>>(A.rows, W.r32, W.v32, W.s32, W.sc32, W.partials, W.counters);
+        MHFEM_WIDTH_DISPATCH(A.width, (k_spmv_dots2<float, WW><<<occ_grid(k_spmv_dots2<float, WW>), KB, 0, s>>>(A.cols, A.vals32, A.width,
+                                                   A.rows, W.s32, W.t32, W.sc32, W.partials, W.counters)));
+        k_update_xr<float><<<occ_grid(k_update_xr<float>), KB, 0, s>>>(A.rows, W.x32, W.p32, W.s32, W.t32, W.r32, W.rh32, W.sc32,
                                                  W.partials, W.counters);
-        k_update_p<float><<<W.grid, KB, 0, s>>>(A.rows, W.p32, W.r32, W.v32, W.rh32, W.sc32);
+        k_update_p<float><<<occ_grid(k_update_p<float>), KB, 0, s>>>(A.rows, W.p32, W.r32, W.v32, W.rh32, W.sc32);
     }
 }
 
 void krylov_spmv_dot_once(const EllMatrix& A, KrylovWork& W, bool fp32, cudaStream_t s)
 {
     if (fp32)
-        k_spmv_dot<float><<<W.grid, KB, 0, s>>>(A.cols, A.vals32, A.width, A.rows, W.p32, W.rh32, W.v32, W.sc32,
-                                                W.partials, W.counters);
+        MHFEM_WIDTH_DISPATCH(A.width, (k_spmv_dot<float, WW><<<occ_grid(k_spmv_dot<float, WW>), KB, 0, s>>>(A.cols, A.vals32, A.width, A.rows,
+                                                 W.p32, W.rh32, W.v32, W.sc32, W.partials, W.counters)));
     else
-        k_spmv_dot<double><<<W.grid, KB, 0, s>>>(A.cols, A.vals, A.width, A.rows, W.p, W.rh, W.v, W.sc,
-                                                 W.partials, W.counters);
+        MHFEM_WIDTH_DISPATCH(A.width, (k_spmv_dot<double, WW><<<occ_grid(k_spmv_dot<double, WW>), KB, 0, s>>>(A.cols, A.vals, A.width, A.rows,
+                                                  W.p, W.rh, W.v, W.sc, W.partials, W.counters)));
 }
 
 void mixed_apply_correction(double* x, KrylovWork& W, cudaStream_t s)
 {
-    k_apply_correction<<<W.grid, KB, 0, s>>>(W.rows, x, W.x32, W.sc);
+    k_apply_correction<<<occ_grid(k_apply_correction), KB, 0, s>>>(W.rows, x, W.x32, W.sc);
 }
 
 }  // namespace mhfem

@@ -1,0 +1,636 @@
+// Learned warm start: a message-passing network over the face adjacency graph,
+// trained and evaluated with hand-written tcgen05 BF16 kernels (FP32
+// accumulation in tensor memory).  It has no counterpart in the reference; it
+// predicts the initial guess of each Krylov solve (the solve itself is the
+// unchanged FP64 BiCGStab).
+//
+// Network (hidden width 64), per face E with neighbours N(E) = the faces that
+// share a cell with E (the off-diagonal pattern of the face system):
+//     h1 = relu(x W0 + b0)                          x: 16 features
+//     a_l = mean_{E' in N(E)} h_l(E')               l = 1, 2, 3
+//     h_{l+1} = relu([h_l, a_l] W_l + b_l) + h_l
+//     out = h4 . wd + bd
+//
+// Kernels (128 faces per tile, 128 threads per CTA, persistent grids):
+//  - k_mpnn_layer<KIN>: each thread stages one face row of the A tile
+//    [h_l | mean of neighbours] (the gather is fused into the staging) in the
+//    canonical K-major layout; one thread issues KIN/16 tcgen05.mma
+//    (M=128, N=64, K=16) into a 64-column TMEM accumulator; the epilogue
+//    (tcgen05.ld, bias, ReLU, residual) writes h_{l+1} in BF16.
+//  - k_mpnn_bwd_dx: dX = dZ W^T (M=128, N=128, K=64) with dZ = dH * (Z > 0)
+//    formed while staging; writes dH_self + dH_next and the scaled
+//    neighbour gradient.
+//  - k_mpnn_bwd_dw: dW = X^T dZ, split over faces: each CTA accumulates its
+//    faces' contribution in TMEM (M=128 features, N=64, K=128 faces per
+//    tile) and writes one FP32 partial; partials are summed in a fixed order.
+//  - gather/transpose, decode + loss, Adam: CUDA-core kernels.
+#include <cuda_bf16.h>
+
+#include "mhfem_internal.h"
+#include "mpnn.h"
+#include "tcgen05.cuh"
+
+namespace mhfem {
+
+namespace {
+
+constexpr int H = kMpnnHidden;  // 64
+constexpr int TB = 128;         // faces per tile = threads per CTA
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b)
+{
+    const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+__device__ __forceinline__ float2 unpack_bf16(uint32_t u)
+{
+    __nv_bfloat162 v = *reinterpret_cast<__nv_bfloat162*>(&u);
+    return __bfloat1622float2(v);
+}
+
+// Stores 8 consecutive bf16 (one uint4) of row `r`, columns k0..k0+7, of a K-major tile.
+__device__ __forceinline__ void st_tile(uint8_t* tile, int r, int k0, int K, uint4 v)
+{
+    *reinterpret_cast<uint4*>(tile + tc::kmajor_offset(r, k0, K)) = v;
+}
+
+struct TileSync {
+    uint64_t* mbar;
+    uint32_t phase;
+};
+
+// MMA over a staged tile pair; thread 0 issues, every thread waits.
+template <int M, int N, int K>
+__device__ __forceinline__ bool tile_mma(uint8_t* sA, uint8_t* sB, uint32_t taddr, TileSync& ts, bool accumulate)
+{
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (threadIdx.x == 0) {
+        constexpr uint32_t idesc = tc::make_idesc_bf16(M, N);
+#pragma unroll
+        for (int ks = 0; ks < K / 16; ++ks) {
+            const uint64_t ad = tc::make_desc(tc::smem_addr(sA) + ks * 256, 128, K * 16);
+            const uint64_t bd = tc::make_desc(tc::smem_addr(sB) + ks * 256, 128, K * 16);
+            tc::mma_bf16(taddr, ad, bd, idesc, accumulate || ks > 0);
+        }
+        tc::mma_commit(ts.mbar);
+    }
+    const bool ok = tc::mbar_wait(ts.mbar, ts.phase);
+    ts.phase ^= 1u;
+    tc::fence_after_sync();
+    return ok;
+}
+
+__device__ __forceinline__ void tile_done()
+{
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+}
+
+// ---- forward layer ----------------------------------------------------------
+
+template <int KIN, bool TRAIN>
+__global__ void __launch_bounds__(TB) k_mpnn_layer(const MpnnView V, int layer)
+{
+    extern __shared__ __align__(128) uint8_t smem[];
+    uint8_t* sA = smem;                      // 128 x KIN
+    uint8_t* sB = smem + TB * KIN * 2;       // 64 x KIN
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tbase;
+    __shared__ float sbias[H];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int64_t F = V.F;
+
+    const __nv_bfloat16* Wf = V.w_fwd[layer];  // [64][KIN]
+    for (int idx = tid; idx < H * KIN / 8; idx += TB) {
+        const int r = idx / (KIN / 8), k0 = (idx % (KIN / 8)) * 8;
+        st_tile(sB, r, k0, KIN, *reinterpret_cast<const uint4*>(Wf + r * KIN + k0));
+    }
+    if (tid < H) sbias[tid] = V.bias[layer][tid];
+    if (warp == 0) {
+        tc::tmem_alloc(&tbase, H);
+        tc::tmem_relinquish();
+    }
+    if (tid == 0) tc::mbar_init(&mbar, 1);
+    tile_done();
+    const uint32_t taddr = tbase;
+    TileSync ts{&mbar, 0};
+    const __nv_bfloat16* hin = (KIN == 16) ? V.x0 : V.h[layer];
+    __nv_bfloat16* hout = V.h[layer + 1];
+    const int64_t ntiles = (F + TB - 1) / TB;
+
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t row = tile * TB + tid;
+        const bool valid = row < F;
+        uint32_t self[KIN == 16 ? 1 : 32];
+        if constexpr (KIN == 16) {
+            uint4 a = make_uint4(0, 0, 0, 0), b = a;
+            if (valid) {
+                a = *reinterpret_cast<const uint4*>(hin + row * 16);
+                b = *reinterpret_cast<const uint4*>(hin + row * 16 + 8);
+            }
+            st_tile(sA, tid, 0, 16, a);
+            st_tile(sA, tid, 8, 16, b);
+        }
+        else {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                uint4 v = make_uint4(0, 0, 0, 0);
+                if (valid) v = *reinterpret_cast<const uint4*>(hin + row * H + 8 * c);
+                self[4 * c + 0] = v.x; self[4 * c + 1] = v.y; self[4 * c + 2] = v.z; self[4 * c + 3] = v.w;
+                st_tile(sA, tid, 8 * c, KIN, v);
+            }
+            // neighbour mean, 32 columns at a time to bound register use
+            const int d = valid ? (int)V.deg[row] : 0;
+            const float inv = d > 0 ? 1.0f / (float)d : 0.0f;
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                float acc[32];
+#pragma unroll
+                for (int q = 0; q < 32; ++q) acc[q] = 0.f;
+                if (valid) {
+                    for (int k = 0; k < V.W; ++k) {
+                        const int32_t c = V.nbr[(int64_t)k * F + row];
+                        if (c == (int32_t)row) continue;
+                        const uint4* src = reinterpret_cast<const uint4*>(hin + (int64_t)c * H + 32 * half);
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const uint4 v = src[u];
+                            const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                            for (int t = 0; t < 4; ++t) {
+                                const float2 f = unpack_bf16(w4[t]);
+                                acc[8 * u + 2 * t] += f.x;
+                                acc[8 * u + 2 * t + 1] += f.y;
+                            }
+                        }
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    uint4 v;
+                    v.x = pack_bf16(acc[8 * u + 0] * inv, acc[8 * u + 1] * inv);
+                    v.y = pack_bf16(acc[8 * u + 2] * inv, acc[8 * u + 3] * inv);
+                    v.z = pack_bf16(acc[8 * u + 4] * inv, acc[8 * u + 5] * inv);
+                    v.w = pack_bf16(acc[8 * u + 6] * inv, acc[8 * u + 7] * inv);
+                    st_tile(sA, tid, H + 32 * half + 8 * u, KIN, v);
+                    if (TRAIN && valid)
+                        *reinterpret_cast<uint4*>(V.a[layer] + row * H + 32 * half + 8 * u) = v;
+                }
+            }
+        }
+        if (!tile_mma<TB, H, KIN>(sA, sB, taddr, ts, false)) {
+            if (tid == 0) atomicOr(V.err, 4);
+            break;
+        }
+        float acc[H];
+        tc::tmem_ld_x64(taddr + ((uint32_t)(32 * warp) << 16), acc);
+        if (valid) {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                uint32_t zo[4], ho[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int q = 8 * c + 2 * t;
+                    const float z0 = acc[q] + sbias[q], z1 = acc[q + 1] + sbias[q + 1];
+                    float o0 = fmaxf(z0, 0.f), o1 = fmaxf(z1, 0.f);
+                    if constexpr (KIN != 16) {
+                        const float2 s = unpack_bf16(self[4 * c + t]);
+                        o0 += s.x;
+                        o1 += s.y;
+                    }
+                    zo[t] = pack_bf16(z0, z1);
+                    ho[t] = pack_bf16(o0, o1);
+                }
+                *reinterpret_cast<uint4*>(hout + row * H + 8 * c) = make_uint4(ho[0], ho[1], ho[2], ho[3]);
+                if (TRAIN)
+                    *reinterpret_cast<uint4*>(V.z[layer] + row * H + 8 * c) = make_uint4(zo[0], zo[1], zo[2], zo[3]);
+            }
+        }
+        tile_done();
+    }
+    tile_done();
+    if (warp == 0) tc::tmem_dealloc(taddr, H);
+}
+
+// ---- decoder, loss and the start of the backward pass --------------------------
+
+// out = h4 . wd + bd.  Inference: guess = base + sd * out on free rows, the
+// Dirichlet value on fixed rows.  Training: loss, dout, dh4 = dout wd and
+// the decoder gradients.
+template <bool TRAIN>
+__global__ void __launch_bounds__(256) k_mpnn_decode(const MpnnView V, const double* base, double sd,
+                                                     const double* rhs, const double* target, double* guess,
+                                                     double inv_nt)
+{
+    __shared__ float swd[H];
+    __shared__ double red[256 / 32][H + 2];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid < H) swd[tid] = V.wd[tid];
+    __syncthreads();
+    const float bd = V.bd[0];
+    double acc_l = 0, acc_db = 0;
+    float acc_w[H];
+#pragma unroll
+    for (int q = 0; q < H; ++q) acc_w[q] = 0.f;
+    const __nv_bfloat16* h4 = V.h[kMpnnLayers + 1];
+    for (int64_t row = (int64_t)blockIdx.x * 256 + tid; row < V.F; row += (int64_t)gridDim.x * 256) {
+        float hv[H];
+        float out = bd;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const uint4 v = *reinterpret_cast<const uint4*>(h4 + row * H + 8 * c);
+            const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const float2 f = unpack_bf16(w4[t]);
+                hv[8 * c + 2 * t] = f.x;
+                hv[8 * c + 2 * t + 1] = f.y;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < H; ++q) out = fmaf(hv[q], swd[q], out);
+        const bool fixed = V.fixed[row] != 0;
+        if (!TRAIN) {
+            guess[row] = fixed ? rhs[row] : base[row] + sd * (double)out;
+            continue;
+        }
+        const double diff = fixed ? 0.0 : ((double)out - target[row]);
+        acc_l += diff * diff;
+        const float dout = (float)(2.0 * diff * inv_nt);
+        acc_db += dout;
+#pragma unroll
+        for (int q = 0; q < H; ++q) acc_w[q] = fmaf(dout, hv[q], acc_w[q]);
+        float* dh = V.dh + row * H;
+#pragma unroll
+        for (int c = 0; c < H / 4; ++c)
+            *reinterpret_cast<float4*>(dh + 4 * c) =
+                make_float4(dout * swd[4 * c], dout * swd[4 * c + 1], dout * swd[4 * c + 2], dout * swd[4 * c + 3]);
+    }
+    if (!TRAIN) return;
+    // block reduction of (dwd[64], dbd, loss) into partials[block][66]
+#pragma unroll
+    for (int q = 0; q < H; ++q) {
+        float v = acc_w[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp][q] = v;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        acc_db += __shfl_down_sync(0xffffffffu, acc_db, o);
+        acc_l += __shfl_down_sync(0xffffffffu, acc_l, o);
+    }
+    if (lane == 0) { red[warp][H] = acc_db; red[warp][H + 1] = acc_l; }
+    __syncthreads();
+    if (tid < H + 2) {
+        double s = 0;
+        for (int w = 0; w < 256 / 32; ++w) s += red[w][tid];
+        V.dec_partials[(int64_t)blockIdx.x * (H + 2) + tid] = s;
+    }
+}
+
+// ---- backward: dX = dZ W^T ------------------------------------------------------
+
+// A = dZ (128 x 64) with dZ = dH * (Z > 0), B = W_in (128 x 64: row k = input k).
+// Epilogue: dH += dX[:, :64] (residual + self path), ga = dX[:, 64:] / deg.
+__global__ void __launch_bounds__(TB) k_mpnn_bwd_dx(const MpnnView V, int layer)
+{
+    extern __shared__ __align__(128) uint8_t smem[];
+    uint8_t* sA = smem;               // 128 x 64
+    uint8_t* sB = smem + TB * H * 2;  // 128 x 64
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tbase;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int64_t F = V.F;
+    const __nv_bfloat16* Wb = V.w_bwd[layer];  // [128][64]
+    for (int idx = tid; idx < 2 * H * H / 8; idx += TB) {
+        const int r = idx / (H / 8), k0 = (idx % (H / 8)) * 8;
+        st_tile(sB, r, k0, H, *reinterpret_cast<const uint4*>(Wb + r * H + k0));
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(&tbase, 2 * H);
+        tc::tmem_relinquish();
+    }
+    if (tid == 0) tc::mbar_init(&mbar, 1);
+    tile_done();
+    const uint32_t taddr = tbase;
+    TileSync ts{&mbar, 0};
+    const int64_t ntiles = (F + TB - 1) / TB;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t row = tile * TB + tid;
+        const bool valid = row < F;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            uint4 out = make_uint4(0, 0, 0, 0);
+            if (valid) {
+                const float4 d0 = *reinterpret_cast<const float4*>(V.dh + row * H + 8 * c);
+                const float4 d1 = *reinterpret_cast<const float4*>(V.dh + row * H + 8 * c + 4);
+                const uint4 zz = *reinterpret_cast<const uint4*>(V.z[layer] + row * H + 8 * c);
+                const float2 z0 = unpack_bf16(zz.x), z1 = unpack_bf16(zz.y), z2 = unpack_bf16(zz.z),
+                             z3 = unpack_bf16(zz.w);
+                out.x = pack_bf16(z0.x > 0 ? d0.x : 0.f, z0.y > 0 ? d0.y : 0.f);
+                out.y = pack_bf16(z1.x > 0 ? d0.z : 0.f, z1.y > 0 ? d0.w : 0.f);
+                out.z = pack_bf16(z2.x > 0 ? d1.x : 0.f, z2.y > 0 ? d1.y : 0.f);
+                out.w = pack_bf16(z3.x > 0 ? d1.z : 0.f, z3.y > 0 ? d1.w : 0.f);
+                *reinterpret_cast<uint4*>(V.dz + row * H + 8 * c) = out;
+            }
+            st_tile(sA, tid, 8 * c, H, out);
+        }
+        if (!tile_mma<TB, 2 * H, H>(sA, sB, taddr, ts, false)) {
+            if (tid == 0) atomicOr(V.err, 4);
+            break;
+        }
+        float acc[H];
+        tc::tmem_ld_x64(taddr + ((uint32_t)(32 * warp) << 16), acc);
+        if (valid) {
+            float* dh = V.dh + row * H;
+#pragma unroll
+            for (int c = 0; c < H / 4; ++c) {
+                float4 v = *reinterpret_cast<float4*>(dh + 4 * c);
+                v.x += acc[4 * c]; v.y += acc[4 * c + 1]; v.z += acc[4 * c + 2]; v.w += acc[4 * c + 3];
+                *reinterpret_cast<float4*>(dh + 4 * c) = v;
+            }
+        }
+        tc::tmem_ld_x64(taddr + ((uint32_t)(32 * warp) << 16) + H, acc);
+        if (valid) {
+            const int d = V.deg[row];
+            const float inv = d > 0 ? 1.0f / (float)d : 0.f;
+            float* ga = V.ga + row * H;
+#pragma unroll
+            for (int c = 0; c < H / 4; ++c)
+                *reinterpret_cast<float4*>(ga + 4 * c) =
+                    make_float4(acc[4 * c] * inv, acc[4 * c + 1] * inv, acc[4 * c + 2] * inv, acc[4 * c + 3] * inv);
+        }
+        tile_done();
+    }
+    tile_done();
+    if (warp == 0) tc::tmem_dealloc(taddr, 2 * H);
+}
+
+// dH[E] += sum_{E' in N(E)} ga[E'] (the adjacency is symmetric, so this is
+// the transpose of the neighbour mean).  16 threads per face, 4 columns each.
+__global__ void __launch_bounds__(256) k_mpnn_gather_add(const MpnnView V)
+{
+    const int64_t gid = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    const int64_t row = gid >> 4;
+    const int c = (int)(gid & 15) * 4;
+    if (row >= V.F) return;
+    float4 s = *reinterpret_cast<const float4*>(V.dh + row * H + c);
+    for (int k = 0; k < V.W; ++k) {
+        const int32_t e = V.nbr[(int64_t)k * V.F + row];
+        if (e == (int32_t)row) continue;
+        const float4 g = *reinterpret_cast<const float4*>(V.ga + (int64_t)e * H + c);
+        s.x += g.x; s.y += g.y; s.z += g.z; s.w += g.w;
+    }
+    *reinterpret_cast<float4*>(V.dh + row * H + c) = s;
+}
+
+// dz0 = dh * (z0 > 0) in BF16 (encoder)
+__global__ void __launch_bounds__(256) k_mpnn_dz0(const MpnnView V)
+{
+    const int64_t gid = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    if (gid >= V.F * (H / 2)) return;
+    const float2 d = *reinterpret_cast<const float2*>(V.dh + 2 * gid);
+    const float2 z = unpack_bf16(*reinterpret_cast<const uint32_t*>(V.z[0] + 2 * gid));
+    *reinterpret_cast<uint32_t*>(V.dz + 2 * gid) = pack_bf16(z.x > 0 ? d.x : 0.f, z.y > 0 ? d.y : 0.f);
+}
+
+// ---- backward: dW = X^T dZ (split over faces) -----------------------------------
+
+// X = [h_l, a_l] (KF = 128) or x0 (KF = 16, zero-padded to 128 rows).  The
+// staging transposes both operands into K-major tiles over the face index.
+template <int KF>
+__global__ void __launch_bounds__(TB) k_mpnn_bwd_dw(const MpnnView V, int layer, float* partials)
+{
+    extern __shared__ __align__(128) uint8_t smem[];
+    uint8_t* sA = smem;                // 128 features x 128 faces
+    uint8_t* sB = smem + TB * TB * 2;  // 64 outputs x 128 faces
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tbase;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t F = V.F;
+    if (KF < TB) {
+        // rows KF..127 of the feature tile stay zero
+        for (int idx = tid; idx < TB * TB / 8; idx += TB) {
+            const int r = idx / (TB / 8), k0 = (idx % (TB / 8)) * 8;
+            st_tile(sA, r, k0, TB, make_uint4(0, 0, 0, 0));
+        }
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(&tbase, H);
+        tc::tmem_relinquish();
+    }
+    if (tid == 0) tc::mbar_init(&mbar, 1);
+    tile_done();
+    const uint32_t taddr = tbase;
+    TileSync ts{&mbar, 0};
+    float dbs[H];
+#pragma unroll
+    for (int q = 0; q < H; ++q) dbs[q] = 0.f;
+    const int64_t ntiles = (F + TB - 1) / TB;
+    bool first = true;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t row = tile * TB + tid;  // this thread's face = column tid of both tiles
+        const bool valid = row < F;
+        __nv_bfloat16* sAh = reinterpret_cast<__nv_bfloat16*>(sA);
+        __nv_bfloat16* sBh = reinterpret_cast<__nv_bfloat16*>(sB);
+        const __nv_bfloat16 zero = __float2bfloat16(0.f);
+        if constexpr (KF == 16) {
+#pragma unroll
+            for (int m = 0; m < 16; ++m)
+                sAh[tc::kmajor_offset(m, tid, TB) / 2] = valid ? V.x0[row * 16 + m] : zero;
+        }
+        else {
+            for (int m = 0; m < H; ++m) {
+                sAh[tc::kmajor_offset(m, tid, TB) / 2] = valid ? V.h[layer][row * H + m] : zero;
+                sAh[tc::kmajor_offset(H + m, tid, TB) / 2] = valid ? V.a[layer][row * H + m] : zero;
+            }
+        }
+        for (int n = 0; n < H; ++n) {
+            const __nv_bfloat16 dzv = valid ? V.dz[row * H + n] : zero;
+            sBh[tc::kmajor_offset(n, tid, TB) / 2] = dzv;
+            dbs[n] += __bfloat162float(dzv);
+        }
+        if (!tile_mma<TB, H, TB>(sA, sB, taddr, ts, !first)) {
+            if (tid == 0) atomicOr(V.err, 4);
+            break;
+        }
+        first = false;
+        tile_done();
+    }
+    // partial dW: row m = 32 warp + lane, 64 output columns
+    float acc[H];
+    if (first) {
+#pragma unroll
+        for (int q = 0; q < H; ++q) acc[q] = 0.f;
+    }
+    else
+        tc::tmem_ld_x64(taddr + ((uint32_t)(32 * warp) << 16), acc);
+    float* P = partials + (int64_t)blockIdx.x * (TB * H + H);
+    const int m = 32 * warp + lane;
+#pragma unroll
+    for (int c = 0; c < H / 4; ++c)
+        *reinterpret_cast<float4*>(P + m * H + 4 * c) = make_float4(acc[4 * c], acc[4 * c + 1], acc[4 * c + 2],
+                                                                    acc[4 * c + 3]);
+    // db partial: reduce dbs over the block
+    __shared__ float red[TB / 32][H];
+#pragma unroll
+    for (int q = 0; q < H; ++q) {
+        float v = dbs[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp][q] = v;
+    }
+    tile_done();
+    if (tid < H) {
+        float s = 0;
+        for (int w = 0; w < TB / 32; ++w) s += red[w][tid];
+        P[TB * H + tid] = s;
+    }
+    if (warp == 0) tc::tmem_dealloc(taddr, H);
+}
+
+// Sums the per-CTA dW / db partials in a fixed order into the flat gradient.
+__global__ void k_mpnn_reduce_dw(const float* partials, int nparts, int KF, float* gW, float* gb)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int total = KF * H + H;
+    if (idx >= total) return;
+    const int src = idx < KF * H ? idx : TB * H + (idx - KF * H);
+    double s = 0;
+    for (int p = 0; p < nparts; ++p) s += partials[(int64_t)p * (TB * H + H) + src];
+    if (idx < KF * H) gW[idx] = (float)s;
+    else gb[idx - KF * H] = (float)s;
+}
+
+__global__ void k_mpnn_reduce_dec(const double* partials, int nparts, float* gwd, float* gbd, double* loss)
+{
+    const int idx = threadIdx.x;
+    if (idx >= H + 2) return;
+    double s = 0;
+    for (int p = 0; p < nparts; ++p) s += partials[(int64_t)p * (H + 2) + idx];
+    if (idx < H) gwd[idx] = (float)s;
+    else if (idx == H) gbd[0] = (float)s;
+    else *loss = s;
+}
+
+// Adam on the FP32 master parameters, then the BF16 copies in both layouts.
+__global__ void k_mpnn_adam(float* params, const float* grads, float* m1, float* m2, int n, float lr, float b1,
+                            float b2, float eps, float c1, float c2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float g = grads[i];
+    const float a = b1 * m1[i] + (1.f - b1) * g;
+    const float b = b2 * m2[i] + (1.f - b2) * g * g;
+    m1[i] = a;
+    m2[i] = b;
+    params[i] -= lr * (a / c1) / (sqrtf(b / c2) + eps);
+}
+
+// w_fwd[n][k] = W[k][n] and w_bwd[k][n] = W[k][n] (BF16) for one layer.
+__global__ void k_mpnn_publish(const float* W, int K, __nv_bfloat16* wf, __nv_bfloat16* wb)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= K * H) return;
+    const int k = i / H, n = i % H;
+    const __nv_bfloat16 v = __float2bfloat16(W[i]);
+    wf[n * K + k] = v;
+    if (wb) wb[i] = v;
+}
+
+}  // namespace
+
+// ---- launchers -----------------------------------------------------------------------
+
+static int mpnn_grid(int64_t F)
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t tiles = (F + TB - 1) / TB;
+    const int64_t g = (int64_t)(sms > 0 ? sms : 152) * 4;
+    return (int)(tiles < g ? (tiles > 0 ? tiles : 1) : g);
+}
+
+int mpnn_grid_size(int64_t F) { return mpnn_grid(F); }
+
+template <typename Kern>
+static void set_smem(Kern k, int bytes)
+{
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+// Every tensor-core kernel requests at least this much shared memory, so at
+// most 4 CTAs share an SM and their TMEM allocations (<= 128 columns each)
+// never exceed the SM's 512 columns.
+constexpr int kMinSmem = 56 * 1024;
+static int smem_req(int need) { return need > kMinSmem ? need : kMinSmem; }
+
+void mpnn_forward(const MpnnView& V, bool train, cudaStream_t s)
+{
+    const int g = mpnn_grid(V.F);
+    const int sm16 = smem_req((TB + H) * 16 * 2), sm128 = smem_req((TB + H) * 2 * H * 2);
+    if (train) {
+        set_smem(k_mpnn_layer<16, true>, sm16);
+        set_smem(k_mpnn_layer<128, true>, sm128);
+        k_mpnn_layer<16, true><<<g, TB, sm16, s>>>(V, 0);
+        for (int l = 1; l <= kMpnnLayers; ++l) k_mpnn_layer<128, true><<<g, TB, sm128, s>>>(V, l);
+    }
+    else {
+        set_smem(k_mpnn_layer<16, false>, sm16);
+        set_smem(k_mpnn_layer<128, false>, sm128);
+        k_mpnn_layer<16, false><<<g, TB, sm16, s>>>(V, 0);
+        for (int l = 1; l <= kMpnnLayers; ++l) k_mpnn_layer<128, false><<<g, TB, sm128, s>>>(V, l);
+    }
+}
+
+void mpnn_guess(const MpnnView& V, const double* base, double sd, const double* rhs, double* guess, cudaStream_t s)
+{
+    k_mpnn_decode<false><<<mpnn_grid(V.F), 256, 0, s>>>(V, base, sd, rhs, nullptr, guess, 0.0);
+}
+
+void mpnn_backward(const MpnnView& V, const double* target, double inv_nt, MpnnGrads& G, cudaStream_t s)
+{
+    const int gdec = mpnn_grid(V.F);
+    k_mpnn_decode<true><<<gdec, 256, 0, s>>>(V, nullptr, 0.0, nullptr, target, nullptr, inv_nt);
+    k_mpnn_reduce_dec<<<1, 128, 0, s>>>(V.dec_partials, gdec, G.g + G.off_wd, G.g + G.off_bd, G.loss);
+    const int g = mpnn_grid(V.F);
+    const int smdx = smem_req((TB + 2 * H) * H * 2);
+    const int smdw = smem_req((TB + H) * TB * 2);
+    set_smem(k_mpnn_bwd_dx, smdx);
+    set_smem(k_mpnn_bwd_dw<128>, smdw);
+    set_smem(k_mpnn_bwd_dw<16>, smdw);
+    const unsigned gadd = (unsigned)((V.F * 16 + 255) / 256);
+    for (int l = kMpnnLayers; l >= 1; --l) {
+        k_mpnn_bwd_dx<<<g, TB, smdx, s>>>(V, l);
+        k_mpnn_bwd_dw<128><<<g, TB, smdw, s>>>(V, l, G.partials);
+        k_mpnn_reduce_dw<<<(2 * H * H + H + 255) / 256, 256, 0, s>>>(G.partials, g, 2 * H, G.g + G.off_W[l],
+                                                                      G.g + G.off_b[l]);
+        k_mpnn_gather_add<<<gadd, 256, 0, s>>>(V);
+    }
+    k_mpnn_dz0<<<(unsigned)((V.F * (H / 2) + 255) / 256), 256, 0, s>>>(V);
+    k_mpnn_bwd_dw<16><<<g, TB, smdw, s>>>(V, 0, G.partials);
+    k_mpnn_reduce_dw<<<(16 * H + H + 255) / 256, 256, 0, s>>>(G.partials, g, 16, G.g + G.off_W[0], G.g + G.off_b[0]);
+}
+
+void mpnn_adam(float* params, const float* grads, float* m1, float* m2, int n, float lr, int t, cudaStream_t s)
+{
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - powf(b1, (float)t), c2 = 1.f - powf(b2, (float)t);
+    k_mpnn_adam<<<(n + 255) / 256, 256, 0, s>>>(params, grads, m1, m2, n, lr, b1, b2, 1e-8f, c1, c2);
+}
+
+void mpnn_publish(const float* W, int K, __nv_bfloat16* wf, __nv_bfloat16* wb, cudaStream_t s)
+{
+    k_mpnn_publish<<<(K * H + 255) / 256, 256, 0, s>>>(W, K, wf, wb);
+}
+
+int mpnn_partials_floats(int64_t F) { return mpnn_grid(F) * (TB * H + H); }
+
+}  // namespace mhfem

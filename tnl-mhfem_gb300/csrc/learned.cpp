@@ -1,0 +1,575 @@
+// Learned warm-start form: host orchestration of the message-passing network
+// (k_mpnn.cu) around the unchanged FP64 BiCGStab solve.
+//
+// Per time step (after the assembly):
+//   1. Zn = the previous step's traces (the default warm start);
+//   2. once the network is trained: guess = 2 Zn - Zn1 + sd * net(features);
+//      the guess replaces the warm start only if its relative residual
+//      ||b - A x|| / ||b|| is smaller than the warm start's;
+//   3. the FP64 BiCGStab runs to the same tolerance as the plain form, so the
+//      network can only change the iteration count;
+//   4. during the first `train_steps` steps the network is trained online
+//      (Adam) on the solution the method just produced.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "handle.h"
+#include "mpnn.h"
+
+namespace mhfem {
+
+struct LearnedState {
+    bool ready = false;
+    int64_t F = 0;
+    int64_t free_rows = 0;
+    uint8_t* deg = nullptr;
+    uint8_t* fixed = nullptr;
+    float* stat = nullptr;
+    float* f_base = nullptr;
+    float* f_psi = nullptr;
+    double f_norm = 1.0;
+    __nv_bfloat16* x0 = nullptr;
+    __nv_bfloat16* h[kMpnnLayers + 2] = {};
+    __nv_bfloat16* a[kMpnnLayers + 1] = {};
+    __nv_bfloat16* z[kMpnnLayers + 1] = {};
+    __nv_bfloat16* dz = nullptr;
+    float* dh = nullptr;
+    float* ga = nullptr;
+    float* params = nullptr;
+    float* grads = nullptr;
+    float* m1 = nullptr;
+    float* m2 = nullptr;
+    __nv_bfloat16* w_fwd[kMpnnLayers + 1] = {};
+    __nv_bfloat16* w_bwd[kMpnnLayers + 1] = {};
+    double* dec_partials = nullptr;
+    float* dw_partials = nullptr;
+    double* loss = nullptr;
+    double* scal = nullptr;
+    double* scal_partials = nullptr;
+    double* Zn = nullptr;
+    double* Zn1 = nullptr;
+    double* base = nullptr;
+    double* guess = nullptr;
+    double* target = nullptr;
+    float* out = nullptr;
+    double* host = nullptr;  // pinned: scales, residuals, loss
+    int32_t* err = nullptr;
+    int hist = 0;
+    int trained_steps = 0;
+    int adam_t = 0;
+    bool params_set = false;
+    // options
+    int train_steps = 200;
+    int train_iters = 2;
+    float lr = 1e-3f;
+    int use_during_training = 0;
+    uint64_t seed = 1234;
+    double last_loss = -1;
+    std::vector<void*> allocs;
+};
+
+namespace {
+
+constexpr int H = kMpnnHidden;
+
+int off_W(int l) { return l == 0 ? 0 : kMpnnFeatures * H + H + (l - 1) * (2 * H * H + H); }
+int off_b(int l) { return off_W(l) + (l == 0 ? kMpnnFeatures : 2 * H) * H; }
+int off_wd() { return off_W(kMpnnLayers + 1); }
+int off_bd() { return off_wd() + H; }
+
+template <typename T>
+cudaError_t lalloc(LearnedState* L, T** p, size_t n)
+{
+    *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * n);
+    if (e == cudaSuccess) L->allocs.push_back((void*)*p);
+    return e;
+}
+
+#define LCK(call)                                                                                   \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return fail(h, e_ == cudaErrorMemoryAllocation ? MHFEM_ERR_OUT_OF_MEMORY : MHFEM_ERR_CUDA, \
+                        "%s failed: %s", #call, cudaGetErrorString(e_));                            \
+    } while (0)
+
+// splitmix64 + Box-Muller: deterministic initial weights
+struct Rng {
+    uint64_t s;
+    uint64_t next()
+    {
+        uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    }
+    double uniform() { return ((next() >> 11) + 0.5) * (1.0 / 9007199254740992.0); }
+    double normal() { return std::sqrt(-2.0 * std::log(uniform())) * std::cos(6.283185307179586 * uniform()); }
+};
+
+void init_params_host(std::vector<float>& p, uint64_t seed)
+{
+    Rng r{seed};
+    p.assign(kMpnnParams, 0.f);
+    for (int i = 0; i < kMpnnFeatures * H; ++i) p[off_W(0) + i] = (float)(r.normal() * std::sqrt(2.0 / kMpnnFeatures));
+    for (int l = 1; l <= kMpnnLayers; ++l)
+        for (int i = 0; i < 2 * H * H; ++i) p[off_W(l) + i] = (float)(r.normal() * std::sqrt(1.0 / (2 * H)));
+    for (int i = 0; i < H; ++i) p[off_wd() + i] = (float)(r.normal() * 0.01);
+}
+
+MpnnView make_view(mhfem_t h)
+{
+    LearnedState* L = h->learned;
+    MpnnView V;
+    V.F = L->F;
+    V.W = h->A.width;
+    V.nbr = h->A.cols;
+    V.deg = L->deg;
+    V.fixed = L->fixed;
+    V.x0 = L->x0;
+    for (int l = 0; l < kMpnnLayers + 2; ++l) V.h[l] = L->h[l];
+    for (int l = 0; l < kMpnnLayers + 1; ++l) {
+        V.a[l] = L->a[l];
+        V.z[l] = L->z[l];
+        V.w_fwd[l] = L->w_fwd[l];
+        V.w_bwd[l] = L->w_bwd[l];
+        V.bias[l] = L->params + off_b(l);
+    }
+    V.dz = L->dz;
+    V.dh = L->dh;
+    V.ga = L->ga;
+    V.wd = L->params + off_wd();
+    V.bd = L->params + off_bd();
+    V.dec_partials = L->dec_partials;
+    V.err = L->err;
+    return V;
+}
+
+MpnnGrads make_grads(mhfem_t h)
+{
+    LearnedState* L = h->learned;
+    MpnnGrads G;
+    G.g = L->grads;
+    for (int l = 0; l <= kMpnnLayers; ++l) {
+        G.off_W[l] = off_W(l);
+        G.off_b[l] = off_b(l);
+    }
+    G.off_wd = off_wd();
+    G.off_bd = off_bd();
+    G.partials = L->dw_partials;
+    G.loss = L->loss;
+    return G;
+}
+
+void publish(mhfem_t h)
+{
+    LearnedState* L = h->learned;
+    for (int l = 0; l <= kMpnnLayers; ++l)
+        mpnn_publish(L->params + off_W(l), l == 0 ? kMpnnFeatures : 2 * H, L->w_fwd[l], l == 0 ? nullptr : L->w_bwd[l],
+                     h->stream);
+}
+
+double coef_at(mhfem_t h, int which, int64_t idx, double dflt)
+{
+    const auto& c = h->h_coef[which];
+    if (c.empty()) return dflt;
+    return c.size() == 1 ? c[0] : c[idx];
+}
+
+}  // namespace
+
+void learned_invalidate(mhfem_t h)
+{
+    if (h->learned) h->learned->ready = false;
+}
+
+void learned_release(mhfem_t h)
+{
+    if (!h->learned) return;
+    for (void* p : h->learned->allocs) cudaFree(p);
+    if (h->learned->host) cudaFreeHost(h->learned->host);
+    delete h->learned;
+    h->learned = nullptr;
+}
+
+// Allocates the network state for the current pattern and builds the static features.
+static mhfem_status learned_prepare(mhfem_t h)
+{
+    if (!h->learned) h->learned = new LearnedState();
+    LearnedState* L = h->learned;
+    if (L->ready && L->F == h->topo.F) return MHFEM_OK;
+    if (h->n != 1) return fail(h, MHFEM_ERR_UNSUPPORTED, "the learned form supports one equation (n = 1)");
+    const int64_t F = h->topo.F, C = h->topo.C;
+    const int nf = h->nf, dim = h->dim;
+    // keep options and parameters across re-preparation
+    const bool had_params = L->params_set;
+    std::vector<float> keep;
+    if (had_params && L->params) {
+        keep.resize(kMpnnParams);
+        cudaMemcpy(keep.data(), L->params, sizeof(float) * kMpnnParams, cudaMemcpyDeviceToHost);
+    }
+    for (void* p : L->allocs) cudaFree(p);
+    L->allocs.clear();
+    L->F = F;
+
+    // graph: degree (non-padding ELL entries) and Dirichlet rows
+    std::vector<uint8_t> deg(F, 0), fixed(F, 0);
+    const int W = h->pat.W;
+    for (int64_t E = 0; E < F; ++E) {
+        int d = 0;
+        for (int k = 0; k < W; ++k)
+            if (h->pat.ell_cols[(size_t)k * F + E] != (int32_t)E) ++d;
+        deg[E] = (uint8_t)d;
+        fixed[E] = (h->topo.face_cells[2 * E + 1] < 0 && h->h_tags[E] == MHFEM_BC_FIXED_VALUE) ? 1 : 0;
+    }
+    int64_t nfree = 0;
+    for (int64_t E = 0; E < F; ++E) nfree += fixed[E] ? 0 : 1;
+    L->free_rows = nfree;
+
+    // static features
+    std::vector<float> stat((size_t)F * 16, 0.f), fb(F, 0.f), fp(F, 0.f);
+    double mean_area = 0;
+    for (int64_t E = 0; E < F; ++E) mean_area += h->topo.face_measure[E];
+    mean_area = F > 0 ? mean_area / F : 1.0;
+    std::vector<double> logD(F, 0.0);
+    double lmean = 0, lsq = 0;
+    double fmax = 0;
+    for (int64_t E = 0; E < F; ++E) {
+        const int32_t K0 = h->topo.face_cells[2 * E], K1 = h->topo.face_cells[2 * E + 1];
+        double ld = std::log(std::max(coef_at(h, MHFEM_COEF_D, K0, 1.0), 1e-300));
+        double f0 = coef_at(h, MHFEM_COEF_F, K0, 0.0), p0 = coef_at(h, MHFEM_COEF_PSI, K0, 0.0);
+        if (K1 >= 0) {
+            ld = 0.5 * (ld + std::log(std::max(coef_at(h, MHFEM_COEF_D, K1, 1.0), 1e-300)));
+            f0 = 0.5 * (f0 + coef_at(h, MHFEM_COEF_F, K1, 0.0));
+            p0 = 0.5 * (p0 + coef_at(h, MHFEM_COEF_PSI, K1, 0.0));
+        }
+        logD[E] = ld;
+        lmean += ld;
+        lsq += ld * ld;
+        fb[E] = (float)f0;
+        fp[E] = (float)p0;
+        fmax = std::max(fmax, std::fabs(f0) + std::fabs(h->src_amp * p0));
+    }
+    lmean /= std::max<int64_t>(F, 1);
+    const double lsd = std::sqrt(std::max(lsq / std::max<int64_t>(F, 1) - lmean * lmean, 0.0));
+    L->f_norm = fmax > 0 ? 1.0 / fmax : 0.0;
+    for (int64_t E = 0; E < F; ++E) {
+        float* s = &stat[(size_t)E * 16];
+        s[3] = (float)(lsd > 0 ? (logD[E] - lmean) / lsd : 0.0);
+        // unit normal, sign-free
+        const int32_t* fv = &h->topo.face_verts[(size_t)E * dim];
+        double n[3] = {0, 0, 0};
+        const double* X0 = &h->h_coords[(size_t)fv[0] * dim];
+        const double* X1 = &h->h_coords[(size_t)fv[1] * dim];
+        if (dim == 2) {
+            n[0] = X1[1] - X0[1];
+            n[1] = -(X1[0] - X0[0]);
+        }
+        else {
+            const double* X2 = &h->h_coords[(size_t)fv[2] * dim];
+            const double a[3] = {X1[0] - X0[0], X1[1] - X0[1], X1[2] - X0[2]};
+            const double b[3] = {X2[0] - X0[0], X2[1] - X0[1], X2[2] - X0[2]};
+            n[0] = a[1] * b[2] - a[2] * b[1];
+            n[1] = a[2] * b[0] - a[0] * b[2];
+            n[2] = a[0] * b[1] - a[1] * b[0];
+        }
+        const double nn = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        for (int d = 0; d < 3; ++d) s[5 + d] = (float)(nn > 0 ? std::fabs(n[d]) / nn : 0.0);
+        s[8] = (float)(h->topo.face_measure[E] / mean_area);
+        s[9] = h->topo.face_cells[2 * E + 1] < 0 ? 1.f : 0.f;
+        s[10] = fixed[E] ? 1.f : 0.f;
+        s[11] = 1.f;
+    }
+    (void)C;
+    (void)nf;
+
+    LCK(lalloc(L, &L->deg, F));
+    LCK(cudaMemcpy(L->deg, deg.data(), F, cudaMemcpyHostToDevice));
+    LCK(lalloc(L, &L->fixed, F));
+    LCK(cudaMemcpy(L->fixed, fixed.data(), F, cudaMemcpyHostToDevice));
+    LCK(lalloc(L, &L->stat, (size_t)F * 16));
+    LCK(cudaMemcpy(L->stat, stat.data(), sizeof(float) * F * 16, cudaMemcpyHostToDevice));
+    LCK(lalloc(L, &L->f_base, F));
+    LCK(cudaMemcpy(L->f_base, fb.data(), sizeof(float) * F, cudaMemcpyHostToDevice));
+    LCK(lalloc(L, &L->f_psi, F));
+    LCK(cudaMemcpy(L->f_psi, fp.data(), sizeof(float) * F, cudaMemcpyHostToDevice));
+    LCK(lalloc(L, &L->x0, (size_t)F * 16));
+    for (int l = 1; l <= kMpnnLayers + 1; ++l) LCK(lalloc(L, &L->h[l], (size_t)F * H));
+    for (int l = 1; l <= kMpnnLayers; ++l) LCK(lalloc(L, &L->a[l], (size_t)F * H));
+    for (int l = 0; l <= kMpnnLayers; ++l) LCK(lalloc(L, &L->z[l], (size_t)F * H));
+    LCK(lalloc(L, &L->dz, (size_t)F * H));
+    LCK(lalloc(L, &L->dh, (size_t)F * H));
+    LCK(lalloc(L, &L->ga, (size_t)F * H));
+    LCK(lalloc(L, &L->params, kMpnnParams));
+    LCK(lalloc(L, &L->grads, kMpnnParams));
+    LCK(lalloc(L, &L->m1, kMpnnParams));
+    LCK(lalloc(L, &L->m2, kMpnnParams));
+    LCK(cudaMemset(L->m1, 0, sizeof(float) * kMpnnParams));
+    LCK(cudaMemset(L->m2, 0, sizeof(float) * kMpnnParams));
+    for (int l = 0; l <= kMpnnLayers; ++l) {
+        const int K = l == 0 ? kMpnnFeatures : 2 * H;
+        LCK(lalloc(L, &L->w_fwd[l], (size_t)K * H));
+        LCK(lalloc(L, &L->w_bwd[l], (size_t)K * H));
+    }
+    LCK(lalloc(L, &L->dec_partials, (size_t)mpnn_grid_size(F) * (H + 2)));
+    LCK(lalloc(L, &L->dw_partials, (size_t)mpnn_partials_floats(F)));
+    LCK(lalloc(L, &L->loss, 1));
+    LCK(lalloc(L, &L->scal, 2));
+    LCK(lalloc(L, &L->scal_partials, 256 * 3 + 1));
+    LCK(cudaMemset(L->scal_partials, 0, sizeof(double) * (256 * 3 + 1)));
+    LCK(lalloc(L, &L->Zn, F));
+    LCK(lalloc(L, &L->Zn1, F));
+    LCK(lalloc(L, &L->base, F));
+    LCK(lalloc(L, &L->guess, F));
+    LCK(lalloc(L, &L->target, F));
+    LCK(lalloc(L, &L->out, F));
+    LCK(lalloc(L, &L->err, 1));
+    LCK(cudaMemset(L->err, 0, sizeof(int32_t)));
+    if (!L->host) LCK(cudaMallocHost((void**)&L->host, sizeof(double) * 8));
+    std::vector<float> p0;
+    if (had_params && !keep.empty()) p0 = keep;
+    else init_params_host(p0, L->seed);
+    LCK(cudaMemcpy(L->params, p0.data(), sizeof(float) * kMpnnParams, cudaMemcpyHostToDevice));
+    L->params_set = true;
+    publish(h);
+    LCK(cudaStreamSynchronize(h->stream));
+    L->hist = 0;
+    L->ready = true;
+    return MHFEM_OK;
+}
+
+static mhfem_status check_err(mhfem_t h)
+{
+    LearnedState* L = h->learned;
+    int32_t e = 0;
+    LCK(cudaMemcpyAsync(&L->host[7], L->err, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    LCK(cudaStreamSynchronize(h->stream));
+    std::memcpy(&e, &L->host[7], sizeof(int32_t));
+    if (e) return fail(h, MHFEM_ERR_CUDA, "tensor-core kernel reported error flags 0x%x (mbarrier wait timed out)", e);
+    return MHFEM_OK;
+}
+
+static mhfem_status train_once(mhfem_t h, int iters)
+{
+    LearnedState* L = h->learned;
+    MpnnView V = make_view(h);
+    MpnnGrads G = make_grads(h);
+    const double inv_nt = L->free_rows > 0 ? 1.0 / (double)L->free_rows : 0.0;
+    for (int it = 0; it < iters; ++it) {
+        mpnn_forward(V, true, h->stream);
+        mpnn_backward(V, L->target, inv_nt, G, h->stream);
+        L->adam_t += 1;
+        mpnn_adam(L->params, L->grads, L->m1, L->m2, kMpnnParams, L->lr, L->adam_t, h->stream);
+        publish(h);
+        h->launches += 4 + 2 + 4 * kMpnnLayers + 3 + 1 + 4;
+    }
+    LCK(cudaMemcpyAsync(&L->host[4], L->loss, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    LCK(cudaGetLastError());
+    return MHFEM_OK;
+}
+
+mhfem_status learned_solve(mhfem_t h, int* iters, double* res, mhfem_step_stats* stats)
+{
+    mhfem_status st = learned_prepare(h);
+    if (st) return st;
+    LearnedState* L = h->learned;
+    const int64_t F = L->F;
+    cudaStream_t s = h->stream;
+    LCK(cudaMemcpyAsync(L->Zn, h->Z_iF, sizeof(double) * F, cudaMemcpyDeviceToDevice, s));
+    const bool have_hist = L->hist >= 1;
+    const bool training = L->trained_steps < L->train_steps;
+    const bool infer = have_hist && (!training || L->use_during_training) && L->trained_steps > 0;
+    double sz = 0, sd = 0;
+    MpnnInputs in{};
+    in.Zn = L->Zn;
+    in.Zn1 = L->Zn1;
+    in.rhs = h->rhs;
+    in.stat = L->stat;
+    in.f_base = L->f_base;
+    in.f_psi = L->f_psi;
+    in.src_scale = h->src_amp * std::sin(2.0 * M_PI * h->cur_t / h->src_period);
+    in.f_norm = L->f_norm;
+    if (have_hist) {
+        mpnn_scales(F, in, L->fixed, L->scal_partials, L->scal, s);
+        LCK(cudaMemcpyAsync(L->host, L->scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        LCK(cudaStreamSynchronize(s));
+        sz = L->host[0];
+        sd = L->host[1];
+        h->launches += 1;
+    }
+    int used = 0;
+    double r_warm = -1, r_guess = -1;
+    const bool have_features = have_hist && sd > 0 && sz > 0;
+    if (have_features) {
+        mpnn_base(F, L->Zn, L->Zn1, L->base, s);
+        mpnn_features(F, in, sz, sd, L->x0, s);
+        h->launches += 2;
+    }
+    if (infer && have_features) {
+        MpnnView V = make_view(h);
+        mpnn_forward(V, false, s);
+        mpnn_guess(V, L->base, sd, h->rhs, L->guess, s);
+        residual_norm_fp64(h->A, h->rhs, L->Zn, h->W, s);
+        LCK(cudaMemcpyAsync(&L->host[2], &h->W.sc->res, sizeof(double), cudaMemcpyDeviceToHost, s));
+        residual_norm_fp64(h->A, h->rhs, L->guess, h->W, s);
+        LCK(cudaMemcpyAsync(&L->host[3], &h->W.sc->res, sizeof(double), cudaMemcpyDeviceToHost, s));
+        LCK(cudaStreamSynchronize(s));
+        h->launches += (kMpnnLayers + 1) + 1 + 2;
+        if ((st = check_err(h)) != MHFEM_OK) return st;
+        r_warm = L->host[2];
+        r_guess = L->host[3];
+        if (std::isfinite(r_guess) && r_guess < r_warm) {
+            LCK(cudaMemcpyAsync(h->Z_iF, L->guess, sizeof(double) * F, cudaMemcpyDeviceToDevice, s));
+            used = 1;
+        }
+    }
+    st = run_fp64(h, h->opts.tol, h->opts.max_iter, iters, res);
+    if (st) return st;
+    if (training && have_features) {
+        mpnn_target(F, h->Z_iF, L->base, sd, L->target, s);
+        h->launches += 1;
+        if ((st = train_once(h, L->train_iters)) != MHFEM_OK) return st;
+        LCK(cudaStreamSynchronize(s));
+        if ((st = check_err(h)) != MHFEM_OK) return st;
+        L->last_loss = L->host[4];
+        L->trained_steps += 1;
+    }
+    std::swap(L->Zn, L->Zn1);  // Zn1 <- the traces this step started from
+    L->hist += 1;
+    if (stats) {
+        stats->guess_used = used;
+        stats->guess_residual = r_guess;
+        stats->warm_residual = r_warm;
+    }
+    return MHFEM_OK;
+}
+
+}  // namespace mhfem
+
+using namespace mhfem;
+
+namespace {
+
+mhfem_status ready_for_learning(mhfem_t h)
+{
+    if (!h) return MHFEM_ERR_INVALID_ARGUMENT;
+    if (!h->has_mesh) return fail(h, MHFEM_ERR_STATE, "mhfem_set_mesh has not been called");
+    if (!h->pattern_ready) {
+        mhfem_status st = mhfem_setup_linear_system(h);
+        if (st) return st;
+    }
+    return learned_prepare(h);
+}
+
+}  // namespace
+
+extern "C" {
+
+mhfem_status mhfem_learned_set_options(mhfem_t h, const mhfem_learned_opts* o)
+{
+    if (!h || !o) return MHFEM_ERR_INVALID_ARGUMENT;
+    if (o->train_steps < 0 || o->train_iters < 1 || !(o->learning_rate > 0))
+        return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "invalid learned-form options");
+    if (!h->learned) h->learned = new LearnedState();
+    LearnedState* L = h->learned;
+    L->train_steps = o->train_steps;
+    L->train_iters = o->train_iters;
+    L->lr = (float)o->learning_rate;
+    L->use_during_training = o->use_during_training;
+    if (o->seed != 0 && o->seed != L->seed) {
+        L->seed = o->seed;
+        L->params_set = false;
+        L->ready = false;
+    }
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_learned_get_params(mhfem_t h, float* params, int64_t count)
+{
+    mhfem_status st = ready_for_learning(h);
+    if (st) return st;
+    if (!params || count != kMpnnParams)
+        return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "the network has %d parameters", kMpnnParams);
+    LCK(cudaMemcpyAsync(params, h->learned->params, sizeof(float) * kMpnnParams, cudaMemcpyDeviceToHost, h->stream));
+    LCK(cudaStreamSynchronize(h->stream));
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_learned_set_params(mhfem_t h, const float* params, int64_t count)
+{
+    mhfem_status st = ready_for_learning(h);
+    if (st) return st;
+    if (!params || count != kMpnnParams)
+        return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "the network has %d parameters", kMpnnParams);
+    LearnedState* L = h->learned;
+    LCK(cudaMemcpyAsync(L->params, params, sizeof(float) * kMpnnParams, cudaMemcpyHostToDevice, h->stream));
+    LCK(cudaMemsetAsync(L->m1, 0, sizeof(float) * kMpnnParams, h->stream));
+    LCK(cudaMemsetAsync(L->m2, 0, sizeof(float) * kMpnnParams, h->stream));
+    L->adam_t = 0;
+    publish(h);
+    LCK(cudaStreamSynchronize(h->stream));
+    L->params_set = true;
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_learned_forward(mhfem_t h, const float* features, float* out)
+{
+    mhfem_status st = ready_for_learning(h);
+    if (st) return st;
+    if (!features || !out) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "null buffers");
+    LearnedState* L = h->learned;
+    const int64_t F = L->F;
+    float* dfeat = nullptr;
+    LCK(cudaMalloc((void**)&dfeat, sizeof(float) * F * 16));
+    cudaMemcpyAsync(dfeat, features, sizeof(float) * F * 16, cudaMemcpyHostToDevice, h->stream);
+    mpnn_features_from_host(F, dfeat, L->x0, h->stream);
+    MpnnView V = make_view(h);
+    mpnn_forward(V, false, h->stream);
+    mpnn_out(V, L->out, h->stream);
+    cudaMemcpyAsync(out, L->out, sizeof(float) * F, cudaMemcpyDeviceToHost, h->stream);
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    cudaFree(dfeat);
+    if (e != cudaSuccess) return fail(h, MHFEM_ERR_CUDA, "learned forward: %s", cudaGetErrorString(e));
+    return check_err(h);
+}
+
+mhfem_status mhfem_learned_gradients(mhfem_t h, const float* features, const double* target, float* grads,
+                                     double* loss)
+{
+    mhfem_status st = ready_for_learning(h);
+    if (st) return st;
+    if (!features || !target || !grads) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "null buffers");
+    LearnedState* L = h->learned;
+    const int64_t F = L->F;
+    float* dfeat = nullptr;
+    LCK(cudaMalloc((void**)&dfeat, sizeof(float) * F * 16));
+    cudaMemcpyAsync(dfeat, features, sizeof(float) * F * 16, cudaMemcpyHostToDevice, h->stream);
+    cudaMemcpyAsync(L->target, target, sizeof(double) * F, cudaMemcpyHostToDevice, h->stream);
+    mpnn_features_from_host(F, dfeat, L->x0, h->stream);
+    MpnnView V = make_view(h);
+    MpnnGrads G = make_grads(h);
+    mpnn_forward(V, true, h->stream);
+    const double inv_nt = L->free_rows > 0 ? 1.0 / (double)L->free_rows : 0.0;
+    mpnn_backward(V, L->target, inv_nt, G, h->stream);
+    cudaMemcpyAsync(grads, L->grads, sizeof(float) * kMpnnParams, cudaMemcpyDeviceToHost, h->stream);
+    cudaMemcpyAsync(&L->host[5], L->loss, sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    cudaFree(dfeat);
+    if (e != cudaSuccess) return fail(h, MHFEM_ERR_CUDA, "learned gradients: %s", cudaGetErrorString(e));
+    if (loss) *loss = L->host[5];
+    return check_err(h);
+}
+
+mhfem_status mhfem_learned_status(mhfem_t h, int32_t* trained_steps, double* last_loss, int32_t* num_params)
+{
+    if (!h) return MHFEM_ERR_INVALID_ARGUMENT;
+    if (trained_steps) *trained_steps = h->learned ? h->learned->trained_steps : 0;
+    if (last_loss) *last_loss = h->learned ? h->learned->last_loss : -1;
+    if (num_params) *num_params = kMpnnParams;
+    return MHFEM_OK;
+}
+
+}  // extern "C"

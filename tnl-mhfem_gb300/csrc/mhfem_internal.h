@@ -111,7 +111,7 @@ void krylov_iterate_fp64(const EllMatrix& A, double* x, KrylovWork& W, int iters
 // mixed: outer residual r = b - A x (FP64) -> sc; scale into r32; inner FP32 solve; x += scale*e
 void mixed_outer_residual(const EllMatrix& A, const double* b, const double* x, KrylovWork& W,
                           double tol, int max_sweeps, cudaStream_t s);
-void mixed_inner_init(KrylovWork& W, double inner_tol, int max_iter, cudaStream_t s);
+void mixed_inner_init(KrylovWork& W, double inner_tol, int adaptive, int max_iter, cudaStream_t s);
 void krylov_iterate_fp32(const EllMatrix& A, KrylovWork& W, int iters, cudaStream_t s);
 void mixed_apply_correction(double* x, KrylovWork& W, cudaStream_t s);
 

@@ -1,0 +1,75 @@
+// Device views and launchers of the learned warm-start network (k_mpnn.cu).
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+namespace mhfem {
+
+constexpr int kMpnnHidden = 64;
+constexpr int kMpnnFeatures = 16;
+constexpr int kMpnnLayers = 3;
+// FP32 master parameters: W0 [16][64], b0, W1..W3 [128][64], b1..b3, wd [64], bd
+constexpr int kMpnnParams = kMpnnFeatures * kMpnnHidden + kMpnnHidden
+                          + kMpnnLayers * (2 * kMpnnHidden * kMpnnHidden + kMpnnHidden) + kMpnnHidden + 1;
+
+struct MpnnView {
+    int64_t F = 0;
+    int W = 0;
+    const int32_t* nbr = nullptr;     // [W][F], padding = own index
+    const uint8_t* deg = nullptr;     // [F]
+    const uint8_t* fixed = nullptr;   // [F] Dirichlet rows (excluded from the loss, guess = rhs)
+    __nv_bfloat16* x0 = nullptr;      // [F][16]
+    __nv_bfloat16* h[kMpnnLayers + 2] = {};  // h[1..4] [F][64]
+    __nv_bfloat16* a[kMpnnLayers + 1] = {};  // a[1..3] [F][64] (training)
+    __nv_bfloat16* z[kMpnnLayers + 1] = {};  // z[0..3] [F][64] (training)
+    __nv_bfloat16* dz = nullptr;      // [F][64]
+    float* dh = nullptr;              // [F][64]
+    float* ga = nullptr;              // [F][64]
+    const __nv_bfloat16* w_fwd[kMpnnLayers + 1] = {};  // [64][K_l]
+    const __nv_bfloat16* w_bwd[kMpnnLayers + 1] = {};  // [K_l][64]
+    const float* bias[kMpnnLayers + 1] = {};           // [64]
+    const float* wd = nullptr;        // [64]
+    const float* bd = nullptr;        // [1]
+    double* dec_partials = nullptr;   // [grid][66]
+    int32_t* err = nullptr;
+};
+
+struct MpnnGrads {
+    float* g = nullptr;               // flat, same layout as the master parameters
+    int off_W[kMpnnLayers + 1] = {}, off_b[kMpnnLayers + 1] = {}, off_wd = 0, off_bd = 0;
+    float* partials = nullptr;        // [grid][128*64 + 64]
+    double* loss = nullptr;
+};
+
+void mpnn_forward(const MpnnView& V, bool train, cudaStream_t s);
+// guess = 2 Zn - Zn1 + sd * out on free rows, rhs on Dirichlet rows
+void mpnn_guess(const MpnnView& V, const double* base, double sd, const double* rhs, double* guess, cudaStream_t s);
+void mpnn_backward(const MpnnView& V, const double* target, double inv_nt, MpnnGrads& G, cudaStream_t s);
+void mpnn_adam(float* params, const float* grads, float* m1, float* m2, int n, float lr, int t, cudaStream_t s);
+void mpnn_publish(const float* W, int K, __nv_bfloat16* wf, __nv_bfloat16* wb, cudaStream_t s);
+int mpnn_partials_floats(int64_t F);
+int mpnn_grid_size(int64_t F);
+
+// feature / target helpers (k_mpnn_io.cu)
+struct MpnnInputs {
+    const double* Zn;        // current face traces (warm start)
+    const double* Zn1;       // previous step's traces
+    const double* rhs;       // scaled right-hand side of the current system
+    const float* stat;       // [F][16] static features (channels 3, 5..11 filled)
+    const float* f_base;     // [F] face average of the source
+    const float* f_psi;      // [F] face average of the source shape psi
+    double src_scale;        // amplitude * sin(2 pi t / T)
+    double f_norm;           // scale of the source channel
+};
+// sz = rms(Zn), sd = rms(Zn - Zn1) over free rows -> scal[0], scal[1]
+void mpnn_scales(int64_t F, const MpnnInputs& in, const uint8_t* fixed, double* partials, double* scal, cudaStream_t s);
+void mpnn_features(int64_t F, const MpnnInputs& in, double sz, double sd, __nv_bfloat16* x0, cudaStream_t s);
+void mpnn_base(int64_t F, const double* Zn, const double* Zn1, double* base, cudaStream_t s);
+void mpnn_target(int64_t F, const double* Znew, const double* base, double sd, double* y, cudaStream_t s);
+void mpnn_features_from_host(int64_t F, const float* xf, __nv_bfloat16* x0, cudaStream_t s);
+void mpnn_out(const MpnnView& V, float* out, cudaStream_t s);
+
+}  // namespace mhfem

@@ -49,7 +49,16 @@ class Desc(ct.Structure):
 
 class SolverOpts(ct.Structure):
     _fields_ = [("tol", ct.c_double), ("max_iter", ct.c_int32), ("inner_tol", ct.c_double),
-                ("max_sweeps", ct.c_int32), ("check_every", ct.c_int32), ("timeout_s", ct.c_double)]
+                ("max_sweeps", ct.c_int32), ("check_every", ct.c_int32), ("timeout_s", ct.c_double),
+                ("inner_adaptive", ct.c_int32)]
+
+
+class LearnedOpts(ct.Structure):
+    _fields_ = [("train_steps", ct.c_int32), ("train_iters", ct.c_int32), ("learning_rate", ct.c_double),
+                ("use_during_training", ct.c_int32), ("seed", ct.c_uint64)]
+
+
+LEARNED_FEATURES = 16
 
 
 class StepStats(ct.Structure):
@@ -94,6 +103,12 @@ SIGNATURES = [
     ("mhfem_get_totals", ct.c_int32, [_P, _pi64, _pi64, _pi64]),
     ("mhfem_get_stream", ct.c_int32, [_P, ct.POINTER(ct.c_void_p)]),
     ("mhfem_time_kernel", ct.c_int32, [_P, ct.c_int32, ct.c_int32, _pd, _pd, _pd]),
+    ("mhfem_learned_set_options", ct.c_int32, [_P, ct.POINTER(LearnedOpts)]),
+    ("mhfem_learned_get_params", ct.c_int32, [_P, ct.POINTER(ct.c_float), ct.c_int64]),
+    ("mhfem_learned_set_params", ct.c_int32, [_P, ct.POINTER(ct.c_float), ct.c_int64]),
+    ("mhfem_learned_forward", ct.c_int32, [_P, ct.POINTER(ct.c_float), ct.POINTER(ct.c_float)]),
+    ("mhfem_learned_gradients", ct.c_int32, [_P, ct.POINTER(ct.c_float), _pd, ct.POINTER(ct.c_float), _pd]),
+    ("mhfem_learned_status", ct.c_int32, [_P, _pi32, _pd, _pi32]),
 ]
 
 _lib = None

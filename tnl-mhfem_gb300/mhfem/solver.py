@@ -121,8 +121,8 @@ class Solver:
                                        _dptr(dirichlet)))
 
     def setup(self, tol: float = 1e-10, max_iter: int = 10000, inner_tol: float = 1e-4, max_sweeps: int = 50,
-              check_every: int = 8, timeout_s: float = 0.0) -> None:
-        o = L.SolverOpts(tol, max_iter, inner_tol, max_sweeps, check_every, timeout_s)
+              check_every: int = 8, timeout_s: float = 0.0, inner_adaptive: bool = True) -> None:
+        o = L.SolverOpts(tol, max_iter, inner_tol, max_sweeps, check_every, timeout_s, int(inner_adaptive))
         self._ck(self.lib.mhfem_set_solver(self._h, ct.byref(o)))
 
     def setInitialCondition(self, Z_iK: np.ndarray, Z_iF: np.ndarray | None = None) -> None:
@@ -213,3 +213,45 @@ class Solver:
         ms = ct.c_double(); b = ct.c_double(); fl = ct.c_double()
         self._ck(self.lib.mhfem_time_kernel(self._h, kernel, reps, ct.byref(ms), ct.byref(b), ct.byref(fl)))
         return {"ms": ms.value, "bytes": b.value, "flops": fl.value}
+
+    # -- learned warm start (MHFEM_FORM_LEARNED) ------------------------
+    def learned_options(self, train_steps: int = 200, train_iters: int = 2, learning_rate: float = 1e-3,
+                        use_during_training: bool = False, seed: int = 0) -> None:
+        o = L.LearnedOpts(train_steps, train_iters, learning_rate, int(use_during_training), seed)
+        self._ck(self.lib.mhfem_learned_set_options(self._h, ct.byref(o)))
+
+    def learned_num_params(self) -> int:
+        n = ct.c_int32()
+        self._ck(self.lib.mhfem_learned_status(self._h, None, None, ct.byref(n)))
+        return n.value
+
+    def learned_params(self) -> np.ndarray:
+        out = np.empty(self.learned_num_params(), np.float32)
+        self._ck(self.lib.mhfem_learned_get_params(self._h, out.ctypes.data_as(ct.POINTER(ct.c_float)), out.size))
+        return out
+
+    def set_learned_params(self, params: np.ndarray) -> None:
+        p = np.ascontiguousarray(params, np.float32)
+        self._ck(self.lib.mhfem_learned_set_params(self._h, p.ctypes.data_as(ct.POINTER(ct.c_float)), p.size))
+
+    def learned_forward(self, features: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(features, np.float32)
+        assert x.shape == (self.F, L.LEARNED_FEATURES)
+        out = np.empty(self.F, np.float32)
+        self._ck(self.lib.mhfem_learned_forward(self._h, x.ctypes.data_as(ct.POINTER(ct.c_float)),
+                                                out.ctypes.data_as(ct.POINTER(ct.c_float))))
+        return out
+
+    def learned_gradients(self, features: np.ndarray, target: np.ndarray):
+        x = np.ascontiguousarray(features, np.float32)
+        y = np.ascontiguousarray(target, np.float64)
+        g = np.empty(self.learned_num_params(), np.float32)
+        loss = ct.c_double()
+        self._ck(self.lib.mhfem_learned_gradients(self._h, x.ctypes.data_as(ct.POINTER(ct.c_float)), _dptr(y),
+                                                  g.ctypes.data_as(ct.POINTER(ct.c_float)), ct.byref(loss)))
+        return loss.value, g
+
+    def learned_status(self):
+        ts = ct.c_int32(); ll = ct.c_double(); n = ct.c_int32()
+        self._ck(self.lib.mhfem_learned_status(self._h, ct.byref(ts), ct.byref(ll), ct.byref(n)))
+        return {"trained_steps": ts.value, "last_loss": ll.value, "num_params": n.value}
