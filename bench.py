@@ -53,6 +53,9 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--learned-train", type=int, default=200,
+                    help="online training steps of the learned form before its timed steps")
     ap.add_argument("--profile-run", action="store_true",
                     help="only the warm-up and timed steps (for an ncu launch list)")
     return ap.parse_args()
@@ -163,6 +166,75 @@ def run_reference_arm(args, rank, world):
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def learned_leg(args, dev, world):
+    """Learned warm start on the time-varying source workload
+    f = 1 + 0.5 sin(2 pi t / T) psi(x), T = 1000 dt: online training on the
+    first `learned_train` steps, then the same warm-up + timed steps for the
+    learned form and for the plain FP64 form started from the identical state."""
+    import numpy as np
+    import torch
+
+    from mhfem import _lib as L
+    from mhfem import problems
+
+    total = 1000
+    pl = problems.diffusion3d_source(N=args.grid, steps=total, form=L.FORM_LEARNED)
+    pl.config.device = dev
+    sl = problems.make_solver(pl, check_every=8)
+    sl.learned_options(train_steps=args.learned_train, train_iters=2, learning_rate=1e-3)
+    t = 0.0
+    t0 = time.perf_counter()
+    train_iters = []
+    for _ in range(args.learned_train):
+        train_iters.append(sl.step(t, pl.dt)["iterations"])
+        t += pl.dt
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    zf, zk = sl.state()
+    pf = problems.diffusion3d_source(N=args.grid, steps=total, form=L.FORM_FP64)
+    pf.config.device = dev
+    sf = problems.make_solver(pf, check_every=8)
+    sf.setInitialCondition(zk, zf)
+    for _ in range(args.warmup):
+        sl.step(t, pl.dt)
+        sf.step(t, pf.dt)
+        t += pl.dt
+    res = {}
+    for name, sol in (("learned", sl), ("fp64", sf)):
+        ext = torch.cuda.ExternalStream(sol.stream(), device=dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        tt = t
+        its, used = [], 0
+        torch.cuda.synchronize()
+        e0.record(ext)
+        for _ in range(args.steps):
+            st = sol.step(tt, pl.dt)
+            its.append(st["iterations"])
+            used += st["guess_used"]
+            tt += pl.dt
+        e1.record(ext)
+        e1.synchronize()
+        res[name] = {"ms": e0.elapsed_time(e1) / args.steps, "iters": float(np.mean(its)), "used": used}
+    zl, _ = sl.state()
+    zp, _ = sf.state()
+    err = float(np.abs(zl - zp).max() / max(np.abs(zp).max(), 1e-300))
+    status = sl.learned_status()
+    sl.close()
+    sf.close()
+    return {"value": world * 1e3 / res["learned"]["ms"], "ms_per_step": res["learned"]["ms"],
+            "workload": f"diffusion3d_source_{args.grid} (f = 1 + 0.5 sin(2 pi t/T) psi, T = 1000 dt)",
+            "fp64_same_steps": {"value": world * 1e3 / res["fp64"]["ms"], "ms_per_step": res["fp64"]["ms"],
+                                "iterations_per_step": res["fp64"]["iters"]},
+            "speedup_vs_fp64": res["fp64"]["ms"] / res["learned"]["ms"],
+            "iterations_per_step": res["learned"]["iters"],
+            "guess_accepted_steps": res["learned"]["used"], "timed_steps": args.steps,
+            "train_steps": args.learned_train, "train_seconds": train_s,
+            "train_phase_iterations_per_step": float(np.mean(train_iters)) if train_iters else None,
+            "final_training_loss": status["last_loss"],
+            "rel_err_face_traces_vs_fp64": err}
 
 
 def cpu_baseline(p, steps):
@@ -309,6 +381,9 @@ def main():
                           "rel_err_face_traces_vs_fp64": err_f, "rel_err_cell_values_vs_fp64": err_k,
                           "spmv_fp32_gbs": sp32["bytes"] / (sp32["ms"] * 1e-3) / 1e9}
         sm.close()
+
+    if not args.no_learned:
+        forms["learned"] = learned_leg(args, dev, world)
 
     e2e = None
     if not args.no_e2e:

@@ -508,7 +508,8 @@ __global__ void k_mpnn_reduce_dw(const float* partials, int nparts, int KF, floa
     else gb[idx - KF * H] = (float)s;
 }
 
-__global__ void k_mpnn_reduce_dec(const double* partials, int nparts, float* gwd, float* gbd, double* loss)
+__global__ void k_mpnn_reduce_dec(const double* partials, int nparts, float* gwd, float* gbd, double* loss,
+                                  double inv_nt)
 {
     const int idx = threadIdx.x;
     if (idx >= H + 2) return;
@@ -516,7 +517,7 @@ __global__ void k_mpnn_reduce_dec(const double* partials, int nparts, float* gwd
     for (int p = 0; p < nparts; ++p) s += partials[(int64_t)p * (H + 2) + idx];
     if (idx < H) gwd[idx] = (float)s;
     else if (idx == H) gbd[0] = (float)s;
-    else *loss = s;
+    else *loss = s * inv_nt;  // mean over the training faces
 }
 
 // Adam on the FP32 master parameters, then the BF16 copies in both layouts.
@@ -599,7 +600,7 @@ void mpnn_backward(const MpnnView& V, const double* target, double inv_nt, MpnnG
 {
     const int gdec = mpnn_grid(V.F);
     k_mpnn_decode<true><<<gdec, 256, 0, s>>>(V, nullptr, 0.0, nullptr, target, nullptr, inv_nt);
-    k_mpnn_reduce_dec<<<1, 128, 0, s>>>(V.dec_partials, gdec, G.g + G.off_wd, G.g + G.off_bd, G.loss);
+    k_mpnn_reduce_dec<<<1, 128, 0, s>>>(V.dec_partials, gdec, G.g + G.off_wd, G.g + G.off_bd, G.loss, inv_nt);
     const int g = mpnn_grid(V.F);
     const int smdx = smem_req((TB + 2 * H) * H * 2);
     const int smdw = smem_req((TB + H) * TB * 2);
