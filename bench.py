@@ -58,6 +58,8 @@ def parse_args():
                     help="online training steps of the learned form before its timed steps")
     ap.add_argument("--profile-run", action="store_true",
                     help="only the warm-up and timed steps (for an ncu launch list)")
+    ap.add_argument("--profile-form", choices=["fp64", "mixed", "learned"], default="fp64",
+                    help="form used by --profile-run (learned: --learned-train training steps first)")
     return ap.parse_args()
 
 
@@ -66,6 +68,22 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def max_over_ranks(value: float, world: int) -> float:
+    """Max of a per-rank timing over all ranks (the slowest replica sets the pace)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_value(steps: int, world: int, el_ms_max: float) -> float:
+    """Whole-job steps/s: every replica ran `steps` steps; the slowest took el_ms_max."""
+    return world * steps / (el_ms_max / 1e3)
 
 
 def measured_peaks():
@@ -237,6 +255,41 @@ def learned_leg(args, dev, world):
             "rel_err_face_traces_vs_fp64": err}
 
 
+def profile_other_form(args, dev):
+    """Warm-up + timed steps of the mixed or learned form only (for ncu launch lists)."""
+    import torch
+
+    from mhfem import _lib as L
+    from mhfem import problems
+
+    if args.profile_form == "mixed":
+        p = problems.diffusion3d(N=args.grid, form=L.FORM_MIXED)
+    else:
+        p = problems.diffusion3d_source(N=args.grid, steps=1000, form=L.FORM_LEARNED)
+    p.config.device = dev
+    s = problems.make_solver(p, check_every=8)
+    t = 0.0
+    if args.profile_form == "learned":
+        s.learned_options(train_steps=args.learned_train, train_iters=2)
+        for _ in range(args.learned_train):
+            s.step(t, p.dt)
+            t += p.dt
+    for _ in range(args.warmup):
+        s.step(t, p.dt)
+        t += p.dt
+    it0, _, _ = s.totals()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.step(t, p.dt)
+        t += p.dt
+    torch.cuda.synchronize()
+    it1, _, _ = s.totals()
+    print(json.dumps({"profile_run": True, "form": args.profile_form,
+                      "ms_per_step": 1e3 * (time.perf_counter() - t0) / args.steps,
+                      "iterations_per_step": (it1 - it0) / args.steps}))
+    s.close()
+
+
 def cpu_baseline(p, steps):
     from oracle.oracle import OracleModel, load
 
@@ -273,6 +326,9 @@ def main():
 
     torch.cuda.set_device(local)
     dev = local
+    if args.profile_run and args.profile_form != "fp64":
+        profile_other_form(args, dev)
+        return
     p = problems.diffusion3d(N=args.grid)
     p.config.device = dev
     s = problems.make_solver(p, check_every=8)
@@ -306,11 +362,9 @@ def main():
     clk = clocks.stop()
     el_ms = ev0.elapsed_time(ev1)
     it1, _, kl1 = s.totals()
+    el_ms = max_over_ranks(el_ms, world)
     if world > 1:
         import torch.distributed as dist
-        tt = torch.tensor([el_ms], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        el_ms = float(tt.item())
         dist.barrier()
     zf64, zk64 = s.state()
     iters = (it1 - it0) / args.steps
@@ -320,7 +374,7 @@ def main():
         s.close()
         return
     ms_step = el_ms / args.steps
-    value = world * args.steps / (el_ms / 1e3)
+    value = replicas_value(args.steps, world, el_ms)
     bytes_step = step_bytes(n, nf, S, C, F, V, W, iters)
 
     # dominant kernel: the FP64 SpMV fused with its dot product
@@ -409,11 +463,7 @@ def main():
         torch.cuda.synchronize()
         e_el = time.perf_counter() - t0
         se.close()
-        if world > 1:
-            import torch.distributed as dist
-            tt = torch.tensor([e_el], dtype=torch.float64)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            e_el = float(tt.item())
+        e_el = max_over_ranks(e_el, world)
         e2e = {"value": world * args.steps / e_el, "unit": UNIT, "h2d_bytes_per_step": 8 * C,
                "d2h_bytes_per_step": 8 * C, "path": "mhfem_set_coeff + mhfem_step + mhfem_get_state (ctypes)",
                "steps": "the same warm-up and timed steps as `value`, on a fresh solver"}

@@ -1,0 +1,103 @@
+"""config.ini driver, boundary-condition storage and the init step."""
+import numpy as np
+import pytest
+
+from helpers import rel_err
+from mhfem import bcstorage, config, init, meshgen, vtkio
+
+CONFIG = """output-directory = out
+mesh = mesh.vtu
+boundary-conditions-file = boundary.bcs
+initial-condition = initial.vtu
+initial-time = 0
+final-time = 0.003
+snapshot-period = 0.001
+time-step = 0.0005
+linear-solver = gmres
+gmres-variant = CGS
+gmres-restarting-max = 30
+preconditioner = diagonal
+convergence-residue = 1e-12
+diffusivity = 1e-3
+"""
+
+
+def _write_case(tmp_path, N=6):
+    coords, cells = meshgen.square_triangles(N)
+    vtkio.write_vtu(tmp_path / "mesh.vtu", coords, cells, {})
+    assert init.main(["--mesh", str(tmp_path / "mesh.vtu"), "--output", str(tmp_path / "initial.vtu"),
+                      "--output-boundary", str(tmp_path / "boundary.bcs")]) == 0
+    (tmp_path / "config.ini").write_text(CONFIG)
+    return coords, cells
+
+
+def test_config_schema(tmp_path):
+    _write_case(tmp_path)
+    cfg = config.parse(tmp_path / "config.ini")
+    assert cfg["diffusivity"] == 1e-3 and cfg["convergence-residue"] == 1e-12
+    assert cfg["initial-time"] == 0.0 and cfg["mesh-format"] == "auto"
+    assert any("BiCGStab" in n for n in cfg.notices)  # gmres requested
+    (tmp_path / "bad.ini").write_text(CONFIG + "no-such-key = 1\n")
+    with pytest.raises(config.ConfigError, match="unknown"):
+        config.parse(tmp_path / "bad.ini")
+    (tmp_path / "missing.ini").write_text(CONFIG.replace("final-time = 0.003\n", ""))
+    with pytest.raises(config.ConfigError, match="final-time"):
+        config.parse(tmp_path / "missing.ini")
+    (tmp_path / "time.ini").write_text(CONFIG.replace("final-time = 0.003", "final-time = -1"))
+    with pytest.raises(config.ConfigError, match="Final time"):
+        config.parse(tmp_path / "time.ini")
+
+
+def test_bc_storage_roundtrip(tmp_path):
+    b = bcstorage.BoundaryConditionsStorage(7)
+    b.tags[:] = [0, 1, 2, 3, 0, 1, 2]
+    b.values[:] = np.arange(7) * 0.5
+    b.dirichletValues[:] = -np.arange(7)
+    b.save(tmp_path / "b.bcs")
+    c = bcstorage.BoundaryConditionsStorage.load(tmp_path / "b.bcs")
+    assert c.dofSize == 7
+    assert np.array_equal(c.tags, b.tags) and np.array_equal(c.values, b.values)
+    assert np.array_equal(c.dirichletValues, b.dirichletValues)
+    raw = bytearray((tmp_path / "b.bcs").read_bytes())
+    raw[len(bcstorage.MAGIC) + 4 + len(bcstorage.SERIALIZATION_TYPE) + 8 + 8] = 9  # corrupt tag
+    (tmp_path / "bad.bcs").write_bytes(bytes(raw))
+    with pytest.raises(ValueError, match="tag"):
+        bcstorage.BoundaryConditionsStorage.load(tmp_path / "bad.bcs")
+
+
+def test_init_matches_reference_formula(tmp_path):
+    coords, cells = _write_case(tmp_path)
+    z = vtkio.read_cell_data(tmp_path / "initial.vtu", "InitialCondition[Z0]")
+    c = meshgen.cell_centroids(coords, cells)
+    x, y = c[:, 0] - 0.5, c[:, 1] - 0.5
+    assert np.allclose(z, np.maximum(0, (x * x / -0.05 + y * y / -0.05 + 5) * 0.2))
+    b = bcstorage.BoundaryConditionsStorage.load(tmp_path / "boundary.bcs")
+    assert b.dofSize == 3 * 36 + 2 * 6 and np.all(b.tags == 0)
+
+
+@pytest.mark.gpu
+def test_driver_end_to_end(tmp_path):
+    from mhfem import problems, run
+    from oracle.oracle import OracleModel
+
+    coords, cells = _write_case(tmp_path)
+    rc = run.main(["--config", str(tmp_path / "config.ini"), "--log-file", str(tmp_path / "log.txt"),
+                   "--verbose", "0"])
+    assert rc == 0
+    out = tmp_path / "out"
+    files = sorted(out.glob("data_*.vtu"))
+    assert [f.name for f in files] == [f"data_{k:05d}.vtu" for k in range(4)]
+    log = (tmp_path / "log.txt").read_text()
+    assert "Total number of time steps:" in log and "Total number of linear solver iterations:" in log
+    z_gpu = vtkio.read_cell_data(files[-1], "Z")
+    # the same model through the oracle: heat equation, D = 1e-3, dt = 5e-4, 6 steps
+    z0 = vtkio.read_cell_data(tmp_path / "initial.vtu", "InitialCondition[Z0]")
+    p = problems.heat2d(N=6)
+    p.coords, p.cells, p.Z0 = coords, cells, z0
+    p.coeffs["D"] = 1e-3
+    m = OracleModel.from_problem(p)
+    t = 0.0
+    for _ in range(6):
+        m.step(t, 5e-4, 1e-14)
+        t += 5e-4
+    assert rel_err(z_gpu, m.Z_iK) < 1e-9

@@ -105,13 +105,15 @@ __device__ __forceinline__ void block_reduce_store(T (&acc)[NV], double* partial
 }
 
 // Returns true in the last block to finish; that block then sees every
-// partial.  The ticket counter is reset for the next launch.
+// partial.  Thread 0 wrote this block's partial, so only thread 0 fences
+// before taking its ticket (the other threads' stores need no ordering: the
+// last block reads partials only).  The counter is reset for the next launch.
 __device__ __forceinline__ bool ticket_last(uint32_t* counter)
 {
     __shared__ bool last;
-    __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
+        __threadfence();
         const uint32_t prev = atomicAdd(counter, 1u);
         last = (prev == gridDim.x - 1);
         if (last) *counter = 0;

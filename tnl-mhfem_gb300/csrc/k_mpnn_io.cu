@@ -11,7 +11,8 @@
 //   5-7 |n_x|, |n_y|, |n_z|   unit normal, sign-free (static)
 //   8  face measure / mean face measure (static)
 //   9  boundary flag, 10 Dirichlet flag, 11 constant 1 (static)
-//   12-15 zero
+//   12 r / rms(r), r = b - A (2 Zn - Zn1) the residual of the extrapolated guess
+//   13-15 zero
 // The network predicts (Z_new - (2 Zn - Zn1)) / sd.
 #include <cuda_bf16.h>
 
@@ -79,6 +80,8 @@ __global__ void __launch_bounds__(256) k_features(int64_t F, MpnnInputs in, doub
     v[1] = (float)((z - in.Zn1[E]) * rsd);
     v[2] = (float)(in.rhs[E] * rsz);
     v[4] = (float)((in.f_base[E] + in.src_scale * in.f_psi[E]) * in.f_norm);
+    const double rn = in.rnorm->snorm;
+    v[12] = rn > 0 ? (float)(in.rbase[E] * (sqrt((double)F) / rn)) : 0.f;
     uint32_t w[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) {

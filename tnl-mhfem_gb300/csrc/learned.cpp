@@ -405,8 +405,12 @@ mhfem_status learned_solve(mhfem_t h, int* iters, double* res, mhfem_step_stats*
     const bool have_features = have_hist && sd > 0 && sz > 0;
     if (have_features) {
         mpnn_base(F, L->Zn, L->Zn1, L->base, s);
+        // residual of the extrapolated guess (into the Krylov r vector; its norm in W.sc->snorm)
+        mixed_outer_residual(h->A, h->rhs, L->base, h->W, h->opts.tol, 1, s);
+        in.rbase = h->W.r;
+        in.rnorm = h->W.sc;
         mpnn_features(F, in, sz, sd, L->x0, s);
-        h->launches += 2;
+        h->launches += 3;
     }
     if (infer && have_features) {
         MpnnView V = make_view(h);

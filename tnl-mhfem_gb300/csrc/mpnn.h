@@ -6,6 +6,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include "mhfem_internal.h"
+
 namespace mhfem {
 
 constexpr int kMpnnHidden = 64;
@@ -63,6 +65,8 @@ struct MpnnInputs {
     const float* f_psi;      // [F] face average of the source shape psi
     double src_scale;        // amplitude * sin(2 pi t / T)
     double f_norm;           // scale of the source channel
+    const double* rbase;     // residual b - A (2 Zn - Zn1) of the extrapolated guess
+    const KrylovScalars* rnorm;  // its 2-norm in ->snorm (written by the residual kernel)
 };
 // sz = rms(Zn), sd = rms(Zn - Zn1) over free rows -> scal[0], scal[1]
 void mpnn_scales(int64_t F, const MpnnInputs& in, const uint8_t* fixed, double* partials, double* scal, cudaStream_t s);
