@@ -261,6 +261,29 @@ mhfem_status mhfem_learned_gradients(mhfem_t h, const float* features, const dou
                                      double* loss);
 mhfem_status mhfem_learned_status(mhfem_t h, int32_t* trained_steps, double* last_loss, int32_t* num_params);
 
+/* ---- allocation-free solve -------------------------------------------------
+ * No counterpart in the reference.  For callers whose device memory belongs
+ * to their own pool allocator (a framework that hands out every buffer from
+ * a pre-reserved arena and cannot have a library call cudaMalloc/cudaFree,
+ * which bypass its accounting and synchronize the device): FP64 BiCGStab on
+ * a caller-owned unit-diagonal system in the layout this library assembles
+ * (ELL of the off-diagonal part, [width][rows], padding column = own row).
+ * cols, vals, rhs and x are DEVICE pointers; x holds the initial guess and
+ * receives the solution; stream is a cudaStream_t (NULL: default stream).
+ * All work vectors live in one static device array of fixed size (about
+ * 12.7 MB, held by every GPU that loads the library until the process
+ * exits), so systems with more than MHFEM_NOALLOC_MAX_ROWS rows are rejected
+ * with MHFEM_ERR_INVALID_ARGUMENT.  The first call on a device looks the
+ * array's address up (cudaGetSymbolAddress) and should come before any
+ * stream capture.  Every call shares the array: calls that overlap on the
+ * GPU (other streams, other threads) race and must be serialized by the
+ * caller.  Returns MHFEM_OK, MHFEM_ERR_NOT_CONVERGED, MHFEM_ERR_BREAKDOWN or
+ * MHFEM_ERR_NOT_FINITE like mhfem_solve. */
+#define MHFEM_NOALLOC_MAX_ROWS 262144
+mhfem_status mhfem_bicgstab_noalloc(const int32_t* cols, const double* vals, int32_t width, int64_t rows,
+                                    const double* rhs, double* x, double tol, int32_t max_iter,
+                                    int32_t* iterations, double* residual, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

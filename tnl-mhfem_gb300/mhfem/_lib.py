@@ -109,7 +109,10 @@ SIGNATURES = [
     ("mhfem_learned_forward", ct.c_int32, [_P, ct.POINTER(ct.c_float), ct.POINTER(ct.c_float)]),
     ("mhfem_learned_gradients", ct.c_int32, [_P, ct.POINTER(ct.c_float), _pd, ct.POINTER(ct.c_float), _pd]),
     ("mhfem_learned_status", ct.c_int32, [_P, _pi32, _pd, _pi32]),
+    ("mhfem_bicgstab_noalloc", ct.c_int32, [_P, _P, ct.c_int32, ct.c_int64, _P, _P, ct.c_double, ct.c_int32,
+                                            _pi32, _pd, _P]),
 ]
+NOALLOC_MAX_ROWS = 262144
 
 _lib = None
 
