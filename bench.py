@@ -225,17 +225,22 @@ def learned_leg(args, dev, world):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         tt = t
-        its, used = [], 0
+        its, used, rg, rw = [], 0, [], []
         torch.cuda.synchronize()
         e0.record(ext)
         for _ in range(args.steps):
             st = sol.step(tt, pl.dt)
             its.append(st["iterations"])
             used += st["guess_used"]
+            if st["guess_residual"] > 0:
+                rg.append(st["guess_residual"])
+                rw.append(st["warm_residual"])
             tt += pl.dt
         e1.record(ext)
         e1.synchronize()
-        res[name] = {"ms": e0.elapsed_time(e1) / args.steps, "iters": float(np.mean(its)), "used": used}
+        res[name] = {"ms": e0.elapsed_time(e1) / args.steps, "iters": float(np.mean(its)), "used": used,
+                     "guess_res": float(np.exp(np.mean(np.log(rg)))) if rg else None,
+                     "warm_res": float(np.exp(np.mean(np.log(rw)))) if rw else None}
     zl, _ = sl.state()
     zp, _ = sf.state()
     err = float(np.abs(zl - zp).max() / max(np.abs(zp).max(), 1e-300))
@@ -249,6 +254,8 @@ def learned_leg(args, dev, world):
             "speedup_vs_fp64": res["fp64"]["ms"] / res["learned"]["ms"],
             "iterations_per_step": res["learned"]["iters"],
             "guess_accepted_steps": res["learned"]["used"], "timed_steps": args.steps,
+            "guess_rel_residual_geomean": res["learned"]["guess_res"],
+            "warm_start_rel_residual_geomean": res["learned"]["warm_res"],
             "train_steps": args.learned_train, "train_seconds": train_s,
             "train_phase_iterations_per_step": float(np.mean(train_iters)) if train_iters else None,
             "final_training_loss": status["last_loss"],

@@ -35,7 +35,8 @@ namespace mhfem {
 namespace {
 
 constexpr int H = kMpnnHidden;  // 64
-constexpr int TB = 128;         // faces per tile = threads per CTA
+constexpr int TB = 128;         // faces per tile
+constexpr int NT = 512;         // threads per CTA of the tensor-core kernels (4 per face)
 
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b)
 {
@@ -93,8 +94,12 @@ __device__ __forceinline__ void tile_done()
 
 // ---- forward layer ----------------------------------------------------------
 
+// 512 threads per 128-row tile: thread (r, qs) = (tid % 128, tid / 128) stages
+// and finishes the 16-column slice qs of row r.  Its warp is 4 qs + r / 32, so
+// warp % 4 == r / 32 is the TMEM lane quarter the warp may read, and the
+// thread keeps its own slice of h_l in registers for the residual.
 template <int KIN, bool TRAIN>
-__global__ void __launch_bounds__(TB) k_mpnn_layer(const MpnnView V, int layer)
+__global__ void __launch_bounds__(NT) k_mpnn_layer(const MpnnView V, int layer)
 {
     extern __shared__ __align__(128) uint8_t smem[];
     uint8_t* sA = smem;                      // 128 x KIN
@@ -103,12 +108,13 @@ __global__ void __launch_bounds__(TB) k_mpnn_layer(const MpnnView V, int layer)
     __shared__ uint32_t tbase;
     __shared__ float sbias[H];
     const int tid = threadIdx.x, warp = tid >> 5;
+    const int r = tid & (TB - 1), qs = tid >> 7;
     const int64_t F = V.F;
 
     const __nv_bfloat16* Wf = V.w_fwd[layer];  // [64][KIN]
-    for (int idx = tid; idx < H * KIN / 8; idx += TB) {
-        const int r = idx / (KIN / 8), k0 = (idx % (KIN / 8)) * 8;
-        st_tile(sB, r, k0, KIN, *reinterpret_cast<const uint4*>(Wf + r * KIN + k0));
+    for (int idx = tid; idx < H * KIN / 8; idx += NT) {
+        const int rr = idx / (KIN / 8), k0 = (idx % (KIN / 8)) * 8;
+        st_tile(sB, rr, k0, KIN, *reinterpret_cast<const uint4*>(Wf + rr * KIN + k0));
     }
     if (tid < H) sbias[tid] = V.bias[layer][tid];
     if (warp == 0) {
@@ -117,104 +123,100 @@ __global__ void __launch_bounds__(TB) k_mpnn_layer(const MpnnView V, int layer)
     }
     if (tid == 0) tc::mbar_init(&mbar, 1);
     tile_done();
-    const uint32_t taddr = tbase;
+    const uint32_t taddr = tbase + ((uint32_t)(32 * (warp & 3)) << 16) + 16 * qs;
     TileSync ts{&mbar, 0};
     const __nv_bfloat16* hin = (KIN == 16) ? V.x0 : V.h[layer];
     __nv_bfloat16* hout = V.h[layer + 1];
     const int64_t ntiles = (F + TB - 1) / TB;
 
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int64_t row = tile * TB + tid;
+        const int64_t row = tile * TB + r;
         const bool valid = row < F;
-        uint32_t self[KIN == 16 ? 1 : 32];
+        uint4 self0 = make_uint4(0, 0, 0, 0), self1 = self0;
         if constexpr (KIN == 16) {
-            uint4 a = make_uint4(0, 0, 0, 0), b = a;
-            if (valid) {
-                a = *reinterpret_cast<const uint4*>(hin + row * 16);
-                b = *reinterpret_cast<const uint4*>(hin + row * 16 + 8);
+            if (qs < 2) {
+                uint4 v = make_uint4(0, 0, 0, 0);
+                if (valid) v = *reinterpret_cast<const uint4*>(hin + row * 16 + 8 * qs);
+                st_tile(sA, r, 8 * qs, 16, v);
             }
-            st_tile(sA, tid, 0, 16, a);
-            st_tile(sA, tid, 8, 16, b);
         }
         else {
-#pragma unroll
-            for (int c = 0; c < 8; ++c) {
-                uint4 v = make_uint4(0, 0, 0, 0);
-                if (valid) v = *reinterpret_cast<const uint4*>(hin + row * H + 8 * c);
-                self[4 * c + 0] = v.x; self[4 * c + 1] = v.y; self[4 * c + 2] = v.z; self[4 * c + 3] = v.w;
-                st_tile(sA, tid, 8 * c, KIN, v);
+            if (valid) {
+                self0 = *reinterpret_cast<const uint4*>(hin + row * H + 16 * qs);
+                self1 = *reinterpret_cast<const uint4*>(hin + row * H + 16 * qs + 8);
             }
-            // neighbour mean, 32 columns at a time to bound register use
+            st_tile(sA, r, 16 * qs, KIN, self0);
+            st_tile(sA, r, 16 * qs + 8, KIN, self1);
+            // neighbour mean of this thread's 16 columns
+            float acc[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) acc[q] = 0.f;
             const int d = valid ? (int)V.deg[row] : 0;
-            const float inv = d > 0 ? 1.0f / (float)d : 0.0f;
+            if (valid) {
+                for (int k = 0; k < V.W; ++k) {
+                    const int32_t c = V.nbr[(int64_t)k * F + row];
+                    if (c == (int32_t)row) continue;
+                    const uint4* src = reinterpret_cast<const uint4*>(hin + (int64_t)c * H + 16 * qs);
 #pragma unroll
-            for (int half = 0; half < 2; ++half) {
-                float acc[32];
+                    for (int u = 0; u < 2; ++u) {
+                        const uint4 v = src[u];
+                        const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-                for (int q = 0; q < 32; ++q) acc[q] = 0.f;
-                if (valid) {
-                    for (int k = 0; k < V.W; ++k) {
-                        const int32_t c = V.nbr[(int64_t)k * F + row];
-                        if (c == (int32_t)row) continue;
-                        const uint4* src = reinterpret_cast<const uint4*>(hin + (int64_t)c * H + 32 * half);
-#pragma unroll
-                        for (int u = 0; u < 4; ++u) {
-                            const uint4 v = src[u];
-                            const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-                            for (int t = 0; t < 4; ++t) {
-                                const float2 f = unpack_bf16(w4[t]);
-                                acc[8 * u + 2 * t] += f.x;
-                                acc[8 * u + 2 * t + 1] += f.y;
-                            }
+                        for (int t = 0; t < 4; ++t) {
+                            const float2 f = unpack_bf16(w4[t]);
+                            acc[8 * u + 2 * t] += f.x;
+                            acc[8 * u + 2 * t + 1] += f.y;
                         }
                     }
                 }
+            }
+            const float inv = d > 0 ? 1.0f / (float)d : 0.0f;
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    uint4 v;
-                    v.x = pack_bf16(acc[8 * u + 0] * inv, acc[8 * u + 1] * inv);
-                    v.y = pack_bf16(acc[8 * u + 2] * inv, acc[8 * u + 3] * inv);
-                    v.z = pack_bf16(acc[8 * u + 4] * inv, acc[8 * u + 5] * inv);
-                    v.w = pack_bf16(acc[8 * u + 6] * inv, acc[8 * u + 7] * inv);
-                    st_tile(sA, tid, H + 32 * half + 8 * u, KIN, v);
-                    if (TRAIN && valid)
-                        *reinterpret_cast<uint4*>(V.a[layer] + row * H + 32 * half + 8 * u) = v;
-                }
+            for (int u = 0; u < 2; ++u) {
+                uint4 v;
+                v.x = pack_bf16(acc[8 * u + 0] * inv, acc[8 * u + 1] * inv);
+                v.y = pack_bf16(acc[8 * u + 2] * inv, acc[8 * u + 3] * inv);
+                v.z = pack_bf16(acc[8 * u + 4] * inv, acc[8 * u + 5] * inv);
+                v.w = pack_bf16(acc[8 * u + 6] * inv, acc[8 * u + 7] * inv);
+                st_tile(sA, r, H + 16 * qs + 8 * u, KIN, v);
+                if (TRAIN && valid) *reinterpret_cast<uint4*>(V.a[layer] + row * H + 16 * qs + 8 * u) = v;
             }
         }
-        if (!tile_mma<TB, H, KIN>(sA, sB, taddr, ts, false)) {
+        if (!tile_mma<TB, H, KIN>(sA, sB, tbase, ts, false)) {
             if (tid == 0) atomicOr(V.err, 4);
             break;
         }
-        float acc[H];
-        tc::tmem_ld_x64(taddr + ((uint32_t)(32 * warp) << 16), acc);
+        float acc[16];
+        tc::tmem_ld_x16(taddr, acc);
         if (valid) {
+            const uint32_t sw[8] = {self0.x, self0.y, self0.z, self0.w, self1.x, self1.y, self1.z, self1.w};
+            uint32_t zo[8], ho[8];
 #pragma unroll
-            for (int c = 0; c < 8; ++c) {
-                uint32_t zo[4], ho[4];
-#pragma unroll
-                for (int t = 0; t < 4; ++t) {
-                    const int q = 8 * c + 2 * t;
-                    const float z0 = acc[q] + sbias[q], z1 = acc[q + 1] + sbias[q + 1];
-                    float o0 = fmaxf(z0, 0.f), o1 = fmaxf(z1, 0.f);
-                    if constexpr (KIN != 16) {
-                        const float2 s = unpack_bf16(self[4 * c + t]);
-                        o0 += s.x;
-                        o1 += s.y;
-                    }
-                    zo[t] = pack_bf16(z0, z1);
-                    ho[t] = pack_bf16(o0, o1);
+            for (int t = 0; t < 8; ++t) {
+                const int q = 2 * t;
+                const float z0 = acc[q] + sbias[16 * qs + q], z1 = acc[q + 1] + sbias[16 * qs + q + 1];
+                float o0 = fmaxf(z0, 0.f), o1 = fmaxf(z1, 0.f);
+                if constexpr (KIN != 16) {
+                    const float2 sv = unpack_bf16(sw[t]);
+                    o0 += sv.x;
+                    o1 += sv.y;
                 }
-                *reinterpret_cast<uint4*>(hout + row * H + 8 * c) = make_uint4(ho[0], ho[1], ho[2], ho[3]);
-                if (TRAIN)
-                    *reinterpret_cast<uint4*>(V.z[layer] + row * H + 8 * c) = make_uint4(zo[0], zo[1], zo[2], zo[3]);
+                zo[t] = pack_bf16(z0, z1);
+                ho[t] = pack_bf16(o0, o1);
+            }
+            uint4* ho4 = reinterpret_cast<uint4*>(hout + row * H + 16 * qs);
+            ho4[0] = make_uint4(ho[0], ho[1], ho[2], ho[3]);
+            ho4[1] = make_uint4(ho[4], ho[5], ho[6], ho[7]);
+            if (TRAIN) {
+                uint4* zo4 = reinterpret_cast<uint4*>(V.z[layer] + row * H + 16 * qs);
+                zo4[0] = make_uint4(zo[0], zo[1], zo[2], zo[3]);
+                zo4[1] = make_uint4(zo[4], zo[5], zo[6], zo[7]);
             }
         }
         tile_done();
     }
     tile_done();
-    if (warp == 0) tc::tmem_dealloc(taddr, H);
+    if (warp == 0) tc::tmem_dealloc(tbase, H);
 }
 
 // ---- decoder, loss and the start of the backward pass --------------------------
@@ -297,8 +299,9 @@ __global__ void __launch_bounds__(256) k_mpnn_decode(const MpnnView V, const dou
 // ---- backward: dX = dZ W^T ------------------------------------------------------
 
 // A = dZ (128 x 64) with dZ = dH * (Z > 0), B = W_in (128 x 64: row k = input k).
+// Thread (r, qs) stages and finishes columns 16 qs .. 16 qs + 15 of row r.
 // Epilogue: dH += dX[:, :64] (residual + self path), ga = dX[:, 64:] / deg.
-__global__ void __launch_bounds__(TB) k_mpnn_bwd_dx(const MpnnView V, int layer)
+__global__ void __launch_bounds__(NT) k_mpnn_bwd_dx(const MpnnView V, int layer)
 {
     extern __shared__ __align__(128) uint8_t smem[];
     uint8_t* sA = smem;               // 128 x 64
@@ -306,11 +309,12 @@ __global__ void __launch_bounds__(TB) k_mpnn_bwd_dx(const MpnnView V, int layer)
     __shared__ uint64_t mbar;
     __shared__ uint32_t tbase;
     const int tid = threadIdx.x, warp = tid >> 5;
+    const int r = tid & (TB - 1), qs = tid >> 7;
     const int64_t F = V.F;
     const __nv_bfloat16* Wb = V.w_bwd[layer];  // [128][64]
-    for (int idx = tid; idx < 2 * H * H / 8; idx += TB) {
-        const int r = idx / (H / 8), k0 = (idx % (H / 8)) * 8;
-        st_tile(sB, r, k0, H, *reinterpret_cast<const uint4*>(Wb + r * H + k0));
+    for (int idx = tid; idx < 2 * H * H / 8; idx += NT) {
+        const int rr = idx / (H / 8), k0 = (idx % (H / 8)) * 8;
+        st_tile(sB, rr, k0, H, *reinterpret_cast<const uint4*>(Wb + rr * H + k0));
     }
     if (warp == 0) {
         tc::tmem_alloc(&tbase, 2 * H);
@@ -318,58 +322,59 @@ __global__ void __launch_bounds__(TB) k_mpnn_bwd_dx(const MpnnView V, int layer)
     }
     if (tid == 0) tc::mbar_init(&mbar, 1);
     tile_done();
-    const uint32_t taddr = tbase;
+    const uint32_t tlane = tbase + ((uint32_t)(32 * (warp & 3)) << 16);
     TileSync ts{&mbar, 0};
     const int64_t ntiles = (F + TB - 1) / TB;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int64_t row = tile * TB + tid;
+        const int64_t row = tile * TB + r;
         const bool valid = row < F;
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
+        for (int c = 0; c < 2; ++c) {
+            const int col = 16 * qs + 8 * c;
             uint4 out = make_uint4(0, 0, 0, 0);
             if (valid) {
-                const float4 d0 = *reinterpret_cast<const float4*>(V.dh + row * H + 8 * c);
-                const float4 d1 = *reinterpret_cast<const float4*>(V.dh + row * H + 8 * c + 4);
-                const uint4 zz = *reinterpret_cast<const uint4*>(V.z[layer] + row * H + 8 * c);
+                const float4 d0 = *reinterpret_cast<const float4*>(V.dh + row * H + col);
+                const float4 d1 = *reinterpret_cast<const float4*>(V.dh + row * H + col + 4);
+                const uint4 zz = *reinterpret_cast<const uint4*>(V.z[layer] + row * H + col);
                 const float2 z0 = unpack_bf16(zz.x), z1 = unpack_bf16(zz.y), z2 = unpack_bf16(zz.z),
                              z3 = unpack_bf16(zz.w);
                 out.x = pack_bf16(z0.x > 0 ? d0.x : 0.f, z0.y > 0 ? d0.y : 0.f);
                 out.y = pack_bf16(z1.x > 0 ? d0.z : 0.f, z1.y > 0 ? d0.w : 0.f);
                 out.z = pack_bf16(z2.x > 0 ? d1.x : 0.f, z2.y > 0 ? d1.y : 0.f);
                 out.w = pack_bf16(z3.x > 0 ? d1.z : 0.f, z3.y > 0 ? d1.w : 0.f);
-                *reinterpret_cast<uint4*>(V.dz + row * H + 8 * c) = out;
+                *reinterpret_cast<uint4*>(V.dz + row * H + col) = out;
             }
-            st_tile(sA, tid, 8 * c, H, out);
+            st_tile(sA, r, col, H, out);
         }
-        if (!tile_mma<TB, 2 * H, H>(sA, sB, taddr, ts, false)) {
+        if (!tile_mma<TB, 2 * H, H>(sA, sB, tbase, ts, false)) {
             if (tid == 0) atomicOr(V.err, 4);
             break;
         }
-        float acc[H];
-        tc::tmem_ld_x64(taddr + ((uint32_t)(32 * warp) << 16), acc);
+        float acc[16];
+        tc::tmem_ld_x16(tlane + 16 * qs, acc);
         if (valid) {
-            float* dh = V.dh + row * H;
+            float* dh = V.dh + row * H + 16 * qs;
 #pragma unroll
-            for (int c = 0; c < H / 4; ++c) {
+            for (int c = 0; c < 4; ++c) {
                 float4 v = *reinterpret_cast<float4*>(dh + 4 * c);
                 v.x += acc[4 * c]; v.y += acc[4 * c + 1]; v.z += acc[4 * c + 2]; v.w += acc[4 * c + 3];
                 *reinterpret_cast<float4*>(dh + 4 * c) = v;
             }
         }
-        tc::tmem_ld_x64(taddr + ((uint32_t)(32 * warp) << 16) + H, acc);
+        tc::tmem_ld_x16(tlane + H + 16 * qs, acc);
         if (valid) {
             const int d = V.deg[row];
             const float inv = d > 0 ? 1.0f / (float)d : 0.f;
-            float* ga = V.ga + row * H;
+            float* ga = V.ga + row * H + 16 * qs;
 #pragma unroll
-            for (int c = 0; c < H / 4; ++c)
+            for (int c = 0; c < 4; ++c)
                 *reinterpret_cast<float4*>(ga + 4 * c) =
                     make_float4(acc[4 * c] * inv, acc[4 * c + 1] * inv, acc[4 * c + 2] * inv, acc[4 * c + 3] * inv);
         }
         tile_done();
     }
     tile_done();
-    if (warp == 0) tc::tmem_dealloc(taddr, 2 * H);
+    if (warp == 0) tc::tmem_dealloc(tbase, 2 * H);
 }
 
 // dH[E] += sum_{E' in N(E)} ga[E'] (the adjacency is symmetric, so this is
@@ -403,22 +408,26 @@ __global__ void __launch_bounds__(256) k_mpnn_dz0(const MpnnView V)
 // ---- backward: dW = X^T dZ (split over faces) -----------------------------------
 
 // X = [h_l, a_l] (KF = 128) or x0 (KF = 16, zero-padded to 128 rows).  The
-// staging transposes both operands into K-major tiles over the face index.
+// staging transposes both operands into K-major tiles over the face index:
+// thread (r, qs) loads 16 features (and 16 dZ columns) of face r with vector
+// loads and scatters them into column r of the tiles.
 template <int KF>
-__global__ void __launch_bounds__(TB) k_mpnn_bwd_dw(const MpnnView V, int layer, float* partials)
+__global__ void __launch_bounds__(NT) k_mpnn_bwd_dw(const MpnnView V, int layer, float* partials)
 {
     extern __shared__ __align__(128) uint8_t smem[];
     uint8_t* sA = smem;                // 128 features x 128 faces
     uint8_t* sB = smem + TB * TB * 2;  // 64 outputs x 128 faces
     __shared__ uint64_t mbar;
     __shared__ uint32_t tbase;
+    __shared__ float red[NT / 32][16];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int r = tid & (TB - 1), qs = tid >> 7;
     const int64_t F = V.F;
     if (KF < TB) {
         // rows KF..127 of the feature tile stay zero
-        for (int idx = tid; idx < TB * TB / 8; idx += TB) {
-            const int r = idx / (TB / 8), k0 = (idx % (TB / 8)) * 8;
-            st_tile(sA, r, k0, TB, make_uint4(0, 0, 0, 0));
+        for (int idx = tid; idx < TB * TB / 8; idx += NT) {
+            const int rr = idx / (TB / 8), k0 = (idx % (TB / 8)) * 8;
+            st_tile(sA, rr, k0, TB, make_uint4(0, 0, 0, 0));
         }
     }
     if (warp == 0) {
@@ -427,60 +436,77 @@ __global__ void __launch_bounds__(TB) k_mpnn_bwd_dw(const MpnnView V, int layer,
     }
     if (tid == 0) tc::mbar_init(&mbar, 1);
     tile_done();
-    const uint32_t taddr = tbase;
     TileSync ts{&mbar, 0};
-    float dbs[H];
+    float dbs[16];
 #pragma unroll
-    for (int q = 0; q < H; ++q) dbs[q] = 0.f;
+    for (int q = 0; q < 16; ++q) dbs[q] = 0.f;
     const int64_t ntiles = (F + TB - 1) / TB;
     bool first = true;
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int64_t row = tile * TB + tid;  // this thread's face = column tid of both tiles
-        const bool valid = row < F;
-        __nv_bfloat16* sAh = reinterpret_cast<__nv_bfloat16*>(sA);
-        __nv_bfloat16* sBh = reinterpret_cast<__nv_bfloat16*>(sB);
-        const __nv_bfloat16 zero = __float2bfloat16(0.f);
-        if constexpr (KF == 16) {
+    __nv_bfloat16* sAh = reinterpret_cast<__nv_bfloat16*>(sA);
+    __nv_bfloat16* sBh = reinterpret_cast<__nv_bfloat16*>(sB);
+    auto scatter = [&](__nv_bfloat16* tile, int m0, uint4 v) {
+        const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-            for (int m = 0; m < 16; ++m)
-                sAh[tc::kmajor_offset(m, tid, TB) / 2] = valid ? V.x0[row * 16 + m] : zero;
+        for (int t = 0; t < 4; ++t) {
+            const __nv_bfloat162 p = *reinterpret_cast<const __nv_bfloat162*>(&w4[t]);
+            tile[tc::kmajor_offset(m0 + 2 * t, r, TB) / 2] = p.x;
+            tile[tc::kmajor_offset(m0 + 2 * t + 1, r, TB) / 2] = p.y;
         }
-        else {
-            for (int m = 0; m < H; ++m) {
-                sAh[tc::kmajor_offset(m, tid, TB) / 2] = valid ? V.h[layer][row * H + m] : zero;
-                sAh[tc::kmajor_offset(H + m, tid, TB) / 2] = valid ? V.a[layer][row * H + m] : zero;
+    };
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t row = tile * TB + r;
+        const bool valid = row < F;
+        const uint4 zero = make_uint4(0, 0, 0, 0);
+        if constexpr (KF == 16) {
+            if (qs == 0) {
+                scatter(sAh, 0, valid ? *reinterpret_cast<const uint4*>(V.x0 + row * 16) : zero);
+                scatter(sAh, 8, valid ? *reinterpret_cast<const uint4*>(V.x0 + row * 16 + 8) : zero);
             }
         }
-        for (int n = 0; n < H; ++n) {
-            const __nv_bfloat16 dzv = valid ? V.dz[row * H + n] : zero;
-            sBh[tc::kmajor_offset(n, tid, TB) / 2] = dzv;
-            dbs[n] += __bfloat162float(dzv);
+        else {
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                const int m = 16 * qs + 8 * c;
+                scatter(sAh, m, valid ? *reinterpret_cast<const uint4*>(V.h[layer] + row * H + m) : zero);
+                scatter(sAh, H + m, valid ? *reinterpret_cast<const uint4*>(V.a[layer] + row * H + m) : zero);
+            }
         }
-        if (!tile_mma<TB, H, TB>(sA, sB, taddr, ts, !first)) {
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            const int n = 16 * qs + 8 * c;
+            const uint4 v = valid ? *reinterpret_cast<const uint4*>(V.dz + row * H + n) : zero;
+            scatter(sBh, n, v);
+            const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const float2 f = unpack_bf16(w4[t]);
+                dbs[8 * c + 2 * t] += f.x;
+                dbs[8 * c + 2 * t + 1] += f.y;
+            }
+        }
+        if (!tile_mma<TB, H, TB>(sA, sB, tbase, ts, !first)) {
             if (tid == 0) atomicOr(V.err, 4);
             break;
         }
         first = false;
         tile_done();
     }
-    // partial dW: row m = 32 warp + lane, 64 output columns
-    float acc[H];
+    // partial dW: TMEM lane m = feature (row r of this thread), columns 16 qs ..
+    float acc[16];
     if (first) {
 #pragma unroll
-        for (int q = 0; q < H; ++q) acc[q] = 0.f;
+        for (int q = 0; q < 16; ++q) acc[q] = 0.f;
     }
     else
-        tc::tmem_ld_x64(taddr + ((uint32_t)(32 * warp) << 16), acc);
+        tc::tmem_ld_x16(tbase + ((uint32_t)(32 * (warp & 3)) << 16) + 16 * qs, acc);
     float* P = partials + (int64_t)blockIdx.x * (TB * H + H);
-    const int m = 32 * warp + lane;
 #pragma unroll
-    for (int c = 0; c < H / 4; ++c)
-        *reinterpret_cast<float4*>(P + m * H + 4 * c) = make_float4(acc[4 * c], acc[4 * c + 1], acc[4 * c + 2],
-                                                                    acc[4 * c + 3]);
-    // db partial: reduce dbs over the block
-    __shared__ float red[TB / 32][H];
+    for (int c = 0; c < 4; ++c)
+        *reinterpret_cast<float4*>(P + r * H + 16 * qs + 4 * c) =
+            make_float4(acc[4 * c], acc[4 * c + 1], acc[4 * c + 2], acc[4 * c + 3]);
+    // db partial: reduce over the 128 faces that share this thread's column slice
 #pragma unroll
-    for (int q = 0; q < H; ++q) {
+    for (int q = 0; q < 16; ++q) {
         float v = dbs[q];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -488,11 +514,12 @@ __global__ void __launch_bounds__(TB) k_mpnn_bwd_dw(const MpnnView V, int layer,
     }
     tile_done();
     if (tid < H) {
-        float s = 0;
-        for (int w = 0; w < TB / 32; ++w) s += red[w][tid];
-        P[TB * H + tid] = s;
+        const int sq = tid / 16, j = tid % 16;
+        float sum = 0;
+        for (int w = 0; w < 4; ++w) sum += red[4 * sq + w][j];
+        P[TB * H + tid] = sum;
     }
-    if (warp == 0) tc::tmem_dealloc(taddr, H);
+    if (warp == 0) tc::tmem_dealloc(tbase, H);
 }
 
 // Sums the per-CTA dW / db partials in a fixed order into the flat gradient.
@@ -580,14 +607,14 @@ void mpnn_forward(const MpnnView& V, bool train, cudaStream_t s)
     if (train) {
         set_smem(k_mpnn_layer<16, true>, sm16);
         set_smem(k_mpnn_layer<128, true>, sm128);
-        k_mpnn_layer<16, true><<<g, TB, sm16, s>>>(V, 0);
-        for (int l = 1; l <= kMpnnLayers; ++l) k_mpnn_layer<128, true><<<g, TB, sm128, s>>>(V, l);
+        k_mpnn_layer<16, true><<<g, NT, sm16, s>>>(V, 0);
+        for (int l = 1; l <= kMpnnLayers; ++l) k_mpnn_layer<128, true><<<g, NT, sm128, s>>>(V, l);
     }
     else {
         set_smem(k_mpnn_layer<16, false>, sm16);
         set_smem(k_mpnn_layer<128, false>, sm128);
-        k_mpnn_layer<16, false><<<g, TB, sm16, s>>>(V, 0);
-        for (int l = 1; l <= kMpnnLayers; ++l) k_mpnn_layer<128, false><<<g, TB, sm128, s>>>(V, l);
+        k_mpnn_layer<16, false><<<g, NT, sm16, s>>>(V, 0);
+        for (int l = 1; l <= kMpnnLayers; ++l) k_mpnn_layer<128, false><<<g, NT, sm128, s>>>(V, l);
     }
 }
 
@@ -609,14 +636,14 @@ void mpnn_backward(const MpnnView& V, const double* target, double inv_nt, MpnnG
     set_smem(k_mpnn_bwd_dw<16>, smdw);
     const unsigned gadd = (unsigned)((V.F * 16 + 255) / 256);
     for (int l = kMpnnLayers; l >= 1; --l) {
-        k_mpnn_bwd_dx<<<g, TB, smdx, s>>>(V, l);
-        k_mpnn_bwd_dw<128><<<g, TB, smdw, s>>>(V, l, G.partials);
+        k_mpnn_bwd_dx<<<g, NT, smdx, s>>>(V, l);
+        k_mpnn_bwd_dw<128><<<g, NT, smdw, s>>>(V, l, G.partials);
         k_mpnn_reduce_dw<<<(2 * H * H + H + 255) / 256, 256, 0, s>>>(G.partials, g, 2 * H, G.g + G.off_W[l],
                                                                       G.g + G.off_b[l]);
         k_mpnn_gather_add<<<gadd, 256, 0, s>>>(V);
     }
     k_mpnn_dz0<<<(unsigned)((V.F * (H / 2) + 255) / 256), 256, 0, s>>>(V);
-    k_mpnn_bwd_dw<16><<<g, TB, smdw, s>>>(V, 0, G.partials);
+    k_mpnn_bwd_dw<16><<<g, NT, smdw, s>>>(V, 0, G.partials);
     k_mpnn_reduce_dw<<<(16 * H + H + 255) / 256, 256, 0, s>>>(G.partials, g, 16, G.g + G.off_W[0], G.g + G.off_b[0]);
 }
 
