@@ -20,6 +20,8 @@
 //    GB300 issues FP64 at 1/57 of the FP32 rate.
 #include <mutex>
 #include <unordered_map>
+#include <initializer_list>
+#include <utility>
 
 #include "mhfem_internal.h"
 
@@ -63,6 +65,27 @@ static int occ_grid(Kern kernel)
     const int g = sms * (nb > 0 ? (nb < 8 ? nb : 8) : 1);
     cache[(const void*)kernel] = g;
     return g;
+}
+
+// Launches an iteration kernel (one wave, occ_grid CTAs) with programmatic
+// stream serialization, so that its CTAs are scheduled while the preceding
+// kernel of the iteration drains (the kernel itself waits for that kernel's
+// results with griddepcontrol.wait).  Captured into a CUDA graph this becomes
+// a programmatic dependency edge.
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kernel)(KArgs...), cudaStream_t s, Args&&... args)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)occ_grid(kernel));
+    cfg.blockDim = dim3(KB);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
 // Compile-time ELL widths of the supported cell types: (2f - 1) n - 1 for
@@ -122,27 +145,56 @@ __device__ __forceinline__ bool ticket_last(uint32_t* counter)
     return last;
 }
 
-// Deterministic sum of the partials by the last block (fixed order).
+// Deterministic sum of the partials by the last block (fixed order): every
+// thread issues its (at most four per pass) partial loads together, the warp
+// sums them with shuffles and warp 0 adds the eight warp sums in order.
 template <int NV>
 __device__ __forceinline__ void final_sums(const double* partials, double (&out)[NV])
 {
-    __shared__ double sh[KB][4];
+    __shared__ double sh[KB / 32][4];
+    double acc[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) acc[q] = 0;
+    const int nb = (int)gridDim.x;
+    for (int b0 = threadIdx.x; b0 < nb; b0 += 4 * KB) {
+        double v[4][NV];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int b = b0 + j * KB;
+#pragma unroll
+            for (int q = 0; q < NV; ++q) v[j][q] = (b < nb) ? __ldcg(partials + (int64_t)b * 4 + q) : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int q = 0; q < NV; ++q) acc[q] += v[j][q];
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
-        double s = 0;
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += KB) s += __ldcg(partials + (int64_t)b * 4 + q);
-        sh[threadIdx.x][q] = s;
+        double v = acc[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[warp][q] = v;
     }
     __syncthreads();
-    for (int w = KB / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w)
 #pragma unroll
-            for (int q = 0; q < NV; ++q) sh[threadIdx.x][q] += sh[threadIdx.x + w][q];
-        __syncthreads();
+    for (int q = 0; q < NV; ++q) {
+        double t = 0;
+#pragma unroll
+        for (int w = 0; w < KB / 32; ++w) t += sh[w][q];
+        out[q] = t;
     }
-#pragma unroll
-    for (int q = 0; q < NV; ++q) out[q] = sh[0][q];
 }
+
+// Programmatic dependent launch: the iteration kernels are launched with
+// programmatic stream serialization, so the next kernel's CTAs are scheduled
+// while this one drains.  pdl_wait() blocks until the preceding kernel has
+// completed and its writes are visible (a no-op for an ordinary launch);
+// every kernel calls it before its first global access and releases its
+// dependent right after.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 // y_r = x_r + sum_k vals[k][r] x[cols[k][r]] (unit diagonal).  With a
 // compile-time width WW every column and value load of the row is issued
@@ -203,6 +255,7 @@ __global__ void __launch_bounds__(KB) k_init(const int32_t* cols, const T* vals,
         sc->rho = s[0];
         sc->rhnorm = sqrt(s[0]);
         sc->restart = 0;
+        sc->half = 0;
         sc->res = sqrt(s[0]) / bn;
         sc->it = 0;
         sc->snorm = 0;
@@ -213,18 +266,101 @@ __global__ void __launch_bounds__(KB) k_init(const int32_t* cols, const T* vals,
     }
 }
 
+// ---- vector access -------------------------------------------------------------
+//
+// The iteration kernels move V consecutive rows per thread and access (float4,
+// double2: 16-byte loads and stores) so that enough bytes are in flight per SM
+// to saturate HBM; the SpMVs of the FP32 solve also process RPT consecutive
+// rows per thread, loading each ELL slot of the RPT rows as one 16-byte word.
+// The host picks V and RPT from the pointers' alignment and the row count.
+
+template <typename T, int V>
+struct alignas(sizeof(T) * V) VecT {
+    T v[V];
+};
+
+template <typename T, int V>
+__device__ __forceinline__ VecT<T, V> ldv(const T* p, int64_t q)
+{
+    return *reinterpret_cast<const VecT<T, V>*>(p + q * V);
+}
+
+template <typename T, int V>
+__device__ __forceinline__ void stv(T* p, int64_t q, const VecT<T, V>& x)
+{
+    *reinterpret_cast<VecT<T, V>*>(p + q * V) = x;
+}
+
+// y_j = x_{r_j} + sum_k vals[k][r_j] x[cols[k][r_j]] for the RPT rows
+// r_j = RPT q + j; self_j = x_{r_j}.  RPT > 1 needs rows % RPT == 0 and a
+// compile-time width.
+template <typename T, int WW, int RPT>
+__device__ __forceinline__ void spmv_rows(const int32_t* __restrict__ cols, const T* __restrict__ vals, int W,
+                                          int64_t rows, int64_t q, const T* __restrict__ x, T (&y)[RPT],
+                                          T (&self)[RPT])
+{
+    if constexpr (WW > 0) {
+        VecT<int32_t, RPT> c[WW];
+        VecT<T, RPT> a[WW];
+#pragma unroll
+        for (int k = 0; k < WW; ++k) {
+            c[k] = ldv<int32_t, RPT>(cols + (int64_t)k * rows, q);
+            a[k] = ldv<T, RPT>(vals + (int64_t)k * rows, q);
+        }
+        T xg[WW][RPT];
+#pragma unroll
+        for (int k = 0; k < WW; ++k)
+#pragma unroll
+            for (int j = 0; j < RPT; ++j) xg[k][j] = x[c[k].v[j]];
+        const VecT<T, RPT> xs = ldv<T, RPT>(x, q);
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) {
+            T acc = xs.v[j];
+#pragma unroll
+            for (int k = 0; k < WW; ++k) acc = fma(a[k].v[j], xg[k][j], acc);
+            y[j] = acc;
+            self[j] = xs.v[j];
+        }
+    }
+    else {
+        static_assert(RPT == 1, "the run-time width takes one row per thread");
+        const T xs = x[q];
+        T acc = xs;
+        for (int k = 0; k < W; ++k) {
+            const int64_t o = (int64_t)k * rows + q;
+            acc = fma(__ldg(vals + o), x[__ldg(cols + o)], acc);
+        }
+        y[0] = acc;
+        self[0] = xs;
+    }
+}
+
+// Grid-stride bounds: threads of the whole grid, this thread's first index.
+#define MHFEM_GRID_STRIDE                                                  \
+    const int64_t gstride = (int64_t)gridDim.x * KB;                       \
+    const int64_t gtid = (int64_t)blockIdx.x * KB + threadIdx.x
+
 // v = A p ; alpha = rho / (rh . v)
-template <typename T, int WW>
+template <typename T, int WW, int RPT>
 __global__ void __launch_bounds__(KB) k_spmv_dot(const int32_t* cols, const T* vals, int W, int64_t rows,
                                                  const T* p, const T* rh, T* v,
                                                  KrylovScalars* sc, double* partials, uint32_t* counter)
 {
+    pdl_wait();
+    pdl_release();
     if (*(volatile int32_t*)&sc->done) return;
+    MHFEM_GRID_STRIDE;
     T acc[1] = {0};
-    for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB) {
-        const T y = spmv_row<T, WW>(cols, vals, W, rows, q, p);
-        v[q] = y;
-        acc[0] = fma(rh[q], y, acc[0]);
+    for (int64_t q = gtid; q < rows / RPT; q += gstride) {
+        T y[RPT], self[RPT];
+        spmv_rows<T, WW, RPT>(cols, vals, W, rows, q, p, y, self);
+        VecT<T, RPT> yv;
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) yv.v[j] = y[j];
+        stv<T, RPT>(v, q, yv);
+        const VecT<T, RPT> h = ldv<T, RPT>(rh, q);
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) acc[0] = fma(h.v[j], y[j], acc[0]);
     }
     block_reduce_store<T, 1>(acc, partials);
     if (!ticket_last(counter)) return;
@@ -238,46 +374,60 @@ __global__ void __launch_bounds__(KB) k_spmv_dot(const int32_t* cols, const T* v
     }
 }
 
-// s = r - alpha v ; ||s||
-template <typename T>
-__global__ void __launch_bounds__(KB) k_update_s(int64_t rows, const T* r, const T* v, T* s,
-                                                 KrylovScalars* sc, double* partials, uint32_t* counter)
+// s = r - alpha v  (||s|| is summed by the next kernel, which reads s anyway)
+template <typename T, int V>
+__global__ void __launch_bounds__(KB) k_update_s(int64_t rows, const T* r, const T* v, T* s, const KrylovScalars* sc)
 {
-    if (*(volatile int32_t*)&sc->done) return;
+    pdl_wait();
+    pdl_release();
+    if (*(volatile const int32_t*)&sc->done) return;
+    MHFEM_GRID_STRIDE;
     const T alpha = (T)sc->alpha;
-    T acc[1] = {0};
-    for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB) {
-        const T sv = fma(-alpha, v[q], r[q]);
-        s[q] = sv;
-        acc[0] = fma(sv, sv, acc[0]);
+    const int64_t nv = rows / V;
+    for (int64_t q = gtid; q < nv; q += gstride) {
+        const VecT<T, V> rr = ldv<T, V>(r, q), vv = ldv<T, V>(v, q);
+        VecT<T, V> ss;
+#pragma unroll
+        for (int j = 0; j < V; ++j) ss.v[j] = fma(-alpha, vv.v[j], rr.v[j]);
+        stv<T, V>(s, q, ss);
     }
-    block_reduce_store<T, 1>(acc, partials);
-    if (!ticket_last(counter)) return;
-    double sum[1];
-    final_sums<1>(partials, sum);
-    if (threadIdx.x == 0) sc->snorm = sqrt(sum[0]) / sc->bnorm;
+    for (int64_t q = nv * V + gtid; q < rows; q += gstride) s[q] = fma(-alpha, v[q], r[q]);
 }
 
-// t = A s ; omega = (t.s)/(t.t)  (skipped when ||s|| already meets the tolerance)
-template <typename T, int WW>
+// t = A s ; ||s|| ; omega = (t.s)/(t.t).  When ||s|| already meets the
+// tolerance the iteration ends on the half step (x += alpha p, next kernel)
+// and t is not used: the same decision as checking ||s|| before the SpMV.
+template <typename T, int WW, int RPT>
 __global__ void __launch_bounds__(KB) k_spmv_dots2(const int32_t* cols, const T* vals, int W, int64_t rows,
                                                    const T* s, T* t,
                                                    KrylovScalars* sc, double* partials, uint32_t* counter)
 {
+    pdl_wait();
+    pdl_release();
     if (*(volatile int32_t*)&sc->done) return;
-    if (sc->snorm < sc->tol) return;
-    T acc[2] = {0, 0};
-    for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB) {
-        const T y = spmv_row<T, WW>(cols, vals, W, rows, q, s);
-        t[q] = y;
-        acc[0] = fma(y, s[q], acc[0]);
-        acc[1] = fma(y, y, acc[1]);
+    MHFEM_GRID_STRIDE;
+    T acc[3] = {0, 0, 0};
+    for (int64_t q = gtid; q < rows / RPT; q += gstride) {
+        T y[RPT], sv[RPT];
+        spmv_rows<T, WW, RPT>(cols, vals, W, rows, q, s, y, sv);
+        VecT<T, RPT> yv;
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) {
+            yv.v[j] = y[j];
+            acc[0] = fma(y[j], sv[j], acc[0]);
+            acc[1] = fma(y[j], y[j], acc[1]);
+            acc[2] = fma(sv[j], sv[j], acc[2]);
+        }
+        stv<T, RPT>(t, q, yv);
     }
-    block_reduce_store<T, 2>(acc, partials);
+    block_reduce_store<T, 3>(acc, partials);
     if (!ticket_last(counter)) return;
-    double sum[2];
-    final_sums<2>(partials, sum);
+    double sum[3];
+    final_sums<3>(partials, sum);
     if (threadIdx.x == 0) {
+        sc->snorm = sqrt(sum[2]) / sc->bnorm;
+        sc->half = (sc->snorm < sc->tol) ? 1 : 0;
+        if (sc->half) return;
         sc->ts = sum[0];
         sc->tt = sum[1];
         if (!finite(sum[0]) || !finite(sum[1])) { sc->status = KS_NOTFINITE; sc->done = 1; }
@@ -287,17 +437,27 @@ __global__ void __launch_bounds__(KB) k_spmv_dots2(const int32_t* cols, const T*
 }
 
 // x += alpha p + omega s ; r = s - omega t ; rho_new = rh.r ; ||r|| ; beta
-template <typename T>
+template <typename T, int V>
 __global__ void __launch_bounds__(KB) k_update_xr(int64_t rows, T* x, const T* p, const T* s, const T* t,
                                                   T* r, const T* rh,
                                                   KrylovScalars* sc, double* partials, uint32_t* counter)
 {
+    pdl_wait();
+    pdl_release();
     if (*(volatile int32_t*)&sc->done) return;
+    MHFEM_GRID_STRIDE;
     const T alpha = (T)sc->alpha;
-    if (sc->snorm < sc->tol) {
+    const int64_t nv = rows / V;
+    if (sc->half) {
         // early exit on the half step: x += alpha p
-        for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB)
-            x[q] = fma(alpha, p[q], x[q]);
+        for (int64_t q = gtid; q < nv; q += gstride) {
+            VecT<T, V> xx = ldv<T, V>(x, q);
+            const VecT<T, V> pp = ldv<T, V>(p, q);
+#pragma unroll
+            for (int j = 0; j < V; ++j) xx.v[j] = fma(alpha, pp.v[j], xx.v[j]);
+            stv<T, V>(x, q, xx);
+        }
+        for (int64_t q = nv * V + gtid; q < rows; q += gstride) x[q] = fma(alpha, p[q], x[q]);
         if (!ticket_last(counter)) return;
         if (threadIdx.x == 0) {
             sc->res = sc->snorm;
@@ -309,7 +469,21 @@ __global__ void __launch_bounds__(KB) k_update_xr(int64_t rows, T* x, const T* p
     }
     const T omega = (T)sc->omega;
     T acc[2] = {0, 0};
-    for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB) {
+    for (int64_t q = gtid; q < nv; q += gstride) {
+        VecT<T, V> xx = ldv<T, V>(x, q);
+        const VecT<T, V> pp = ldv<T, V>(p, q), ss = ldv<T, V>(s, q), tt = ldv<T, V>(t, q), hh = ldv<T, V>(rh, q);
+        VecT<T, V> rr;
+#pragma unroll
+        for (int j = 0; j < V; ++j) {
+            xx.v[j] = fma(omega, ss.v[j], fma(alpha, pp.v[j], xx.v[j]));
+            rr.v[j] = fma(-omega, tt.v[j], ss.v[j]);
+            acc[0] = fma(hh.v[j], rr.v[j], acc[0]);
+            acc[1] = fma(rr.v[j], rr.v[j], acc[1]);
+        }
+        stv<T, V>(x, q, xx);
+        stv<T, V>(r, q, rr);
+    }
+    for (int64_t q = nv * V + gtid; q < rows; q += gstride) {
         const T sv = s[q];
         x[q] = fma(omega, sv, fma(alpha, p[q], x[q]));
         const T rv = fma(-omega, t[q], sv);
@@ -345,22 +519,84 @@ __global__ void __launch_bounds__(KB) k_update_xr(int64_t rows, T* x, const T* p
 }
 
 // p = r + beta (p - omega v); on a restart rh = p = r
-template <typename T>
+template <typename T, int V>
 __global__ void __launch_bounds__(KB) k_update_p(int64_t rows, T* p, const T* r, const T* v, T* rh,
                                                  const KrylovScalars* sc)
 {
+    pdl_wait();
+    pdl_release();
     if (*(volatile const int32_t*)&sc->done) return;
+    MHFEM_GRID_STRIDE;
     const T beta = (T)sc->beta, omega = (T)sc->omega;
+    const int64_t nv = rows / V;
     if (sc->restart) {
-        for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB) {
+        for (int64_t q = gtid; q < nv; q += gstride) {
+            const VecT<T, V> rr = ldv<T, V>(r, q);
+            stv<T, V>(p, q, rr);
+            stv<T, V>(rh, q, rr);
+        }
+        for (int64_t q = nv * V + gtid; q < rows; q += gstride) {
             const T rv = r[q];
             p[q] = rv;
             rh[q] = rv;
         }
         return;
     }
-    for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB)
-        p[q] = fma(beta, fma(-omega, v[q], p[q]), r[q]);
+    for (int64_t q = gtid; q < nv; q += gstride) {
+        VecT<T, V> pp = ldv<T, V>(p, q);
+        const VecT<T, V> rr = ldv<T, V>(r, q), vv = ldv<T, V>(v, q);
+#pragma unroll
+        for (int j = 0; j < V; ++j) pp.v[j] = fma(beta, fma(-omega, vv.v[j], pp.v[j]), rr.v[j]);
+        stv<T, V>(p, q, pp);
+    }
+    for (int64_t q = nv * V + gtid; q < rows; q += gstride) p[q] = fma(beta, fma(-omega, v[q], p[q]), r[q]);
+}
+
+// ---- launch shapes ---------------------------------------------------------------
+
+static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// Vector width of the streaming updates: 16-byte accesses when every vector
+// of the solve starts on a 16-byte boundary (the tail rows go one by one).
+template <typename T>
+static bool vec_ok(std::initializer_list<const void*> ptrs)
+{
+    for (const void* p : ptrs)
+        if (!aligned16(p)) return false;
+    return true;
+}
+
+// Rows per thread of the SpMV: 4 (FP32) when the ELL slots and the vectors
+// are 16-byte aligned (rows % 4 == 0) and the width is a compile-time one of
+// at most 6 entries (so the 4 rows' loads stay in registers).
+static bool spmv4_ok(const EllMatrix& A, std::initializer_list<const void*> ptrs)
+{
+    if (A.rows % 4 != 0 || (A.width != 4 && A.width != 6)) return false;
+    for (const void* p : ptrs)
+        if (!aligned16(p)) return false;
+    return aligned16(A.cols) && aligned16(A.vals32);
+}
+
+// Rows per thread of an SpMV instance: RPT for the widths 4 and 6, else 1.
+constexpr int spmv_rpt(int WW, int RPT) { return (WW == 4 || WW == 6) ? RPT : 1; }
+
+// One BiCGStab iteration: five kernels, each a single wave.  Streaming
+// updates with V rows per thread, SpMVs with RPT rows per thread.
+template <typename T, int V, int RPT>
+static void iterate(const EllMatrix& A, const T* vals, T* x, T* r, T* rh, T* p, T* v, T* s, T* t,
+                    KrylovScalars* sc, KrylovWork& W, int iters, cudaStream_t st)
+{
+    const int32_t* cols = A.cols;
+    for (int it = 0; it < iters; ++it) {
+        MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dot<T, WW, spmv_rpt(WW, RPT)>, st, cols, vals, A.width,
+                                                 A.rows, (const T*)p, (const T*)rh, v, sc, W.partials, W.counters));
+        launch_pdl(k_update_s<T, V>, st, A.rows, (const T*)r, (const T*)v, s, (const KrylovScalars*)sc);
+        MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dots2<T, WW, spmv_rpt(WW, RPT)>, st, cols, vals, A.width,
+                                                 A.rows, (const T*)s, t, sc, W.partials, W.counters));
+        launch_pdl(k_update_xr<T, V>, st, A.rows, x, (const T*)p, (const T*)s, (const T*)t, r, (const T*)rh, sc,
+                   W.partials, W.counters);
+        launch_pdl(k_update_p<T, V>, st, A.rows, p, (const T*)r, (const T*)v, rh, (const KrylovScalars*)sc);
+    }
 }
 
 // ---- FP64 solve --------------------------------------------------------------
@@ -376,18 +612,14 @@ void krylov_init_fp64(const EllMatrix& A, const double* b, double* x, KrylovWork
                                               W.r, W.rh, W.p, W.sc, W.partials, W.counters)));
 }
 
+// The FP64 SpMV keeps one row per thread: it is bound by the FP64 pipe as
+// much as by HBM, and more rows per thread only lower the occupancy.
 void krylov_iterate_fp64(const EllMatrix& A, double* x, KrylovWork& W, int iters, cudaStream_t s)
 {
-    for (int it = 0; it < iters; ++it) {
-        MHFEM_WIDTH_DISPATCH(A.width, (k_spmv_dot<double, WW><<<occ_grid(k_spmv_dot<double, WW>), KB, 0, s>>>(A.cols, A.vals, A.width, A.rows,
-                                                  W.p, W.rh, W.v, W.sc, W.partials, W.counters)));
-        k_update_s<double><<<occ_grid(k_update_s<double>), KB, 0, s>>>(A.rows, W.r, W.v, W.s, W.sc, W.partials, W.counters);
-        MHFEM_WIDTH_DISPATCH(A.width, (k_spmv_dots2<double, WW><<<occ_grid(k_spmv_dots2<double, WW>), KB, 0, s>>>(A.cols, A.vals, A.width,
-                                                    A.rows, W.s, W.t, W.sc, W.partials, W.counters)));
-        k_update_xr<double><<<occ_grid(k_update_xr<double>), KB, 0, s>>>(A.rows, x, W.p, W.s, W.t, W.r, W.rh, W.sc, W.partials,
-                                                  W.counters);
-        k_update_p<double><<<occ_grid(k_update_p<double>), KB, 0, s>>>(A.rows, W.p, W.r, W.v, W.rh, W.sc);
-    }
+    if (vec_ok<double>({x, W.r, W.rh, W.p, W.v, W.s, W.t}))
+        iterate<double, 2, 1>(A, A.vals, x, W.r, W.rh, W.p, W.v, W.s, W.t, W.sc, W, iters, s);
+    else
+        iterate<double, 1, 1>(A, A.vals, x, W.r, W.rh, W.p, W.v, W.s, W.t, W.sc, W, iters, s);
 }
 
 // ---- residual of a candidate (learned gate) ------------------------------------
@@ -485,6 +717,7 @@ __global__ void __launch_bounds__(KB) k_inner_init(int64_t rows, const double* r
         sc->rho = s[0];
         sc->rhnorm = sqrt(s[0]);
         sc->restart = 0;
+        sc->half = 0;
         sc->res = 1.0;
         sc->it = 0;
         sc->snorm = 1.0;
@@ -518,26 +751,32 @@ void mixed_inner_init(KrylovWork& W, double inner_tol, int adaptive, int max_ite
 
 void krylov_iterate_fp32(const EllMatrix& A, KrylovWork& W, int iters, cudaStream_t s)
 {
-    for (int it = 0; it < iters; ++it) {
-        MHFEM_WIDTH_DISPATCH(A.width, (k_spmv_dot<float, WW><<<occ_grid(k_spmv_dot<float, WW>), KB, 0, s>>>(A.cols, A.vals32, A.width, A.rows,
-                                                 W.p32, W.rh32, W.v32, W.sc32, W.partials, W.counters)));
-        k_update_s<float><<<occ_grid(k_update_s<float>), KB, 0, s>>>(A.rows, W.r32, W.v32, W.s32, W.sc32, W.partials, W.counters);
-        MHFEM_WIDTH_DISPATCH(A.width, (k_spmv_dots2<float, WW><<<occ_grid(k_spmv_dots2<float, WW>), KB, 0, s>>>(A.cols, A.vals32, A.width,
-                                                   A.rows, W.s32, W.t32, W.sc32, W.partials, W.counters)));
-        k_update_xr<float><<<occ_grid(k_update_xr<float>), KB, 0, s>>>(A.rows, W.x32, W.p32, W.s32, W.t32, W.r32, W.rh32, W.sc32,
-                                                 W.partials, W.counters);
-        k_update_p<float><<<occ_grid(k_update_p<float>), KB, 0, s>>>(A.rows, W.p32, W.r32, W.v32, W.rh32, W.sc32);
-    }
+    const bool v4 = vec_ok<float>({W.x32, W.r32, W.rh32, W.p32, W.v32, W.s32, W.t32});
+    if (v4 && spmv4_ok(A, {W.p32, W.rh32, W.v32, W.s32, W.t32}))
+        iterate<float, 4, 4>(A, A.vals32, W.x32, W.r32, W.rh32, W.p32, W.v32, W.s32, W.t32, W.sc32, W, iters, s);
+    else if (v4)
+        iterate<float, 4, 1>(A, A.vals32, W.x32, W.r32, W.rh32, W.p32, W.v32, W.s32, W.t32, W.sc32, W, iters, s);
+    else
+        iterate<float, 1, 1>(A, A.vals32, W.x32, W.r32, W.rh32, W.p32, W.v32, W.s32, W.t32, W.sc32, W, iters, s);
 }
 
 void krylov_spmv_dot_once(const EllMatrix& A, KrylovWork& W, bool fp32, cudaStream_t s)
 {
-    if (fp32)
-        MHFEM_WIDTH_DISPATCH(A.width, (k_spmv_dot<float, WW><<<occ_grid(k_spmv_dot<float, WW>), KB, 0, s>>>(A.cols, A.vals32, A.width, A.rows,
-                                                 W.p32, W.rh32, W.v32, W.sc32, W.partials, W.counters)));
+    if (fp32) {
+        if (spmv4_ok(A, {W.p32, W.rh32, W.v32}))
+            MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dot<float, WW, spmv_rpt(WW, 4)>, s,
+                                                     (const int32_t*)A.cols, (const float*)A.vals32, A.width, A.rows,
+                                                     (const float*)W.p32, (const float*)W.rh32, W.v32, W.sc32,
+                                                     W.partials, W.counters));
+        else
+            MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dot<float, WW, 1>, s, (const int32_t*)A.cols,
+                                                     (const float*)A.vals32, A.width, A.rows, (const float*)W.p32,
+                                                     (const float*)W.rh32, W.v32, W.sc32, W.partials, W.counters));
+    }
     else
-        MHFEM_WIDTH_DISPATCH(A.width, (k_spmv_dot<double, WW><<<occ_grid(k_spmv_dot<double, WW>), KB, 0, s>>>(A.cols, A.vals, A.width, A.rows,
-                                                  W.p, W.rh, W.v, W.sc, W.partials, W.counters)));
+        MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dot<double, WW, 1>, s, (const int32_t*)A.cols,
+                                                 (const double*)A.vals, A.width, A.rows, (const double*)W.p,
+                                                 (const double*)W.rh, W.v, W.sc, W.partials, W.counters));
 }
 
 void mixed_apply_correction(double* x, KrylovWork& W, cudaStream_t s)

@@ -25,7 +25,7 @@ struct KrylovScalars {
     double bnorm, res, snorm;
     double rv, ts, tt, rr, rhnorm;
     int32_t it, done, status, max_iter;
-    int32_t restart, pad;
+    int32_t restart, half;  // half: the iteration ends on the half step (||s|| < tol)
     double tol;
 };
 
