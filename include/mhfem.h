@@ -118,6 +118,8 @@ typedef struct {
     double  guess_residual;   /* learned form: relative residual of the predicted guess */
     double  warm_residual;    /* relative residual of the previous-step warm start */
     double  ms_pre, ms_assemble, ms_solve, ms_post;   /* device time per phase */
+    double  ms_guess;         /* learned form: device time of the guess (features, network, gate
+                                 residuals), included in ms_solve; 0 for the other forms */
 } mhfem_step_stats;
 
 /* ---- lifecycle ---------------------------------------------------------- */

@@ -624,10 +624,12 @@ mhfem_status mhfem_solve(mhfem_t h, mhfem_step_stats* stats)
     }
     int iters = 0, sweeps = 1;
     double res = 0;
+    h->guess_timed = false;
     if (stats) {
         stats->guess_used = 0;
         stats->guess_residual = -1;
         stats->warm_residual = -1;
+        stats->ms_guess = 0;
     }
     if (h->desc.form == MHFEM_FORM_MIXED) st = run_mixed(h, &iters, &sweeps, &res);
     else if (h->desc.form == MHFEM_FORM_LEARNED) st = learned_solve(h, &iters, &res, stats);
@@ -671,6 +673,9 @@ mhfem_status mhfem_step(mhfem_t h, double t, double tau, mhfem_step_stats* stats
         cudaEventElapsedTime(&c, h->ev[2], h->ev[3]);
         cudaEventElapsedTime(&d, h->ev[3], h->ev[4]);
         stats->ms_pre = a; stats->ms_assemble = b; stats->ms_solve = c; stats->ms_post = d;
+        float g = 0;
+        if (h->guess_timed) cudaEventElapsedTime(&g, h->ev[5], h->ev[6]);
+        stats->ms_guess = g;
     }
     return MHFEM_OK;
 }

@@ -70,7 +70,8 @@ struct mhfem_solver_s {
     cudaGraphExec_t g64 = nullptr, g32 = nullptr;
     int g64_iters = 0, g32_iters = 0;
 
-    cudaEvent_t ev[5] = {};
+    cudaEvent_t ev[7] = {};  // phase boundaries 0..4; 5, 6: the learned guess
+    bool guess_timed = false;
     std::vector<void*> allocs;
 
     // host copies used to build the learned form's static features

@@ -94,21 +94,32 @@ __device__ __forceinline__ void tile_done()
 
 // ---- forward layer ----------------------------------------------------------
 
-// 512 threads per 128-row tile: thread (r, qs) = (tid % 128, tid / 128) stages
-// and finishes the 16-column slice qs of row r.  Its warp is 4 qs + r / 32, so
-// warp % 4 == r / 32 is the TMEM lane quarter the warp may read, and the
-// thread keeps its own slice of h_l in registers for the residual.
+// Row stride (bytes) of the output staging tile: 128 bytes of BF16 plus 16
+// bytes of padding, so the epilogue's per-row 16-byte stores spread over all
+// banks.
+constexpr int kOutStride = 2 * H + 16;
+
+// Global <-> tile traffic is row-coalesced: thread t moves the 16-byte chunk
+// c = t % 8 (columns 8c .. 8c + 7) of the rows t / 8 and t / 8 + 64, so a warp
+// reads or writes four whole 128-byte rows per instruction (for the
+// neighbour gather too: the four rows' k-th neighbours).  The epilogue is
+// row-per-thread: thread (r, qs) = (t % 128, t / 128) reads columns
+// 16 qs .. 16 qs + 15 of row r from TMEM (warp % 4 == r / 32 is its TMEM lane
+// quarter) and writes them to the staging tile.
 template <int KIN, bool TRAIN>
 __global__ void __launch_bounds__(NT) k_mpnn_layer(const MpnnView V, int layer)
 {
     extern __shared__ __align__(128) uint8_t smem[];
-    uint8_t* sA = smem;                      // 128 x KIN
-    uint8_t* sB = smem + TB * KIN * 2;       // 64 x KIN
+    uint8_t* sA = smem;                            // 128 x KIN (K-major)
+    uint8_t* sB = sA + TB * KIN * 2;               // 64 x KIN (K-major)
+    uint8_t* sO = sB + H * KIN * 2;                // 128 rows x kOutStride: h_{l+1}
+    uint8_t* sZ = sO + TB * kOutStride;            // 128 rows x kOutStride: z_l (training)
     __shared__ uint64_t mbar;
     __shared__ uint32_t tbase;
     __shared__ float sbias[H];
     const int tid = threadIdx.x, warp = tid >> 5;
-    const int r = tid & (TB - 1), qs = tid >> 7;
+    const int r = tid & (TB - 1), qs = tid >> 7;  // epilogue mapping
+    const int c8 = tid & 7, slot = tid >> 3;      // row-coalesced mapping
     const int64_t F = V.F;
 
     const __nv_bfloat16* Wf = V.w_fwd[layer];  // [64][KIN]
@@ -130,66 +141,83 @@ __global__ void __launch_bounds__(NT) k_mpnn_layer(const MpnnView V, int layer)
     const int64_t ntiles = (F + TB - 1) / TB;
 
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int64_t row = tile * TB + r;
-        const bool valid = row < F;
-        uint4 self0 = make_uint4(0, 0, 0, 0), self1 = self0;
+        const int64_t row0 = tile * TB;
         if constexpr (KIN == 16) {
-            if (qs < 2) {
+            // 128 rows x 32 bytes: two chunks per row
+            if (tid < 2 * TB) {
+                const int rr = tid >> 1, ch = tid & 1;
                 uint4 v = make_uint4(0, 0, 0, 0);
-                if (valid) v = *reinterpret_cast<const uint4*>(hin + row * 16 + 8 * qs);
-                st_tile(sA, r, 8 * qs, 16, v);
+                if (row0 + rr < F) v = __ldg(reinterpret_cast<const uint4*>(hin + (row0 + rr) * 16 + 8 * ch));
+                st_tile(sA, rr, 8 * ch, 16, v);
             }
         }
         else {
-            if (valid) {
-                self0 = *reinterpret_cast<const uint4*>(hin + row * H + 16 * qs);
-                self1 = *reinterpret_cast<const uint4*>(hin + row * H + 16 * qs + 8);
-            }
-            st_tile(sA, r, 16 * qs, KIN, self0);
-            st_tile(sA, r, 16 * qs + 8, KIN, self1);
-            // neighbour mean of this thread's 16 columns
-            float acc[16];
+            // neighbour indices of both rows first (padding entries point at
+            // the row itself); the eight lanes of a row read the same words
+            int32_t nbs[2][kMpnnMaxWidth];
 #pragma unroll
-            for (int q = 0; q < 16; ++q) acc[q] = 0.f;
-            const int d = valid ? (int)V.deg[row] : 0;
-            if (valid) {
-                for (int k = 0; k < V.W; ++k) {
-                    const int32_t c = V.nbr[(int64_t)k * F + row];
-                    if (c == (int32_t)row) continue;
-                    const uint4* src = reinterpret_cast<const uint4*>(hin + (int64_t)c * H + 16 * qs);
+            for (int j = 0; j < 2; ++j) {
+                const int64_t row = row0 + slot + 64 * j;
 #pragma unroll
-                    for (int u = 0; u < 2; ++u) {
-                        const uint4 v = src[u];
-                        const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-                        for (int t = 0; t < 4; ++t) {
-                            const float2 f = unpack_bf16(w4[t]);
-                            acc[8 * u + 2 * t] += f.x;
-                            acc[8 * u + 2 * t + 1] += f.y;
-                        }
-                    }
+                for (int k = 0; k < kMpnnMaxWidth; ++k) {
+                    int32_t c = -1;
+                    if (row < F && k < V.W) c = __ldg(V.nbr + (int64_t)k * F + row);
+                    nbs[j][k] = (c == (int32_t)row) ? -1 : c;
                 }
             }
-            const float inv = d > 0 ? 1.0f / (float)d : 0.0f;
 #pragma unroll
-            for (int u = 0; u < 2; ++u) {
+            for (int j = 0; j < 2; ++j) {
+                const int rr = slot + 64 * j;
+                const int64_t row = row0 + rr;
+                const bool valid = row < F;
+                const int32_t* nb = nbs[j];
+                uint4 self = make_uint4(0, 0, 0, 0);
+                if (valid) self = __ldg(reinterpret_cast<const uint4*>(hin + row * H + 8 * c8));
+                const int d = valid ? (int)V.deg[row] : 0;
+                uint4 g[kMpnnMaxWidth];
+#pragma unroll
+                for (int k = 0; k < kMpnnMaxWidth; ++k) {
+                    g[k] = make_uint4(0, 0, 0, 0);
+                    if (nb[k] >= 0) g[k] = __ldg(reinterpret_cast<const uint4*>(hin + (int64_t)nb[k] * H + 8 * c8));
+                }
+                st_tile(sA, rr, 8 * c8, KIN, self);
+                float acc[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) acc[q] = 0.f;
+#pragma unroll
+                for (int k = 0; k < kMpnnMaxWidth; ++k) {
+                    const uint32_t w4[4] = {g[k].x, g[k].y, g[k].z, g[k].w};
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        const float2 f = unpack_bf16(w4[t]);
+                        acc[2 * t] += f.x;
+                        acc[2 * t + 1] += f.y;
+                    }
+                }
+                const float inv = d > 0 ? 1.0f / (float)d : 0.0f;
                 uint4 v;
-                v.x = pack_bf16(acc[8 * u + 0] * inv, acc[8 * u + 1] * inv);
-                v.y = pack_bf16(acc[8 * u + 2] * inv, acc[8 * u + 3] * inv);
-                v.z = pack_bf16(acc[8 * u + 4] * inv, acc[8 * u + 5] * inv);
-                v.w = pack_bf16(acc[8 * u + 6] * inv, acc[8 * u + 7] * inv);
-                st_tile(sA, r, H + 16 * qs + 8 * u, KIN, v);
-                if (TRAIN && valid) *reinterpret_cast<uint4*>(V.a[layer] + row * H + 16 * qs + 8 * u) = v;
+                v.x = pack_bf16(acc[0] * inv, acc[1] * inv);
+                v.y = pack_bf16(acc[2] * inv, acc[3] * inv);
+                v.z = pack_bf16(acc[4] * inv, acc[5] * inv);
+                v.w = pack_bf16(acc[6] * inv, acc[7] * inv);
+                st_tile(sA, rr, H + 8 * c8, KIN, v);
+                if (TRAIN && valid) *reinterpret_cast<uint4*>(V.a[layer] + row * H + 8 * c8) = v;
             }
         }
         if (!tile_mma<TB, H, KIN>(sA, sB, tbase, ts, false)) {
             if (tid == 0) atomicOr(V.err, 4);
             break;
         }
-        float acc[16];
-        tc::tmem_ld_x16(taddr, acc);
-        if (valid) {
-            const uint32_t sw[8] = {self0.x, self0.y, self0.z, self0.w, self1.x, self1.y, self1.z, self1.w};
+        {
+            float acc[16];
+            tc::tmem_ld_x16(taddr, acc);
+            uint32_t sw[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            if constexpr (KIN != 16) {
+                const uint4 s0 = *reinterpret_cast<const uint4*>(sA + tc::kmajor_offset(r, 16 * qs, KIN));
+                const uint4 s1 = *reinterpret_cast<const uint4*>(sA + tc::kmajor_offset(r, 16 * qs + 8, KIN));
+                sw[0] = s0.x; sw[1] = s0.y; sw[2] = s0.z; sw[3] = s0.w;
+                sw[4] = s1.x; sw[5] = s1.y; sw[6] = s1.z; sw[7] = s1.w;
+            }
             uint32_t zo[8], ho[8];
 #pragma unroll
             for (int t = 0; t < 8; ++t) {
@@ -204,16 +232,29 @@ __global__ void __launch_bounds__(NT) k_mpnn_layer(const MpnnView V, int layer)
                 zo[t] = pack_bf16(z0, z1);
                 ho[t] = pack_bf16(o0, o1);
             }
-            uint4* ho4 = reinterpret_cast<uint4*>(hout + row * H + 16 * qs);
-            ho4[0] = make_uint4(ho[0], ho[1], ho[2], ho[3]);
-            ho4[1] = make_uint4(ho[4], ho[5], ho[6], ho[7]);
+            uint4* so = reinterpret_cast<uint4*>(sO + r * kOutStride + 32 * qs);
+            so[0] = make_uint4(ho[0], ho[1], ho[2], ho[3]);
+            so[1] = make_uint4(ho[4], ho[5], ho[6], ho[7]);
             if (TRAIN) {
-                uint4* zo4 = reinterpret_cast<uint4*>(V.z[layer] + row * H + 16 * qs);
-                zo4[0] = make_uint4(zo[0], zo[1], zo[2], zo[3]);
-                zo4[1] = make_uint4(zo[4], zo[5], zo[6], zo[7]);
+                uint4* sz = reinterpret_cast<uint4*>(sZ + r * kOutStride + 32 * qs);
+                sz[0] = make_uint4(zo[0], zo[1], zo[2], zo[3]);
+                sz[1] = make_uint4(zo[4], zo[5], zo[6], zo[7]);
             }
         }
         tile_done();
+        // row-coalesced write-out of the staged tile
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int rr = slot + 64 * j;
+            const int64_t row = row0 + rr;
+            if (row < F) {
+                *reinterpret_cast<uint4*>(hout + row * H + 8 * c8) =
+                    *reinterpret_cast<const uint4*>(sO + rr * kOutStride + 16 * c8);
+                if (TRAIN)
+                    *reinterpret_cast<uint4*>(V.z[layer] + row * H + 8 * c8) =
+                        *reinterpret_cast<const uint4*>(sZ + rr * kOutStride + 16 * c8);
+            }
+        }
     }
     tile_done();
     if (warp == 0) tc::tmem_dealloc(tbase, H);
@@ -385,14 +426,53 @@ __global__ void __launch_bounds__(256) k_mpnn_gather_add(const MpnnView V)
     const int64_t row = gid >> 4;
     const int c = (int)(gid & 15) * 4;
     if (row >= V.F) return;
+    int32_t nb[kMpnnMaxWidth];
+#pragma unroll
+    for (int k = 0; k < kMpnnMaxWidth; ++k) {
+        const int32_t e = (k < V.W) ? __ldg(V.nbr + (int64_t)k * V.F + row) : (int32_t)row;
+        nb[k] = (e == (int32_t)row) ? -1 : e;
+    }
+    float4 g[kMpnnMaxWidth];
+#pragma unroll
+    for (int k = 0; k < kMpnnMaxWidth; ++k)
+        g[k] = (nb[k] >= 0) ? __ldg(reinterpret_cast<const float4*>(V.ga + (int64_t)nb[k] * H + c))
+                            : make_float4(0.f, 0.f, 0.f, 0.f);
     float4 s = *reinterpret_cast<const float4*>(V.dh + row * H + c);
-    for (int k = 0; k < V.W; ++k) {
-        const int32_t e = V.nbr[(int64_t)k * V.F + row];
-        if (e == (int32_t)row) continue;
-        const float4 g = *reinterpret_cast<const float4*>(V.ga + (int64_t)e * H + c);
-        s.x += g.x; s.y += g.y; s.z += g.z; s.w += g.w;
+#pragma unroll
+    for (int k = 0; k < kMpnnMaxWidth; ++k) {
+        s.x += g[k].x; s.y += g[k].y; s.z += g[k].z; s.w += g[k].w;
     }
     *reinterpret_cast<float4*>(V.dh + row * H + c) = s;
+}
+
+// Inference decoder: guess = base + sd (h4 . wd + bd) on free rows, the
+// Dirichlet value on fixed rows.  Eight lanes per face, 8 columns (16 bytes)
+// each, so a warp reads four whole 128-byte rows per load.
+__global__ void __launch_bounds__(256) k_mpnn_guess(const MpnnView V, const double* base, double sd,
+                                                    const double* rhs, double* guess)
+{
+    const int l8 = threadIdx.x & 7;
+    float w[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) w[q] = V.wd[8 * l8 + q];
+    const float bd = V.bd[0];
+    const __nv_bfloat16* h4 = V.h[kMpnnLayers + 1];
+    const int64_t stride = (int64_t)gridDim.x * (256 / 8);
+    for (int64_t row = ((int64_t)blockIdx.x * 256 + threadIdx.x) >> 3; row < V.F; row += stride) {
+        const uint4 v = __ldg(reinterpret_cast<const uint4*>(h4 + row * H + 8 * l8));
+        const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+        float o = 0.f;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const float2 f = unpack_bf16(w4[t]);
+            o = fmaf(f.x, w[2 * t], o);
+            o = fmaf(f.y, w[2 * t + 1], o);
+        }
+        o += __shfl_xor_sync(0xffffffffu, o, 1);
+        o += __shfl_xor_sync(0xffffffffu, o, 2);
+        o += __shfl_xor_sync(0xffffffffu, o, 4);
+        if (l8 == 0) guess[row] = V.fixed[row] ? rhs[row] : base[row] + sd * (double)(o + bd);
+    }
 }
 
 // dz0 = dh * (z0 > 0) in BF16 (encoder)
@@ -588,10 +668,14 @@ static int mpnn_grid(int64_t F)
 
 int mpnn_grid_size(int64_t F) { return mpnn_grid(F); }
 
+// Dynamic shared memory limit of a kernel, with the carveout at its maximum
+// so that the occupancy the registers allow is not cut by a small default
+// shared-memory partition.
 template <typename Kern>
 static void set_smem(Kern k, int bytes)
 {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
 }
 
 // Every tensor-core kernel requests at least this much shared memory, so at
@@ -600,27 +684,67 @@ static void set_smem(Kern k, int bytes)
 constexpr int kMinSmem = 56 * 1024;
 static int smem_req(int need) { return need > kMinSmem ? need : kMinSmem; }
 
+// Grid of a forward layer kernel: every CTA resident at once (the kernel
+// loops over tiles), so no second wave waits for the first.
+template <typename Kern>
+static int resident_grid(Kern k, int smem, int64_t F)
+{
+    int dev = 0, sms = 0, regs_sm = 0, smem_sm = 0, thr_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+    cudaFuncAttributes fa{};
+    int per_sm = 1;
+    if (cudaFuncGetAttributes(&fa, k) == cudaSuccess && fa.numRegs > 0) {
+        // registers are allocated per warp in units of 256
+        const int regs_warp = ((fa.numRegs * 32 + 255) / 256) * 256;
+        const int by_regs = regs_sm / (regs_warp * (NT / 32));
+        const int by_smem = smem_sm / ((int)fa.sharedSizeBytes + smem + 1024);  // 1 KB reserved per CTA
+        const int by_thr = thr_sm / NT;
+        per_sm = by_regs < by_smem ? by_regs : by_smem;
+        per_sm = per_sm < by_thr ? per_sm : by_thr;
+    }
+    if (per_sm < 1) per_sm = 1;
+    if (per_sm > 4) per_sm = 4;  // TMEM: at most 4 CTAs x 128 columns per SM
+    const int64_t tiles = (F + TB - 1) / TB;
+    const int64_t g = (int64_t)(sms > 0 ? sms : 152) * per_sm;
+    return (int)(tiles < g ? (tiles > 0 ? tiles : 1) : g);
+}
+
+// Shared memory of a forward layer: A and B tiles, the output staging tile
+// and, in training, the pre-activation staging tile.
+static int layer_smem(int kin, bool train)
+{
+    return smem_req((TB + H) * kin * 2 + (train ? 2 : 1) * TB * kOutStride);
+}
+
+template <bool TRAIN>
+static void forward_layers(const MpnnView& V, cudaStream_t s)
+{
+    const int sm16 = layer_smem(16, TRAIN), sm128 = layer_smem(128, TRAIN);
+    set_smem(k_mpnn_layer<16, TRAIN>, sm16);
+    set_smem(k_mpnn_layer<128, TRAIN>, sm128);
+    k_mpnn_layer<16, TRAIN><<<resident_grid(k_mpnn_layer<16, TRAIN>, sm16, V.F), NT, sm16, s>>>(V, 0);
+    const int g = resident_grid(k_mpnn_layer<128, TRAIN>, sm128, V.F);
+    for (int l = 1; l <= kMpnnLayers; ++l) k_mpnn_layer<128, TRAIN><<<g, NT, sm128, s>>>(V, l);
+}
+
 void mpnn_forward(const MpnnView& V, bool train, cudaStream_t s)
 {
-    const int g = mpnn_grid(V.F);
-    const int sm16 = smem_req((TB + H) * 16 * 2), sm128 = smem_req((TB + H) * 2 * H * 2);
-    if (train) {
-        set_smem(k_mpnn_layer<16, true>, sm16);
-        set_smem(k_mpnn_layer<128, true>, sm128);
-        k_mpnn_layer<16, true><<<g, NT, sm16, s>>>(V, 0);
-        for (int l = 1; l <= kMpnnLayers; ++l) k_mpnn_layer<128, true><<<g, NT, sm128, s>>>(V, l);
-    }
-    else {
-        set_smem(k_mpnn_layer<16, false>, sm16);
-        set_smem(k_mpnn_layer<128, false>, sm128);
-        k_mpnn_layer<16, false><<<g, NT, sm16, s>>>(V, 0);
-        for (int l = 1; l <= kMpnnLayers; ++l) k_mpnn_layer<128, false><<<g, NT, sm128, s>>>(V, l);
-    }
+    if (train) forward_layers<true>(V, s);
+    else forward_layers<false>(V, s);
 }
 
 void mpnn_guess(const MpnnView& V, const double* base, double sd, const double* rhs, double* guess, cudaStream_t s)
 {
-    k_mpnn_decode<false><<<mpnn_grid(V.F), 256, 0, s>>>(V, base, sd, rhs, nullptr, guess, 0.0);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t blocks = (V.F + 31) / 32;
+    const int64_t cap = (int64_t)(sms > 0 ? sms : 152) * 8;
+    k_mpnn_guess<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(V, base, sd, rhs, guess);
 }
 
 void mpnn_backward(const MpnnView& V, const double* target, double inv_nt, MpnnGrads& G, cudaStream_t s)
@@ -628,23 +752,28 @@ void mpnn_backward(const MpnnView& V, const double* target, double inv_nt, MpnnG
     const int gdec = mpnn_grid(V.F);
     k_mpnn_decode<true><<<gdec, 256, 0, s>>>(V, nullptr, 0.0, nullptr, target, nullptr, inv_nt);
     k_mpnn_reduce_dec<<<1, 128, 0, s>>>(V.dec_partials, gdec, G.g + G.off_wd, G.g + G.off_bd, G.loss, inv_nt);
-    const int g = mpnn_grid(V.F);
     const int smdx = smem_req((TB + 2 * H) * H * 2);
     const int smdw = smem_req((TB + H) * TB * 2);
     set_smem(k_mpnn_bwd_dx, smdx);
     set_smem(k_mpnn_bwd_dw<128>, smdw);
     set_smem(k_mpnn_bwd_dw<16>, smdw);
+    // one resident wave each; the dW partials (one per CTA) fit the buffer
+    // sized for mpnn_grid, which resident_grid never exceeds (<= 4 CTAs/SM)
+    const int gdx = resident_grid(k_mpnn_bwd_dx, smdx, V.F);
+    const int gdw = resident_grid(k_mpnn_bwd_dw<128>, smdw, V.F);
+    const int gdw0 = resident_grid(k_mpnn_bwd_dw<16>, smdw, V.F);
     const unsigned gadd = (unsigned)((V.F * 16 + 255) / 256);
     for (int l = kMpnnLayers; l >= 1; --l) {
-        k_mpnn_bwd_dx<<<g, NT, smdx, s>>>(V, l);
-        k_mpnn_bwd_dw<128><<<g, NT, smdw, s>>>(V, l, G.partials);
-        k_mpnn_reduce_dw<<<(2 * H * H + H + 255) / 256, 256, 0, s>>>(G.partials, g, 2 * H, G.g + G.off_W[l],
+        k_mpnn_bwd_dx<<<gdx, NT, smdx, s>>>(V, l);
+        k_mpnn_bwd_dw<128><<<gdw, NT, smdw, s>>>(V, l, G.partials);
+        k_mpnn_reduce_dw<<<(2 * H * H + H + 255) / 256, 256, 0, s>>>(G.partials, gdw, 2 * H, G.g + G.off_W[l],
                                                                       G.g + G.off_b[l]);
         k_mpnn_gather_add<<<gadd, 256, 0, s>>>(V);
     }
     k_mpnn_dz0<<<(unsigned)((V.F * (H / 2) + 255) / 256), 256, 0, s>>>(V);
-    k_mpnn_bwd_dw<16><<<g, NT, smdw, s>>>(V, 0, G.partials);
-    k_mpnn_reduce_dw<<<(16 * H + H + 255) / 256, 256, 0, s>>>(G.partials, g, 16, G.g + G.off_W[0], G.g + G.off_b[0]);
+    k_mpnn_bwd_dw<16><<<gdw0, NT, smdw, s>>>(V, 0, G.partials);
+    k_mpnn_reduce_dw<<<(16 * H + H + 255) / 256, 256, 0, s>>>(G.partials, gdw0, 16, G.g + G.off_W[0],
+                                                              G.g + G.off_b[0]);
 }
 
 void mpnn_adam(float* params, const float* grads, float* m1, float* m2, int n, float lr, int t, cudaStream_t s)

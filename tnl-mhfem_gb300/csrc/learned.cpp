@@ -202,6 +202,8 @@ static mhfem_status learned_prepare(mhfem_t h)
     LearnedState* L = h->learned;
     if (L->ready && L->F == h->topo.F) return MHFEM_OK;
     if (h->n != 1) return fail(h, MHFEM_ERR_UNSUPPORTED, "the learned form supports one equation (n = 1)");
+    if (h->pat.W > kMpnnMaxWidth)
+        return fail(h, MHFEM_ERR_UNSUPPORTED, "the learned form takes at most %d neighbours per face", kMpnnMaxWidth);
     const int64_t F = h->topo.F, C = h->topo.C;
     const int nf = h->nf, dim = h->dim;
     // keep options and parameters across re-preparation
@@ -392,6 +394,10 @@ mhfem_status learned_solve(mhfem_t h, int* iters, double* res, mhfem_step_stats*
     in.f_psi = L->f_psi;
     in.src_scale = h->src_amp * std::sin(2.0 * M_PI * h->cur_t / h->src_period);
     in.f_norm = L->f_norm;
+    if (infer) {
+        cudaEventRecord(h->ev[5], s);
+        h->guess_timed = true;
+    }
     if (have_hist) {
         mpnn_scales(F, in, L->fixed, L->scal_partials, L->scal, s);
         LCK(cudaMemcpyAsync(L->host, L->scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -430,6 +436,7 @@ mhfem_status learned_solve(mhfem_t h, int* iters, double* res, mhfem_step_stats*
             used = 1;
         }
     }
+    if (h->guess_timed) cudaEventRecord(h->ev[6], s);
     st = run_fp64(h, h->opts.tol, h->opts.max_iter, iters, res);
     if (st) return st;
     if (training && have_features) {

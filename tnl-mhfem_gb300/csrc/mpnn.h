@@ -13,6 +13,9 @@ namespace mhfem {
 constexpr int kMpnnHidden = 64;
 constexpr int kMpnnFeatures = 16;
 constexpr int kMpnnLayers = 3;
+// Largest neighbour count the network kernels take (triangles: 4, tetrahedra: 6
+// for one equation).
+constexpr int kMpnnMaxWidth = 6;
 // FP32 master parameters: W0 [16][64], b0, W1..W3 [128][64], b1..b3, wd [64], bd
 constexpr int kMpnnParams = kMpnnFeatures * kMpnnHidden + kMpnnHidden
                           + kMpnnLayers * (2 * kMpnnHidden * kMpnnHidden + kMpnnHidden) + kMpnnHidden + 1;

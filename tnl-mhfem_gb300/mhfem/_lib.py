@@ -65,7 +65,7 @@ class StepStats(ct.Structure):
     _fields_ = [("iterations", ct.c_int32), ("sweeps", ct.c_int32), ("residual", ct.c_double),
                 ("guess_used", ct.c_int32), ("guess_residual", ct.c_double), ("warm_residual", ct.c_double),
                 ("ms_pre", ct.c_double), ("ms_assemble", ct.c_double), ("ms_solve", ct.c_double),
-                ("ms_post", ct.c_double)]
+                ("ms_post", ct.c_double), ("ms_guess", ct.c_double)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
