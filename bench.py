@@ -201,7 +201,7 @@ def learned_leg(args, dev, world):
     pl = problems.diffusion3d_source(N=args.grid, steps=total, form=L.FORM_LEARNED)
     pl.config.device = dev
     sl = problems.make_solver(pl, check_every=8)
-    sl.learned_options(train_steps=args.learned_train, train_iters=2, learning_rate=1e-3)
+    sl.learned_options(train_steps=args.learned_train, train_iters=4, learning_rate=3e-3)
     t = 0.0
     t0 = time.perf_counter()
     train_iters = []
@@ -277,7 +277,7 @@ def profile_other_form(args, dev):
     s = problems.make_solver(p, check_every=8)
     t = 0.0
     if args.profile_form == "learned":
-        s.learned_options(train_steps=args.learned_train, train_iters=2)
+        s.learned_options(train_steps=args.learned_train, train_iters=4, learning_rate=3e-3)
         for _ in range(args.learned_train):
             s.step(t, p.dt)
             t += p.dt

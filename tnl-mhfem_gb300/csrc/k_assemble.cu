@@ -18,7 +18,10 @@
 
 namespace mhfem {
 
-template <int NF, int NE>
+// W32: also write the FP32 copy of the values (mixed form).  A template flag,
+// not a run-time test, so that the FP64-only variant carries no conversions
+// (which issue on the scarce FP64 pipe even when predicated off).
+template <int NF, int NE, bool W32>
 __global__ void __launch_bounds__(256) k_assemble(const DevProblem P, const uint32_t* __restrict__ qmap,
                                                   const uint8_t* __restrict__ qdiag, int W,
                                                   double* __restrict__ vals, float* __restrict__ vals32,
@@ -40,12 +43,21 @@ __global__ void __launch_bounds__(256) k_assemble(const DevProblem P, const uint
         const int idx = q * NE + j;
         const int k = idx - (idx > dslot ? 1 : 0);
         vals[(int64_t)k * rows + row] = v;
-        if (vals32) vals32[(int64_t)k * rows + row] = (float)v;
+        if constexpr (W32) vals32[(int64_t)k * rows + row] = (float)v;
     };
-    auto load_rec = [&](int64_t K, int e, double (&A)[RL]) {
-        const double* rec = P.rec + ((K * NF + e) * NE + i) * (int64_t)P.rec_stride;
+    // A record is read by one row only, but the 32-byte sectors it spans are
+    // shared with the neighbouring records of the same cell, which other rows
+    // read a little earlier or later: ordinary caching keeps those sectors in
+    // L2 between the reads.  The stride is even, so records start on 16 bytes.
+    auto rec_ptr = [&](int64_t K, int e) { return P.rec + ((K * NF + e) * NE + i) * (int64_t)P.rec_stride; };
+    auto load_rec = [&](const double* rec, double (&A)[RL]) {
 #pragma unroll
-        for (int q = 0; q < RL; ++q) A[q] = __ldcs(rec + q);
+        for (int q = 0; q + 1 < RL; q += 2) {
+            const double2 v = __ldg(reinterpret_cast<const double2*>(rec + q));
+            A[q] = v.x;
+            A[q + 1] = v.y;
+        }
+        if constexpr (RL % 2) A[RL - 1] = __ldg(rec + RL - 1);
     };
 
     if (kk.y < 0) {
@@ -56,10 +68,13 @@ __global__ void __launch_bounds__(256) k_assemble(const DevProblem P, const uint
             return;
         }
         double A[RL];
-        load_rec(kk.x, e0, A);
-        const double diag = A[i * NF + e0];
+        const double* r0 = rec_ptr(kk.x, e0);
+        load_rec(r0, A);
+        // the entries at run-time positions are re-read from the record (an
+        // L1 hit), which keeps A in registers and costs no FP64 selects
+        const double diag = __ldg(r0 + i * NF + e0);
         if (!(diag > 0)) atomicOr(P.err_flags, 1);
-        const double rd = 1.0 / diag;
+        const double rd = recip_newton(diag);
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
             const int q = (qm >> (4 * f)) & 15u;
@@ -77,11 +92,18 @@ __global__ void __launch_bounds__(256) k_assemble(const DevProblem P, const uint
     }
 
     double A0[RL], A1[RL];
-    load_rec(kk.x, e0, A0);
-    load_rec(kk.y, e1, A1);
-    const double diag = A0[i * NF + e0] + A1[i * NF + e1];
+    const double* r0 = rec_ptr(kk.x, e0);
+    const double* r1 = rec_ptr(kk.y, e1);
+    load_rec(r0, A0);
+    load_rec(r1, A1);
+    // column e1 of the K1 record and the diagonal, re-read from the records
+    // (L1 hits) at their run-time positions
+    double a1e[NE];
+#pragma unroll
+    for (int j = 0; j < NE; ++j) a1e[j] = __ldg(r1 + j * NF + e1);
+    const double diag = __ldg(r0 + i * NF + e0) + __ldg(r1 + i * NF + e1);
     if (!(diag > 0)) atomicOr(P.err_flags, 1);
-    const double rd = 1.0 / diag;
+    const double rd = recip_newton(diag);
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
         const int q = (qm >> (4 * f)) & 15u;
@@ -89,7 +111,7 @@ __global__ void __launch_bounds__(256) k_assemble(const DevProblem P, const uint
         for (int j = 0; j < NE; ++j) {
             if (f == e0) {
                 if (j == i) continue;  // the unit diagonal (LinearSystem.h:196-201)
-                put(q, j, (A0[j * NF + e0] + A1[j * NF + e1]) * rd);
+                put(q, j, (A0[j * NF + f] + a1e[j]) * rd);
             }
             else
                 put(q, j, A0[j * NF + f] * rd);
@@ -110,11 +132,19 @@ int launch_assemble(const DevProblem& P, const AssemblyMap& M, EllMatrix& A, dou
 {
     if (P.rows == 0) return 0;
     const unsigned grid = (unsigned)((P.rows + 255) / 256);
-    float* v32 = write32 ? A.vals32 : nullptr;
-    if (P.nf == 3 && P.n == 1) k_assemble<3, 1><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, v32, rhs);
-    else if (P.nf == 3 && P.n == 2) k_assemble<3, 2><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, v32, rhs);
-    else if (P.nf == 4 && P.n == 1) k_assemble<4, 1><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, v32, rhs);
-    else k_assemble<4, 2><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, v32, rhs);
+    float* v32 = A.vals32;
+    if (write32) {
+        if (P.nf == 3 && P.n == 1) k_assemble<3, 1, true><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, v32, rhs);
+        else if (P.nf == 3 && P.n == 2) k_assemble<3, 2, true><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, v32, rhs);
+        else if (P.nf == 4 && P.n == 1) k_assemble<4, 1, true><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, v32, rhs);
+        else k_assemble<4, 2, true><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, v32, rhs);
+    }
+    else {
+        if (P.nf == 3 && P.n == 1) k_assemble<3, 1, false><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, nullptr, rhs);
+        else if (P.nf == 3 && P.n == 2) k_assemble<3, 2, false><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, nullptr, rhs);
+        else if (P.nf == 4 && P.n == 1) k_assemble<4, 1, false><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, nullptr, rhs);
+        else k_assemble<4, 2, false><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, nullptr, rhs);
+    }
     return 1;
 }
 

@@ -172,7 +172,7 @@ __device__ __forceinline__ void lu_inverse(double (&A)[NF][NF], double scale, do
             for (int q = 0; q < k; ++q) s = fma(-A[k][q], A[q][j], s);
             A[k][j] = s;
         }
-        rp[k] = 1.0 / A[k][k];
+        rp[k] = recip_newton(A[k][k]);
 #pragma unroll
         for (int i = k + 1; i < NF; ++i) {
             double s = A[i][k];
@@ -208,7 +208,7 @@ __device__ __forceinline__ void lu_inverse(double (&A)[NF][NF], double scale, do
 enum { MODE_NO_ADV = 0, MODE_ADV = 1, MODE_CELL_DIRICHLET = 2, MODE_SKIP = 3 };
 
 template <int NF, int NE>
-__global__ void __launch_bounds__(128) k_cell_local(const DevProblem P, const double tau, const double src_scale)
+__global__ void __launch_bounds__(128) k_cell_local(const DevProblem P, const double rtau, const double src_scale)
 {
     constexpr int S = (NF == 3) ? 9 : 14;
     const int64_t K = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(128) k_cell_local(const DevProblem P, const do
     // R_ijKe, R_iK (SecondaryCoefficients.h:50-127)
     double RQ[NE][NE][NF];
     double RK[NE];
-    const double mtau = meas / tau;
+    const double mtau = meas * rtau;
 #pragma unroll
     for (int i = 0; i < NE; ++i) {
 #pragma unroll
@@ -344,17 +344,17 @@ __global__ void __launch_bounds__(128) k_cell_local(const DevProblem P, const do
         }
     }
     if constexpr (NE == 1) {
-        const double rq = 1.0 / Q[0][0];
+        const double rq = recip_newton(Q[0][0]);
         RK[0] *= rq;
 #pragma unroll
         for (int e = 0; e < NF; ++e) RQ[0][0][e] *= rq;
     }
     else {
         // 2x2 Doolittle LU without pivoting
-        const double r0 = 1.0 / Q[0][0];
+        const double r0 = recip_newton(Q[0][0]);
         const double l10 = Q[1][0] * r0;
         const double u11 = fma(-l10, Q[0][1], Q[1][1]);
-        const double r1 = 1.0 / u11;
+        const double r1 = recip_newton(u11);
         auto solve2 = [&](double& x0, double& x1) {
             const double y1 = fma(-l10, x0, x1);
             x1 = y1 * r1;
@@ -570,7 +570,7 @@ int launch_cell_local(const DevProblem& P, double tau, cudaStream_t s)
 {
     if (P.C == 0) return 0;
     const double src_scale = P.src_amp * sin(P.src_omega * P.src_time);
-    MHFEM_DISPATCH(P.nf, P.n, (k_cell_local<NF, NE><<<blocks_for(P.C, 128), 128, 0, s>>>(P, tau, src_scale)));
+    MHFEM_DISPATCH(P.nf, P.n, (k_cell_local<NF, NE><<<blocks_for(P.C, 128), 128, 0, s>>>(P, 1.0 / tau, src_scale)));
     return 1;
 }
 

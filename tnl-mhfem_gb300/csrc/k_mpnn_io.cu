@@ -23,6 +23,9 @@ namespace mhfem {
 
 namespace {
 
+// sz = rms(Zn), sd = rms(Zn - Zn1) over the free rows.  Grid-stride over a
+// fixed grid; the last block to finish sums the per-block partials with all
+// its threads, in a fixed order.
 __global__ void __launch_bounds__(256) k_scales(int64_t F, const double* Zn, const double* Zn1, const uint8_t* fixed,
                                                 double* partials, double* scal, uint32_t* counter)
 {
@@ -35,6 +38,7 @@ __global__ void __launch_bounds__(256) k_scales(int64_t F, const double* Zn, con
         c += 1;
     }
     __shared__ double red[3][256 / 32];
+    __shared__ bool last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -52,24 +56,46 @@ __global__ void __launch_bounds__(256) k_scales(int64_t F, const double* Zn, con
         partials[blockIdx.x * 3 + 2] = n;
         __threadfence();
         const uint32_t prev = atomicAdd(counter, 1u);
-        if (prev == gridDim.x - 1) {
-            double A = 0, B = 0, N = 0;
-            for (unsigned p = 0; p < gridDim.x; ++p) {
-                A += __ldcg(partials + 3 * p);
-                B += __ldcg(partials + 3 * p + 1);
-                N += __ldcg(partials + 3 * p + 2);
-            }
-            N = N > 0 ? N : 1;
-            scal[0] = sqrt(A / N);
-            scal[1] = sqrt(B / N);
-            *counter = 0;
-        }
+        last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    double A = 0, B = 0, N = 0;
+    for (unsigned p = threadIdx.x; p < gridDim.x; p += 256) {
+        A += __ldcg(partials + 3 * p);
+        B += __ldcg(partials + 3 * p + 1);
+        N += __ldcg(partials + 3 * p + 2);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        A += __shfl_down_sync(0xffffffffu, A, o);
+        B += __shfl_down_sync(0xffffffffu, B, o);
+        N += __shfl_down_sync(0xffffffffu, N, o);
+    }
+    __syncthreads();
+    if (lane == 0) { red[0][warp] = A; red[1][warp] = B; red[2][warp] = N; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        A = B = N = 0;
+        for (int w = 0; w < 256 / 32; ++w) { A += red[0][w]; B += red[1][w]; N += red[2][w]; }
+        N = N > 0 ? N : 1;
+        scal[0] = sqrt(A / N);
+        scal[1] = sqrt(B / N);
+        *counter = 0;
     }
 }
 
 __global__ void __launch_bounds__(256) k_features(int64_t F, MpnnInputs in, double rsz, double rsd,
                                                   __nv_bfloat16* x0)
 {
+    // scale of the residual channel, once per block (FP64 division and square
+    // root are scarce on this part)
+    __shared__ float rscale;
+    if (threadIdx.x == 0) {
+        const double rn = in.rnorm->snorm;
+        rscale = rn > 0 ? (float)(sqrt((double)F) / rn) : 0.f;
+    }
+    __syncthreads();
     const int64_t E = (int64_t)blockIdx.x * 256 + threadIdx.x;
     if (E >= F) return;
     float v[16];
@@ -80,8 +106,7 @@ __global__ void __launch_bounds__(256) k_features(int64_t F, MpnnInputs in, doub
     v[1] = (float)((z - in.Zn1[E]) * rsd);
     v[2] = (float)(in.rhs[E] * rsz);
     v[4] = (float)((in.f_base[E] + in.src_scale * in.f_psi[E]) * in.f_norm);
-    const double rn = in.rnorm->snorm;
-    v[12] = rn > 0 ? (float)(in.rbase[E] * (sqrt((double)F) / rn)) : 0.f;
+    v[12] = (float)in.rbase[E] * rscale;
     uint32_t w[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
@@ -128,9 +153,15 @@ static unsigned nb(int64_t n) { return (unsigned)((n + 255) / 256); }
 void mpnn_scales(int64_t F, const MpnnInputs& in, const uint8_t* fixed, double* partials, double* scal,
                  cudaStream_t s)
 {
-    // partials: [grid*3] doubles followed by one uint32 ticket counter (zero-initialized)
-    const int grid = 256;
-    uint32_t* counter = reinterpret_cast<uint32_t*>(partials + grid * 3);
+    // partials: [kScalesMaxGrid*3] doubles followed by one uint32 ticket
+    // counter (zero-initialized); 8 CTAs per SM
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int grid = (sms > 0 ? sms : 152) * 8;
+    if (grid > kScalesMaxGrid) grid = kScalesMaxGrid;
+    if ((int64_t)grid * 256 > F) grid = (int)((F + 255) / 256) > 0 ? (int)((F + 255) / 256) : 1;
+    uint32_t* counter = reinterpret_cast<uint32_t*>(partials + kScalesMaxGrid * 3);
     k_scales<<<grid, 256, 0, s>>>(F, in.Zn, in.Zn1, fixed, partials, scal, counter);
 }
 

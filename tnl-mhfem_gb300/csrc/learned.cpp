@@ -320,8 +320,8 @@ static mhfem_status learned_prepare(mhfem_t h)
     LCK(lalloc(L, &L->dw_partials, (size_t)mpnn_partials_floats(F)));
     LCK(lalloc(L, &L->loss, 1));
     LCK(lalloc(L, &L->scal, 2));
-    LCK(lalloc(L, &L->scal_partials, 256 * 3 + 1));
-    LCK(cudaMemset(L->scal_partials, 0, sizeof(double) * (256 * 3 + 1)));
+    LCK(lalloc(L, &L->scal_partials, kScalesMaxGrid * 3 + 1));
+    LCK(cudaMemset(L->scal_partials, 0, sizeof(double) * (kScalesMaxGrid * 3 + 1)));
     LCK(lalloc(L, &L->Zn, F));
     LCK(lalloc(L, &L->Zn1, F));
     LCK(lalloc(L, &L->base, F));

@@ -32,6 +32,41 @@ struct KrylovScalars {
 // Krylov status codes written to KrylovScalars::status.
 enum : int32_t { KS_RUNNING = 0, KS_CONVERGED = 1, KS_MAXITER = 2, KS_BREAKDOWN = 3, KS_NOTFINITE = 4 };
 
+#ifdef __CUDACC__
+// 1 / d in FP64 for the row scaling of the assembly and the LU pivots of the
+// cell kernel.  GB300 issues FP64 at 1/57 of the FP32 rate and both kernels
+// are bound by their FP64 pipe, where an IEEE FP64 division costs about as
+// much as the rest of a face row.  Newton-Raphson reciprocal iteration
+// (r <- r + r (1 - d r), quadratic convergence) from an FP32 reciprocal
+// estimate: 2^-22 -> 2^-44 -> below FP64 rounding after two steps, i.e.
+// within an ulp or two of the correctly rounded quotient (the GPU parity
+// tests bound the local quantities and the assembled values at 1e-12
+// relative against the oracle's IEEE division).  The FP32 operand and the
+// FP32 estimate move between the two IEEE formats by integer bit operations
+// (sign, rebiased exponent, truncated mantissa), so the FP64 pipe only sees
+// the four fused multiply-adds.  Magnitudes outside [2^-100, 2^100] (and 0,
+// inf, NaN) take the IEEE division.
+static __device__ __noinline__ double recip_ieee(double d) { return 1.0 / d; }
+
+__device__ __forceinline__ double recip_newton(double d)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e < 1023 - 100 || e > 1023 + 100) return recip_ieee(d);
+    const unsigned fb = ((unsigned)(b >> 32) & 0x80000000u) | ((unsigned)(e - 1023 + 127) << 23) |
+                        (unsigned)((b >> 29) & 0x7fffffu);
+    const unsigned rb = __float_as_uint(__frcp_rn(__uint_as_float(fb)));
+    const unsigned long long r64 = ((unsigned long long)(rb & 0x80000000u) << 32) |
+                                   ((unsigned long long)(((rb >> 23) & 0xffu) - 127u + 1023u) << 52) |
+                                   ((unsigned long long)(rb & 0x7fffffu) << 29);
+    double r = __longlong_as_double((long long)r64);
+    double t = fma(-d, r, 1.0);
+    r = fma(r, t, r);
+    t = fma(-d, r, 1.0);
+    return fma(r, t, r);
+}
+#endif
+
 // Device-side view of a problem, passed by value to kernels.
 struct DevProblem {
     int dim, nf, n, S, lumping, advection, mobility_upwind;

@@ -71,7 +71,9 @@ struct MpnnInputs {
     const double* rbase;     // residual b - A (2 Zn - Zn1) of the extrapolated guess
     const KrylovScalars* rnorm;  // its 2-norm in ->snorm (written by the residual kernel)
 };
-// sz = rms(Zn), sd = rms(Zn - Zn1) over free rows -> scal[0], scal[1]
+// sz = rms(Zn), sd = rms(Zn - Zn1) over free rows -> scal[0], scal[1];
+// partials holds kScalesMaxGrid * 3 + 1 doubles, the last word zeroed once
+constexpr int kScalesMaxGrid = 4096;
 void mpnn_scales(int64_t F, const MpnnInputs& in, const uint8_t* fixed, double* partials, double* scal, cudaStream_t s);
 void mpnn_features(int64_t F, const MpnnInputs& in, double sz, double sd, __nv_bfloat16* x0, cudaStream_t s);
 void mpnn_base(int64_t F, const double* Zn, const double* Zn1, double* base, cudaStream_t s);
