@@ -247,6 +247,9 @@ typedef struct {
     double  learning_rate;        /* Adam step size (default 1e-3)                  */
     int32_t use_during_training;  /* 1: also try the guess while still training     */
     uint64_t seed;                /* initial weights (0 keeps the current ones)     */
+    double  lr_final;             /* learning rate at the last training step, as a
+                                     fraction of learning_rate, reached by a cosine
+                                     decay over the training steps (1: constant)     */
 } mhfem_learned_opts;
 
 #define MHFEM_LEARNED_FEATURES 16
@@ -273,7 +276,7 @@ mhfem_status mhfem_learned_status(mhfem_t h, int32_t* trained_steps, double* las
  * cols, vals, rhs and x are DEVICE pointers; x holds the initial guess and
  * receives the solution; stream is a cudaStream_t (NULL: default stream).
  * All work vectors live in one static device array of fixed size (about
- * 12.7 MB, held by every GPU that loads the library until the process
+ * 12.8 MB, held by every GPU that loads the library until the process
  * exits), so systems with more than MHFEM_NOALLOC_MAX_ROWS rows are rejected
  * with MHFEM_ERR_INVALID_ARGUMENT.  The first call on a device looks the
  * array's address up (cudaGetSymbolAddress) and should come before any

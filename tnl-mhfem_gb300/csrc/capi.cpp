@@ -439,7 +439,7 @@ mhfem_status ensure_pattern(mhfem_t h)
         CK(dalloc(h, &Wk.v32, (size_t)rows)); CK(dalloc(h, &Wk.s32, (size_t)rows)); CK(dalloc(h, &Wk.t32, (size_t)rows));
         CK(dalloc(h, &Wk.x32, (size_t)rows));
     }
-    CK(dalloc(h, &Wk.partials, (size_t)Wk.grid * 4));
+    CK(dalloc(h, &Wk.partials, (size_t)Wk.grid * 8));  // 8 partial sums per block at most
     CK(dalloc(h, &Wk.counters, (size_t)4));
     CK(cudaMemset(Wk.counters, 0, sizeof(uint32_t) * 4));
     CK(dalloc(h, &Wk.sc, (size_t)1));

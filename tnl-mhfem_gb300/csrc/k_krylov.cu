@@ -104,10 +104,14 @@ static void launch_pdl(void (*kernel)(KArgs...), cudaStream_t s, Args&&... args)
 // restart threshold of |(rh, r)| relative to ||r|| ||rh|| (same as the oracle)
 constexpr double kRestartEps = 1e-14;
 
+// Per-block partial sums: up to kPartStride values per block.
+constexpr int kPartStride = 8;
+
 template <typename T, int NV>
 __device__ __forceinline__ void block_reduce_store(T (&acc)[NV], double* partials)
 {
-    __shared__ double sh[KB / 32][4];
+    static_assert(NV <= kPartStride, "too many partial sums");
+    __shared__ double sh[KB / 32][kPartStride];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
@@ -122,7 +126,7 @@ __device__ __forceinline__ void block_reduce_store(T (&acc)[NV], double* partial
         for (int q = 0; q < NV; ++q) {
             double s = 0;
             for (int w = 0; w < KB / 32; ++w) s += sh[w][q];
-            partials[(int64_t)blockIdx.x * 4 + q] = s;
+            partials[(int64_t)blockIdx.x * kPartStride + q] = s;
         }
     }
 }
@@ -151,7 +155,7 @@ __device__ __forceinline__ bool ticket_last(uint32_t* counter)
 template <int NV>
 __device__ __forceinline__ void final_sums(const double* partials, double (&out)[NV])
 {
-    __shared__ double sh[KB / 32][4];
+    __shared__ double sh[KB / 32][kPartStride];
     double acc[NV];
 #pragma unroll
     for (int q = 0; q < NV; ++q) acc[q] = 0;
@@ -162,7 +166,7 @@ __device__ __forceinline__ void final_sums(const double* partials, double (&out)
         for (int j = 0; j < 4; ++j) {
             const int b = b0 + j * KB;
 #pragma unroll
-            for (int q = 0; q < NV; ++q) v[j][q] = (b < nb) ? __ldcg(partials + (int64_t)b * 4 + q) : 0.0;
+            for (int q = 0; q < NV; ++q) v[j][q] = (b < nb) ? __ldcg(partials + (int64_t)b * kPartStride + q) : 0.0;
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j)
@@ -620,6 +624,88 @@ void krylov_iterate_fp64(const EllMatrix& A, double* x, KrylovWork& W, int iters
         iterate<double, 2, 1>(A, A.vals, x, W.r, W.rh, W.p, W.v, W.s, W.t, W.sc, W, iters, s);
     else
         iterate<double, 1, 1>(A, A.vals, x, W.r, W.rh, W.p, W.v, W.s, W.t, W.sc, W, iters, s);
+}
+
+// ---- learned form: one pass for the guess inputs --------------------------------
+
+// base = 2 Zn - Zn1 (the extrapolated guess), r_base = b - A base, and the
+// norms the guess needs, in one pass over the matrix: A Zn and A Zn1 are
+// formed row by row (A base = 2 A Zn - A Zn1), so the ELL arrays are read
+// once.  Sums: r_base^2, (b - A Zn)^2, b^2 over all rows; Zn^2,
+// (Zn - Zn1)^2 and the count over the free rows.  The last block writes
+// out[0] = rms(Zn) and out[1] = rms(Zn - Zn1) over the free rows,
+// out[2] = ||r_base||, out[3] = ||b - A Zn|| / ||b|| (the warm start's
+// relative residual) and out[4] = ||b||.
+template <int WW>
+__global__ void __launch_bounds__(KB) k_learned_prep(const int32_t* __restrict__ cols,
+                                                     const double* __restrict__ vals, int W, int64_t rows,
+                                                     const double* __restrict__ b, const double* __restrict__ Zn,
+                                                     const double* __restrict__ Zn1, const uint8_t* __restrict__ fixed,
+                                                     double* __restrict__ base, double* __restrict__ rbase,
+                                                     double* out, double* partials, uint32_t* counter)
+{
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB) {
+        const double z = Zn[q], z1 = Zn1[q], bq = b[q];
+        double yz = z, y1 = z1;
+        if constexpr (WW > 0) {
+            int32_t c[WW];
+            double v[WW];
+#pragma unroll
+            for (int k = 0; k < WW; ++k) {
+                c[k] = __ldg(cols + (int64_t)k * rows + q);
+                v[k] = __ldg(vals + (int64_t)k * rows + q);
+            }
+#pragma unroll
+            for (int k = 0; k < WW; ++k) {
+                yz = fma(v[k], Zn[c[k]], yz);
+                y1 = fma(v[k], Zn1[c[k]], y1);
+            }
+        }
+        else {
+            for (int k = 0; k < W; ++k) {
+                const int64_t o = (int64_t)k * rows + q;
+                const double v = __ldg(vals + o);
+                const int32_t c = __ldg(cols + o);
+                yz = fma(v, Zn[c], yz);
+                y1 = fma(v, Zn1[c], y1);
+            }
+        }
+        base[q] = fma(2.0, z, -z1);
+        const double rb = bq - fma(2.0, yz, -y1), rw = bq - yz;
+        rbase[q] = rb;
+        acc[0] = fma(rb, rb, acc[0]);
+        acc[1] = fma(rw, rw, acc[1]);
+        acc[2] = fma(bq, bq, acc[2]);
+        if (!fixed[q]) {
+            const double d = z - z1;
+            acc[3] = fma(z, z, acc[3]);
+            acc[4] = fma(d, d, acc[4]);
+            acc[5] += 1.0;
+        }
+    }
+    block_reduce_store<double, 6>(acc, partials);
+    if (!ticket_last(counter)) return;
+    double s[6];
+    final_sums<6>(partials, s);
+    if (threadIdx.x == 0) {
+        const double n = s[5] > 0 ? s[5] : 1.0;
+        const double bn = s[2] > 0 ? sqrt(s[2]) : 1.0;
+        out[0] = sqrt(s[3] / n);
+        out[1] = sqrt(s[4] / n);
+        out[2] = sqrt(s[0]);
+        out[3] = sqrt(s[1]) / bn;
+        out[4] = bn;
+    }
+}
+
+void learned_prep_fp64(const EllMatrix& A, const double* b, const double* Zn, const double* Zn1,
+                       const uint8_t* fixed, double* base, double* rbase, double* out, KrylovWork& W,
+                       cudaStream_t s)
+{
+    MHFEM_WIDTH_DISPATCH(A.width, (k_learned_prep<WW><<<occ_grid(k_learned_prep<WW>), KB, 0, s>>>(
+                                      A.cols, A.vals, A.width, A.rows, b, Zn, Zn1, fixed, base, rbase, out,
+                                      W.partials, W.counters)));
 }
 
 // ---- residual of a candidate (learned gate) ------------------------------------

@@ -56,6 +56,14 @@ __device__ __forceinline__ void st_tile(uint8_t* tile, int r, int k0, int K, uin
     *reinterpret_cast<uint4*>(tile + tc::kmajor_offset(r, k0, K)) = v;
 }
 
+// Bulk L2 prefetch of a contiguous range (16-byte aligned start, size a
+// multiple of 16 bytes): the next tile's rows and neighbour indices are on
+// their way to L2 while the current tile is processed.
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(p), "r"(bytes) : "memory");
+}
+
 struct TileSync {
     uint64_t* mbar;
     uint32_t phase;
@@ -106,8 +114,14 @@ constexpr int kOutStride = 2 * H + 16;
 // row-per-thread: thread (r, qs) = (t % 128, t / 128) reads columns
 // 16 qs .. 16 qs + 15 of row r from TMEM (warp % 4 == r / 32 is its TMEM lane
 // quarter) and writes them to the staging tile.
-template <int KIN, bool TRAIN>
-__global__ void __launch_bounds__(NT) k_mpnn_layer(const MpnnView V, int layer)
+// Inference keeps 3 CTAs per SM resident (registers capped at 42; the
+// staging of the three CTAs' tiles overlaps the others' MMA and epilogue);
+// training also stages the pre-activations and fits 2.  DEC (inference, last
+// layer): the decoder runs in the epilogue -- each thread's 16 columns of
+// h4 (as stored in BF16) dotted with wd, the four slices of a row summed in
+// shared memory -- and the guess is written instead of h4.
+template <int KIN, bool TRAIN, bool DEC = false>
+__global__ void __launch_bounds__(NT, TRAIN ? 2 : 3) k_mpnn_layer(const MpnnView V, int layer)
 {
     extern __shared__ __align__(128) uint8_t smem[];
     uint8_t* sA = smem;                            // 128 x KIN (K-major)
@@ -117,9 +131,12 @@ __global__ void __launch_bounds__(NT) k_mpnn_layer(const MpnnView V, int layer)
     __shared__ uint64_t mbar;
     __shared__ uint32_t tbase;
     __shared__ float sbias[H];
+    __shared__ float swd[DEC ? H : 1];
+    __shared__ float sdec[DEC ? 4 : 1][DEC ? TB : 1];
     const int tid = threadIdx.x, warp = tid >> 5;
     const int r = tid & (TB - 1), qs = tid >> 7;  // epilogue mapping
     const int c8 = tid & 7, slot = tid >> 3;      // row-coalesced mapping
+    static_assert(!(DEC && TRAIN), "the fused decoder is an inference path");
     const int64_t F = V.F;
 
     const __nv_bfloat16* Wf = V.w_fwd[layer];  // [64][KIN]
@@ -128,6 +145,8 @@ __global__ void __launch_bounds__(NT) k_mpnn_layer(const MpnnView V, int layer)
         st_tile(sB, rr, k0, KIN, *reinterpret_cast<const uint4*>(Wf + rr * KIN + k0));
     }
     if (tid < H) sbias[tid] = V.bias[layer][tid];
+    if constexpr (DEC)
+        if (tid < H) swd[tid] = V.wd[tid];
     if (warp == 0) {
         tc::tmem_alloc(&tbase, H);
         tc::tmem_relinquish();
@@ -142,6 +161,19 @@ __global__ void __launch_bounds__(NT) k_mpnn_layer(const MpnnView V, int layer)
 
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t row0 = tile * TB;
+        // the next tile of this CTA: its input rows and (hidden layers) its
+        // neighbour index slices; whole 16-byte multiples inside the arrays
+        if (tid == 0 && tile + gridDim.x < ntiles) {
+            const int64_t nr0 = (tile + gridDim.x) * TB;
+            const int64_t nrows = (F - nr0) < TB ? (F - nr0) : TB;
+            prefetch_l2(hin + nr0 * (KIN == 16 ? 16 : H), (uint32_t)(nrows * (KIN == 16 ? 32 : 2 * H)));
+            if constexpr (KIN != 16) {
+                const uint32_t ib = (uint32_t)((nrows * 4) & ~15);
+                if (ib > 0)
+                    for (int k = 0; k < V.W; ++k)
+                        if ((((uint64_t)(V.nbr + (int64_t)k * F + nr0)) & 15) == 0) prefetch_l2(V.nbr + (int64_t)k * F + nr0, ib);
+            }
+        }
         if constexpr (KIN == 16) {
             // 128 rows x 32 bytes: two chunks per row
             if (tid < 2 * TB) {
@@ -232,9 +264,21 @@ __global__ void __launch_bounds__(NT) k_mpnn_layer(const MpnnView V, int layer)
                 zo[t] = pack_bf16(z0, z1);
                 ho[t] = pack_bf16(o0, o1);
             }
-            uint4* so = reinterpret_cast<uint4*>(sO + r * kOutStride + 32 * qs);
-            so[0] = make_uint4(ho[0], ho[1], ho[2], ho[3]);
-            so[1] = make_uint4(ho[4], ho[5], ho[6], ho[7]);
+            if constexpr (DEC) {
+                float part = 0.f;
+#pragma unroll
+                for (int t = 0; t < 8; ++t) {
+                    const float2 hv = unpack_bf16(ho[t]);
+                    part = fmaf(hv.x, swd[16 * qs + 2 * t], part);
+                    part = fmaf(hv.y, swd[16 * qs + 2 * t + 1], part);
+                }
+                sdec[qs][r] = part;
+            }
+            else {
+                uint4* so = reinterpret_cast<uint4*>(sO + r * kOutStride + 32 * qs);
+                so[0] = make_uint4(ho[0], ho[1], ho[2], ho[3]);
+                so[1] = make_uint4(ho[4], ho[5], ho[6], ho[7]);
+            }
             if (TRAIN) {
                 uint4* sz = reinterpret_cast<uint4*>(sZ + r * kOutStride + 32 * qs);
                 sz[0] = make_uint4(zo[0], zo[1], zo[2], zo[3]);
@@ -242,17 +286,26 @@ __global__ void __launch_bounds__(NT) k_mpnn_layer(const MpnnView V, int layer)
             }
         }
         tile_done();
-        // row-coalesced write-out of the staged tile
+        if constexpr (DEC) {
+            if (tid < TB && row0 + tid < F) {
+                const int64_t row = row0 + tid;
+                const float out = sdec[0][tid] + sdec[1][tid] + sdec[2][tid] + sdec[3][tid] + V.bd[0];
+                V.dec_guess[row] = V.fixed[row] ? V.dec_rhs[row] : V.dec_base[row] + V.dec_scal[1] * (double)out;
+            }
+        }
+        else {
+            // row-coalesced write-out of the staged tile
 #pragma unroll
-        for (int j = 0; j < 2; ++j) {
-            const int rr = slot + 64 * j;
-            const int64_t row = row0 + rr;
-            if (row < F) {
-                *reinterpret_cast<uint4*>(hout + row * H + 8 * c8) =
-                    *reinterpret_cast<const uint4*>(sO + rr * kOutStride + 16 * c8);
-                if (TRAIN)
-                    *reinterpret_cast<uint4*>(V.z[layer] + row * H + 8 * c8) =
-                        *reinterpret_cast<const uint4*>(sZ + rr * kOutStride + 16 * c8);
+            for (int j = 0; j < 2; ++j) {
+                const int rr = slot + 64 * j;
+                const int64_t row = row0 + rr;
+                if (row < F) {
+                    *reinterpret_cast<uint4*>(hout + row * H + 8 * c8) =
+                        *reinterpret_cast<const uint4*>(sO + rr * kOutStride + 16 * c8);
+                    if (TRAIN)
+                        *reinterpret_cast<uint4*>(V.z[layer] + row * H + 8 * c8) =
+                            *reinterpret_cast<const uint4*>(sZ + rr * kOutStride + 16 * c8);
+                }
             }
         }
     }
@@ -262,13 +315,9 @@ __global__ void __launch_bounds__(NT) k_mpnn_layer(const MpnnView V, int layer)
 
 // ---- decoder, loss and the start of the backward pass --------------------------
 
-// out = h4 . wd + bd.  Inference: guess = base + sd * out on free rows, the
-// Dirichlet value on fixed rows.  Training: loss, dout, dh4 = dout wd and
-// the decoder gradients.
-template <bool TRAIN>
-__global__ void __launch_bounds__(256) k_mpnn_decode(const MpnnView V, const double* base, double sd,
-                                                     const double* rhs, const double* target, double* guess,
-                                                     double inv_nt)
+// Training decoder: out = h4 . wd + bd, the loss, dout, dh4 = dout wd and
+// the decoder gradients (one partial per block).
+__global__ void __launch_bounds__(256) k_mpnn_decode(const MpnnView V, const double* target, double inv_nt)
 {
     __shared__ float swd[H];
     __shared__ double red[256 / 32][H + 2];
@@ -298,10 +347,6 @@ __global__ void __launch_bounds__(256) k_mpnn_decode(const MpnnView V, const dou
 #pragma unroll
         for (int q = 0; q < H; ++q) out = fmaf(hv[q], swd[q], out);
         const bool fixed = V.fixed[row] != 0;
-        if (!TRAIN) {
-            guess[row] = fixed ? rhs[row] : base[row] + sd * (double)out;
-            continue;
-        }
         const double diff = fixed ? 0.0 : ((double)out - target[row]);
         acc_l += diff * diff;
         const float dout = (float)(2.0 * diff * inv_nt);
@@ -314,7 +359,6 @@ __global__ void __launch_bounds__(256) k_mpnn_decode(const MpnnView V, const dou
             *reinterpret_cast<float4*>(dh + 4 * c) =
                 make_float4(dout * swd[4 * c], dout * swd[4 * c + 1], dout * swd[4 * c + 2], dout * swd[4 * c + 3]);
     }
-    if (!TRAIN) return;
     // block reduction of (dwd[64], dbd, loss) into partials[block][66]
 #pragma unroll
     for (int q = 0; q < H; ++q) {
@@ -445,35 +489,6 @@ __global__ void __launch_bounds__(256) k_mpnn_gather_add(const MpnnView V)
     *reinterpret_cast<float4*>(V.dh + row * H + c) = s;
 }
 
-// Inference decoder: guess = base + sd (h4 . wd + bd) on free rows, the
-// Dirichlet value on fixed rows.  Eight lanes per face, 8 columns (16 bytes)
-// each, so a warp reads four whole 128-byte rows per load.
-__global__ void __launch_bounds__(256) k_mpnn_guess(const MpnnView V, const double* base, double sd,
-                                                    const double* rhs, double* guess)
-{
-    const int l8 = threadIdx.x & 7;
-    float w[8];
-#pragma unroll
-    for (int q = 0; q < 8; ++q) w[q] = V.wd[8 * l8 + q];
-    const float bd = V.bd[0];
-    const __nv_bfloat16* h4 = V.h[kMpnnLayers + 1];
-    const int64_t stride = (int64_t)gridDim.x * (256 / 8);
-    for (int64_t row = ((int64_t)blockIdx.x * 256 + threadIdx.x) >> 3; row < V.F; row += stride) {
-        const uint4 v = __ldg(reinterpret_cast<const uint4*>(h4 + row * H + 8 * l8));
-        const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
-        float o = 0.f;
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            const float2 f = unpack_bf16(w4[t]);
-            o = fmaf(f.x, w[2 * t], o);
-            o = fmaf(f.y, w[2 * t + 1], o);
-        }
-        o += __shfl_xor_sync(0xffffffffu, o, 1);
-        o += __shfl_xor_sync(0xffffffffu, o, 2);
-        o += __shfl_xor_sync(0xffffffffu, o, 4);
-        if (l8 == 0) guess[row] = V.fixed[row] ? rhs[row] : base[row] + sd * (double)(o + bd);
-    }
-}
 
 // dz0 = dh * (z0 > 0) in BF16 (encoder)
 __global__ void __launch_bounds__(256) k_mpnn_dz0(const MpnnView V)
@@ -737,20 +752,23 @@ void mpnn_forward(const MpnnView& V, bool train, cudaStream_t s)
     else forward_layers<false>(V, s);
 }
 
-void mpnn_guess(const MpnnView& V, const double* base, double sd, const double* rhs, double* guess, cudaStream_t s)
+void mpnn_infer_guess(const MpnnView& V, cudaStream_t s)
 {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t blocks = (V.F + 31) / 32;
-    const int64_t cap = (int64_t)(sms > 0 ? sms : 152) * 8;
-    k_mpnn_guess<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(V, base, sd, rhs, guess);
+    const int sm16 = layer_smem(16, false), sm128 = layer_smem(128, false);
+    set_smem(k_mpnn_layer<16, false>, sm16);
+    set_smem(k_mpnn_layer<128, false>, sm128);
+    set_smem(k_mpnn_layer<128, false, true>, sm128);
+    k_mpnn_layer<16, false><<<resident_grid(k_mpnn_layer<16, false>, sm16, V.F), NT, sm16, s>>>(V, 0);
+    const int g = resident_grid(k_mpnn_layer<128, false>, sm128, V.F);
+    for (int l = 1; l < kMpnnLayers; ++l) k_mpnn_layer<128, false><<<g, NT, sm128, s>>>(V, l);
+    k_mpnn_layer<128, false, true><<<resident_grid(k_mpnn_layer<128, false, true>, sm128, V.F), NT, sm128, s>>>(
+        V, kMpnnLayers);
 }
 
 void mpnn_backward(const MpnnView& V, const double* target, double inv_nt, MpnnGrads& G, cudaStream_t s)
 {
     const int gdec = mpnn_grid(V.F);
-    k_mpnn_decode<true><<<gdec, 256, 0, s>>>(V, nullptr, 0.0, nullptr, target, nullptr, inv_nt);
+    k_mpnn_decode<<<gdec, 256, 0, s>>>(V, target, inv_nt);
     k_mpnn_reduce_dec<<<1, 128, 0, s>>>(V.dec_partials, gdec, G.g + G.off_wd, G.g + G.off_bd, G.loss, inv_nt);
     const int smdx = smem_req((TB + 2 * H) * H * 2);
     const int smdw = smem_req((TB + H) * TB * 2);

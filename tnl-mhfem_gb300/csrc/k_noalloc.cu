@@ -10,7 +10,7 @@
 //
 // The Krylov work vectors, the per-CTA partial sums and the device scalars
 // live in one file-scope static device array of fixed size: every GPU that
-// loads the library holds it (about 12.7 MB) until the process exits, and
+// loads the library holds it (about 12.8 MB) until the process exits, and
 // systems with more than MHFEM_NOALLOC_MAX_ROWS rows are rejected.
 #include <mutex>
 
@@ -22,7 +22,7 @@ namespace {
 constexpr int64_t kMaxRows = MHFEM_NOALLOC_MAX_ROWS;
 constexpr int64_t kMaxGrid = 4096;                     // per-CTA partials (>= any Krylov grid here)
 constexpr int64_t kVecDoubles = 6 * kMaxRows;          // r, rh, p, v, s, t
-constexpr int64_t kPartialDoubles = 4 * kMaxGrid;
+constexpr int64_t kPartialDoubles = 8 * kMaxGrid;
 constexpr int64_t kScalarDoubles = (sizeof(mhfem::KrylovScalars) + 7) / 8;
 constexpr int64_t kCounterDoubles = 2;                 // ticket counters (uint32)
 constexpr int64_t kScratchDoubles = kVecDoubles + kPartialDoubles + kScalarDoubles + kCounterDoubles;

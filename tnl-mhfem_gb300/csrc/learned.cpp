@@ -45,8 +45,7 @@ struct LearnedState {
     double* dec_partials = nullptr;
     float* dw_partials = nullptr;
     double* loss = nullptr;
-    double* scal = nullptr;
-    double* scal_partials = nullptr;
+    double* scal = nullptr;  // [8] device: learned_prep_fp64's out[0..4], r_guess, used
     double* Zn = nullptr;
     double* Zn1 = nullptr;
     double* base = nullptr;
@@ -63,6 +62,7 @@ struct LearnedState {
     int train_steps = 200;
     int train_iters = 2;
     float lr = 1e-3f;
+    double lr_final = 1.0;  // fraction of lr at the last training step (cosine decay)
     int use_during_training = 0;
     uint64_t seed = 1234;
     double last_loss = -1;
@@ -319,9 +319,8 @@ static mhfem_status learned_prepare(mhfem_t h)
     LCK(lalloc(L, &L->dec_partials, (size_t)mpnn_grid_size(F) * (H + 2)));
     LCK(lalloc(L, &L->dw_partials, (size_t)mpnn_partials_floats(F)));
     LCK(lalloc(L, &L->loss, 1));
-    LCK(lalloc(L, &L->scal, 2));
-    LCK(lalloc(L, &L->scal_partials, kScalesMaxGrid * 3 + 1));
-    LCK(cudaMemset(L->scal_partials, 0, sizeof(double) * (kScalesMaxGrid * 3 + 1)));
+    LCK(lalloc(L, &L->scal, 8));
+    LCK(cudaMemset(L->scal, 0, sizeof(double) * 8));
     LCK(lalloc(L, &L->Zn, F));
     LCK(lalloc(L, &L->Zn1, F));
     LCK(lalloc(L, &L->base, F));
@@ -360,11 +359,14 @@ static mhfem_status train_once(mhfem_t h, int iters)
     MpnnView V = make_view(h);
     MpnnGrads G = make_grads(h);
     const double inv_nt = L->free_rows > 0 ? 1.0 / (double)L->free_rows : 0.0;
+    // cosine decay from lr to lr * lr_final over the training steps
+    const double prog = L->train_steps > 1 ? (double)L->trained_steps / (double)(L->train_steps - 1) : 1.0;
+    const float lr = (float)(L->lr * (L->lr_final + (1.0 - L->lr_final) * 0.5 * (1.0 + std::cos(M_PI * std::fmin(prog, 1.0)))));
     for (int it = 0; it < iters; ++it) {
         mpnn_forward(V, true, h->stream);
         mpnn_backward(V, L->target, inv_nt, G, h->stream);
         L->adam_t += 1;
-        mpnn_adam(L->params, L->grads, L->m1, L->m2, kMpnnParams, L->lr, L->adam_t, h->stream);
+        mpnn_adam(L->params, L->grads, L->m1, L->m2, kMpnnParams, lr, L->adam_t, h->stream);
         publish(h);
         h->launches += 4 + 2 + 4 * kMpnnLayers + 3 + 1 + 4;
     }
@@ -384,7 +386,6 @@ mhfem_status learned_solve(mhfem_t h, int* iters, double* res, mhfem_step_stats*
     const bool have_hist = L->hist >= 1;
     const bool training = L->trained_steps < L->train_steps;
     const bool infer = have_hist && (!training || L->use_during_training) && L->trained_steps > 0;
-    double sz = 0, sd = 0;
     MpnnInputs in{};
     in.Zn = L->Zn;
     in.Zn1 = L->Zn1;
@@ -394,53 +395,57 @@ mhfem_status learned_solve(mhfem_t h, int* iters, double* res, mhfem_step_stats*
     in.f_psi = L->f_psi;
     in.src_scale = h->src_amp * std::sin(2.0 * M_PI * h->cur_t / h->src_period);
     in.f_norm = L->f_norm;
+    in.rbase = h->W.r;  // the Krylov r vector is idle until the solve
+    in.scal = L->scal;
     if (infer) {
         cudaEventRecord(h->ev[5], s);
         h->guess_timed = true;
     }
+    // Inference runs without a host round trip: the scales stay on the
+    // device and the gate decides there.  Training reads the scales (the
+    // target divides by sd), outside the timed use phase.
+    bool have_features = false;
     if (have_hist) {
-        mpnn_scales(F, in, L->fixed, L->scal_partials, L->scal, s);
-        LCK(cudaMemcpyAsync(L->host, L->scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
-        LCK(cudaStreamSynchronize(s));
-        sz = L->host[0];
-        sd = L->host[1];
+        learned_prep_fp64(h->A, h->rhs, L->Zn, L->Zn1, L->fixed, L->base, h->W.r, L->scal, h->W, s);
         h->launches += 1;
-    }
-    int used = 0;
-    double r_warm = -1, r_guess = -1;
-    const bool have_features = have_hist && sd > 0 && sz > 0;
-    if (have_features) {
-        mpnn_base(F, L->Zn, L->Zn1, L->base, s);
-        // residual of the extrapolated guess (into the Krylov r vector; its norm in W.sc->snorm)
-        mixed_outer_residual(h->A, h->rhs, L->base, h->W, h->opts.tol, 1, s);
-        in.rbase = h->W.r;
-        in.rnorm = h->W.sc;
-        mpnn_features(F, in, sz, sd, L->x0, s);
-        h->launches += 3;
-    }
-    if (infer && have_features) {
-        MpnnView V = make_view(h);
-        mpnn_forward(V, false, s);
-        mpnn_guess(V, L->base, sd, h->rhs, L->guess, s);
-        residual_norm_fp64(h->A, h->rhs, L->Zn, h->W, s);
-        LCK(cudaMemcpyAsync(&L->host[2], &h->W.sc->res, sizeof(double), cudaMemcpyDeviceToHost, s));
-        residual_norm_fp64(h->A, h->rhs, L->guess, h->W, s);
-        LCK(cudaMemcpyAsync(&L->host[3], &h->W.sc->res, sizeof(double), cudaMemcpyDeviceToHost, s));
-        LCK(cudaStreamSynchronize(s));
-        h->launches += (kMpnnLayers + 1) + 1 + 2;
-        if ((st = check_err(h)) != MHFEM_OK) return st;
-        r_warm = L->host[2];
-        r_guess = L->host[3];
-        if (std::isfinite(r_guess) && r_guess < r_warm) {
-            LCK(cudaMemcpyAsync(h->Z_iF, L->guess, sizeof(double) * F, cudaMemcpyDeviceToDevice, s));
-            used = 1;
+        if (training) {
+            LCK(cudaMemcpyAsync(L->host, L->scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+            LCK(cudaStreamSynchronize(s));
+            have_features = L->host[0] > 0 && L->host[1] > 0;
         }
+        else
+            have_features = true;  // zero scales make the features zero; the gate rejects a useless guess
+        if (have_features) {
+            mpnn_features(F, in, L->x0, s);
+            h->launches += 1;
+        }
+    }
+    const bool guessed = infer && have_features;
+    if (guessed) {
+        MpnnView V = make_view(h);
+        V.dec_base = L->base;
+        V.dec_rhs = h->rhs;
+        V.dec_scal = L->scal;
+        V.dec_guess = L->guess;
+        mpnn_infer_guess(V, s);
+        residual_norm_fp64(h->A, h->rhs, L->guess, h->W, s);
+        mpnn_gate(F, L->guess, h->Z_iF, &h->W.sc->res, L->scal, s);
+        h->launches += (kMpnnLayers + 1) + 2;
     }
     if (h->guess_timed) cudaEventRecord(h->ev[6], s);
     st = run_fp64(h, h->opts.tol, h->opts.max_iter, iters, res);
     if (st) return st;
+    int used = 0;
+    double r_warm = -1, r_guess = -1;
+    if (guessed) {
+        LCK(cudaMemcpyAsync(L->host, L->scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        if ((st = check_err(h)) != MHFEM_OK) return st;  // synchronizes the stream
+        r_warm = L->host[3];
+        r_guess = L->host[5];
+        used = L->host[6] != 0.0 ? 1 : 0;
+    }
     if (training && have_features) {
-        mpnn_target(F, h->Z_iF, L->base, sd, L->target, s);
+        mpnn_target(F, h->Z_iF, L->base, L->scal, L->target, s);
         h->launches += 1;
         if ((st = train_once(h, L->train_iters)) != MHFEM_OK) return st;
         LCK(cudaStreamSynchronize(s));
@@ -482,13 +487,15 @@ extern "C" {
 mhfem_status mhfem_learned_set_options(mhfem_t h, const mhfem_learned_opts* o)
 {
     if (!h || !o) return MHFEM_ERR_INVALID_ARGUMENT;
-    if (o->train_steps < 0 || o->train_iters < 1 || !(o->learning_rate > 0))
+    if (o->train_steps < 0 || o->train_iters < 1 || !(o->learning_rate > 0) || !(o->lr_final > 0) ||
+        o->lr_final > 1)
         return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "invalid learned-form options");
     if (!h->learned) h->learned = new LearnedState();
     LearnedState* L = h->learned;
     L->train_steps = o->train_steps;
     L->train_iters = o->train_iters;
     L->lr = (float)o->learning_rate;
+    L->lr_final = o->lr_final;
     L->use_during_training = o->use_during_training;
     if (o->seed != 0 && o->seed != L->seed) {
         L->seed = o->seed;

@@ -132,7 +132,7 @@ struct KrylovWork {
     double *r = nullptr, *rh = nullptr, *p = nullptr, *v = nullptr, *s = nullptr, *t = nullptr;
     float *r32 = nullptr, *rh32 = nullptr, *p32 = nullptr, *v32 = nullptr, *s32 = nullptr,
           *t32 = nullptr, *x32 = nullptr;
-    double* partials = nullptr;      // [grid][4]
+    double* partials = nullptr;      // [grid][8]
     uint32_t* counters = nullptr;    // last-block counters
     KrylovScalars* sc = nullptr;     // device scalars (FP64 solve / outer)
     KrylovScalars* sc32 = nullptr;   // device scalars (inner FP32 solve)
@@ -155,6 +155,13 @@ void residual_norm_fp64(const EllMatrix& A, const double* b, const double* x, Kr
                         cudaStream_t s);
 
 int krylov_grid();
+
+// Learned form, one pass before the network: base = 2 Zn - Zn1, rbase =
+// b - A base, out[0..4] = rms(Zn), rms(Zn - Zn1) (free rows), ||rbase||,
+// ||b - A Zn|| / ||b||, ||b||.
+void learned_prep_fp64(const EllMatrix& A, const double* b, const double* Zn, const double* Zn1,
+                       const uint8_t* fixed, double* base, double* rbase, double* out, KrylovWork& W,
+                       cudaStream_t s);
 
 // One launch of the SpMV + dot kernel on the current Krylov vectors (timing).
 void krylov_spmv_dot_once(const EllMatrix& A, KrylovWork& W, bool fp32, cudaStream_t s);

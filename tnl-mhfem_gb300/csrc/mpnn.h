@@ -40,6 +40,12 @@ struct MpnnView {
     const float* bd = nullptr;        // [1]
     double* dec_partials = nullptr;   // [grid][66]
     int32_t* err = nullptr;
+    // inference: the decoder fused into the last layer writes
+    // guess = base + sd (h4 . wd + bd) on free rows, the Dirichlet value on fixed rows
+    const double* dec_base = nullptr;
+    const double* dec_rhs = nullptr;
+    const double* dec_scal = nullptr;  // device scales, sd = rms(Zn - Zn1) at [1]
+    double* dec_guess = nullptr;
 };
 
 struct MpnnGrads {
@@ -49,9 +55,12 @@ struct MpnnGrads {
     double* loss = nullptr;
 };
 
+// All layers; every hidden state is written (training, and the forward of
+// the C ABI's parity entry point).
 void mpnn_forward(const MpnnView& V, bool train, cudaStream_t s);
-// guess = 2 Zn - Zn1 + sd * out on free rows, rhs on Dirichlet rows
-void mpnn_guess(const MpnnView& V, const double* base, double sd, const double* rhs, double* guess, cudaStream_t s);
+// Inference: layers 0..2, then the last layer with the decoder fused into its
+// epilogue (V.dec_* set); h4 is not stored.
+void mpnn_infer_guess(const MpnnView& V, cudaStream_t s);
 void mpnn_backward(const MpnnView& V, const double* target, double inv_nt, MpnnGrads& G, cudaStream_t s);
 void mpnn_adam(float* params, const float* grads, float* m1, float* m2, int n, float lr, int t, cudaStream_t s);
 void mpnn_publish(const float* W, int K, __nv_bfloat16* wf, __nv_bfloat16* wb, cudaStream_t s);
@@ -69,15 +78,14 @@ struct MpnnInputs {
     double src_scale;        // amplitude * sin(2 pi t / T)
     double f_norm;           // scale of the source channel
     const double* rbase;     // residual b - A (2 Zn - Zn1) of the extrapolated guess
-    const KrylovScalars* rnorm;  // its 2-norm in ->snorm (written by the residual kernel)
+    const double* scal;      // device: rms(Zn), rms(Zn - Zn1) over the free rows, ||rbase||
 };
-// sz = rms(Zn), sd = rms(Zn - Zn1) over free rows -> scal[0], scal[1];
-// partials holds kScalesMaxGrid * 3 + 1 doubles, the last word zeroed once
-constexpr int kScalesMaxGrid = 4096;
-void mpnn_scales(int64_t F, const MpnnInputs& in, const uint8_t* fixed, double* partials, double* scal, cudaStream_t s);
-void mpnn_features(int64_t F, const MpnnInputs& in, double sz, double sd, __nv_bfloat16* x0, cudaStream_t s);
-void mpnn_base(int64_t F, const double* Zn, const double* Zn1, double* base, cudaStream_t s);
-void mpnn_target(int64_t F, const double* Znew, const double* base, double sd, double* y, cudaStream_t s);
+void mpnn_features(int64_t F, const MpnnInputs& in, __nv_bfloat16* x0, cudaStream_t s);
+// training target y = (Znew - base) / sd with sd = scal[1] (device)
+void mpnn_target(int64_t F, const double* Znew, const double* base, const double* scal, double* y, cudaStream_t s);
+// the learned gate: Z = guess if guess's relative residual (*rguess) is finite and
+// below the warm start's (scal[3]); scal[5] = *rguess, scal[6] = 1 if used
+void mpnn_gate(int64_t F, const double* guess, double* Z, const double* rguess, double* scal, cudaStream_t s);
 void mpnn_features_from_host(int64_t F, const float* xf, __nv_bfloat16* x0, cudaStream_t s);
 void mpnn_out(const MpnnView& V, float* out, cudaStream_t s);
 
