@@ -239,6 +239,7 @@ def learned_leg(args, dev, world):
         e1.record(ext)
         e1.synchronize()
         res[name] = {"ms": e0.elapsed_time(e1) / args.steps, "iters": float(np.mean(its)), "used": used,
+                     "its": [int(v) for v in its],
                      "guess_res": float(np.exp(np.mean(np.log(rg)))) if rg else None,
                      "warm_res": float(np.exp(np.mean(np.log(rw)))) if rw else None}
     zl, _ = sl.state()
@@ -253,6 +254,9 @@ def learned_leg(args, dev, world):
                                 "iterations_per_step": res["fp64"]["iters"]},
             "speedup_vs_fp64": res["fp64"]["ms"] / res["learned"]["ms"],
             "iterations_per_step": res["learned"]["iters"],
+            # the guess weakens with the distance from the training window
+            "iterations_first_last_5": [res["learned"]["its"][:5], res["learned"]["its"][-5:]],
+            "fp64_iterations_first_last_5": [res["fp64"]["its"][:5], res["fp64"]["its"][-5:]],
             "guess_accepted_steps": res["learned"]["used"], "timed_steps": args.steps,
             "guess_rel_residual_geomean": res["learned"]["guess_res"],
             "warm_start_rel_residual_geomean": res["learned"]["warm_res"],
