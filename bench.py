@@ -439,11 +439,33 @@ def main():
         err_f = float(np.abs(zfm - zf64).max() / max(np.abs(zf64).max(), 1e-300))
         err_k = float(np.abs(zkm - zk64).max() / max(np.abs(zk64).max(), 1e-300))
         sp32 = sm.time_kernel(L.KERNEL_SPMV_FP32, reps=50)
+        # Single-step accuracy from one common state: the mixed and the FP64
+        # form at the same tolerance, each against the FP64 form solved to
+        # 1e-13.  After many steps the two forms' traces differ by the
+        # tolerance's own error (the "vs_fp64" figures above); this isolates
+        # the precision of the mixed solve from that.
+        pr = problems.diffusion3d(N=args.grid)
+        pr.config.device = dev
+        sr = problems.make_solver(pr, check_every=8)
+        outs = {}
+        for name, tol in (("ref", 1e-13), ("fp64", pr.tol)):
+            sr.setInitialCondition(zkm, zfm)
+            sr.setup(tol=tol, max_iter=20000, check_every=8)
+            sr.step(tm, pr.dt)
+            outs[name] = sr.state()
+        sr.close()
+        sm.step(tm, pm.dt)
+        outs["mixed"] = sm.state()
+        zr, kr = outs["ref"]
+        rel = lambda a, b: float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
         forms["mixed"] = {"value": world * args.steps / (mel / 1e3), "ms_per_step": mel / args.steps,
                           "speedup_vs_fp64": (args.steps / mel) / (args.steps / el_ms),
                           "inner_iterations_per_step": (itm1 - itm0) / args.steps,
                           "sweeps_per_step": statistics.mean(sweeps),
                           "rel_err_face_traces_vs_fp64": err_f, "rel_err_cell_values_vs_fp64": err_k,
+                          "one_step_rel_err_vs_fp64_at_1e-13": {
+                              "mixed": [rel(outs["mixed"][0], zr), rel(outs["mixed"][1], kr)],
+                              "fp64_at_same_tol": [rel(outs["fp64"][0], zr), rel(outs["fp64"][1], kr)]},
                           "spmv_fp32_gbs": sp32["bytes"] / (sp32["ms"] * 1e-3) / 1e9}
         sm.close()
 

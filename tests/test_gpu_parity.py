@@ -6,6 +6,9 @@ cell averages within 1e-10 relative after each time step (both solves run
 to a relative residual of 1e-13 so the comparison measures the path, not the
 solver tolerance).
 """
+import copy
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -120,6 +123,53 @@ def test_diffusion3d_full_size():
     rowptr, cols, _, _ = s.system()
     assert np.array_equal(rowptr, m.rowptr) and np.array_equal(cols, m.cols)
     s.close()
+
+
+def test_adr2d_full_size():
+    """The 512^2 two-component advection-diffusion-reaction workload (n = 2,
+    mass lumping, explicit upwind, inflow / outflow / wall boundaries): 2
+    steps against the oracle."""
+    p = problems.adr2d(N=512, steps=2)
+    s, m = _pair(p, check_every=8)
+    assert s.C == 524288 and s.F == 787456
+    t = 0.0
+    for _ in range(p.steps):
+        s.step(t, p.dt)
+        m.step(t, p.dt, 1e-13)
+        t += p.dt
+    zf, zk = s.state()
+    assert rel_err(zf, m.Z_iF) < TOL_STATE
+    assert rel_err(zk, m.Z_iK) < TOL_STATE
+    rowptr, cols, _, _ = s.system()
+    assert np.array_equal(rowptr, m.rowptr) and np.array_equal(cols, m.cols)
+    s.close()
+
+
+def test_mixed_128_cube():
+    """Mixed precision on the 128^3 cube (12,582,912 tetrahedra, 25,264,128
+    faces), where the CPU oracle is too slow: 2 steps at tol 1e-12, face
+    traces and cell values within 1e-8 of the GPU FP64 form (checked against
+    the oracle at 64^3 above), the final FP64 residual below the tolerance in
+    every step."""
+    p = problems.diffusion3d(N=128, steps=2, form=L.FORM_MIXED)
+    p.tol = 1e-12  # at 1e-10 the two forms already differ by ~1.5e-8 through the tolerance alone
+    sm = problems.make_solver(p, check_every=8)
+    pf = copy.copy(p)
+    pf.config = dataclasses.replace(p.config, form=L.FORM_FP64)
+    sf = problems.make_solver(pf, check_every=8)
+    assert sm.F == 25264128 and sm.C == 12582912
+    t = 0.0
+    for _ in range(p.steps):
+        a = sm.step(t, p.dt)
+        b = sf.step(t, p.dt)
+        assert a["residual"] < p.tol and b["residual"] < p.tol
+        t += p.dt
+    zm, km = sm.state()
+    zf, kf = sf.state()
+    assert rel_err(zm, zf) < 1e-8
+    assert rel_err(km, kf) < 1e-8
+    sm.close()
+    sf.close()
 
 
 def test_mixed_precision_matches_fp64_oracle():
