@@ -344,17 +344,18 @@ __device__ __forceinline__ void spmv_rows(const int32_t* __restrict__ cols, cons
     const int64_t gstride = (int64_t)gridDim.x * KB;                       \
     const int64_t gtid = (int64_t)blockIdx.x * KB + threadIdx.x
 
-// v = A p ; alpha = rho / (rh . v)
+// ---- iteration phases ------------------------------------------------------------
+//
+// Each phase is a grid-stride loop over rows plus, for the reductions, the
+// scalar update that the last CTA applies.  The five iteration kernels below
+// each run one phase; the persistent kernel runs all five with grid barriers.
+
+// v = A p ; acc = (rh, v)
 template <typename T, int WW, int RPT>
-__global__ void __launch_bounds__(KB) k_spmv_dot(const int32_t* cols, const T* vals, int W, int64_t rows,
-                                                 const T* p, const T* rh, T* v,
-                                                 KrylovScalars* sc, double* partials, uint32_t* counter)
+__device__ __forceinline__ void phase_spmv_dot(const int32_t* cols, const T* vals, int W, int64_t rows,
+                                               const T* p, const T* rh, T* v, int64_t gtid, int64_t gstride,
+                                               T (&acc)[1])
 {
-    pdl_wait();
-    pdl_release();
-    if (*(volatile int32_t*)&sc->done) return;
-    MHFEM_GRID_STRIDE;
-    T acc[1] = {0};
     for (int64_t q = gtid; q < rows / RPT; q += gstride) {
         T y[RPT], self[RPT];
         spmv_rows<T, WW, RPT>(cols, vals, W, rows, q, p, y, self);
@@ -366,27 +367,22 @@ __global__ void __launch_bounds__(KB) k_spmv_dot(const int32_t* cols, const T* v
 #pragma unroll
         for (int j = 0; j < RPT; ++j) acc[0] = fma(h.v[j], y[j], acc[0]);
     }
-    block_reduce_store<T, 1>(acc, partials);
-    if (!ticket_last(counter)) return;
-    double s[1];
-    final_sums<1>(partials, s);
-    if (threadIdx.x == 0) {
-        sc->rv = s[0];
-        if (!finite(s[0])) { sc->status = KS_NOTFINITE; sc->done = 1; }
-        else if (s[0] == 0) { sc->status = KS_BREAKDOWN; sc->done = 1; }
-        else sc->alpha = sc->rho / s[0];
-    }
 }
 
-// s = r - alpha v  (||s|| is summed by the next kernel, which reads s anyway)
-template <typename T, int V>
-__global__ void __launch_bounds__(KB) k_update_s(int64_t rows, const T* r, const T* v, T* s, const KrylovScalars* sc)
+// alpha = rho / (rh, v)
+__device__ __forceinline__ void scalars_alpha(KrylovScalars* sc, const double (&s)[1])
 {
-    pdl_wait();
-    pdl_release();
-    if (*(volatile const int32_t*)&sc->done) return;
-    MHFEM_GRID_STRIDE;
-    const T alpha = (T)sc->alpha;
+    sc->rv = s[0];
+    if (!finite(s[0])) { sc->status = KS_NOTFINITE; sc->done = 1; }
+    else if (s[0] == 0) { sc->status = KS_BREAKDOWN; sc->done = 1; }
+    else sc->alpha = sc->rho / s[0];
+}
+
+// s = r - alpha v
+template <typename T, int V>
+__device__ __forceinline__ void phase_update_s(int64_t rows, const T* r, const T* v, T* s, T alpha, int64_t gtid,
+                                               int64_t gstride)
+{
     const int64_t nv = rows / V;
     for (int64_t q = gtid; q < nv; q += gstride) {
         const VecT<T, V> rr = ldv<T, V>(r, q), vv = ldv<T, V>(v, q);
@@ -398,19 +394,11 @@ __global__ void __launch_bounds__(KB) k_update_s(int64_t rows, const T* r, const
     for (int64_t q = nv * V + gtid; q < rows; q += gstride) s[q] = fma(-alpha, v[q], r[q]);
 }
 
-// t = A s ; ||s|| ; omega = (t.s)/(t.t).  When ||s|| already meets the
-// tolerance the iteration ends on the half step (x += alpha p, next kernel)
-// and t is not used: the same decision as checking ||s|| before the SpMV.
+// t = A s ; acc = (t, s), (t, t), (s, s)
 template <typename T, int WW, int RPT>
-__global__ void __launch_bounds__(KB) k_spmv_dots2(const int32_t* cols, const T* vals, int W, int64_t rows,
-                                                   const T* s, T* t,
-                                                   KrylovScalars* sc, double* partials, uint32_t* counter)
+__device__ __forceinline__ void phase_spmv_dots2(const int32_t* cols, const T* vals, int W, int64_t rows,
+                                                 const T* s, T* t, int64_t gtid, int64_t gstride, T (&acc)[3])
 {
-    pdl_wait();
-    pdl_release();
-    if (*(volatile int32_t*)&sc->done) return;
-    MHFEM_GRID_STRIDE;
-    T acc[3] = {0, 0, 0};
     for (int64_t q = gtid; q < rows / RPT; q += gstride) {
         T y[RPT], sv[RPT];
         spmv_rows<T, WW, RPT>(cols, vals, W, rows, q, s, y, sv);
@@ -424,55 +412,51 @@ __global__ void __launch_bounds__(KB) k_spmv_dots2(const int32_t* cols, const T*
         }
         stv<T, RPT>(t, q, yv);
     }
-    block_reduce_store<T, 3>(acc, partials);
-    if (!ticket_last(counter)) return;
-    double sum[3];
-    final_sums<3>(partials, sum);
-    if (threadIdx.x == 0) {
-        sc->snorm = sqrt(sum[2]) / sc->bnorm;
-        sc->half = (sc->snorm < sc->tol) ? 1 : 0;
-        if (sc->half) return;
-        sc->ts = sum[0];
-        sc->tt = sum[1];
-        if (!finite(sum[0]) || !finite(sum[1])) { sc->status = KS_NOTFINITE; sc->done = 1; }
-        else if (sum[1] == 0) { sc->status = KS_BREAKDOWN; sc->done = 1; }
-        else sc->omega = sum[0] / sum[1];
-    }
 }
 
-// x += alpha p + omega s ; r = s - omega t ; rho_new = rh.r ; ||r|| ; beta
-template <typename T, int V>
-__global__ void __launch_bounds__(KB) k_update_xr(int64_t rows, T* x, const T* p, const T* s, const T* t,
-                                                  T* r, const T* rh,
-                                                  KrylovScalars* sc, double* partials, uint32_t* counter)
+// ||s||, the half-step test, omega = (t, s) / (t, t)
+__device__ __forceinline__ void scalars_omega(KrylovScalars* sc, const double (&sum)[3])
 {
-    pdl_wait();
-    pdl_release();
-    if (*(volatile int32_t*)&sc->done) return;
-    MHFEM_GRID_STRIDE;
-    const T alpha = (T)sc->alpha;
+    sc->snorm = sqrt(sum[2]) / sc->bnorm;
+    sc->half = (sc->snorm < sc->tol) ? 1 : 0;
+    if (sc->half) return;
+    sc->ts = sum[0];
+    sc->tt = sum[1];
+    if (!finite(sum[0]) || !finite(sum[1])) { sc->status = KS_NOTFINITE; sc->done = 1; }
+    else if (sum[1] == 0) { sc->status = KS_BREAKDOWN; sc->done = 1; }
+    else sc->omega = sum[0] / sum[1];
+}
+
+// half step: x += alpha p
+template <typename T, int V>
+__device__ __forceinline__ void phase_half(int64_t rows, T* x, const T* p, T alpha, int64_t gtid, int64_t gstride)
+{
     const int64_t nv = rows / V;
-    if (sc->half) {
-        // early exit on the half step: x += alpha p
-        for (int64_t q = gtid; q < nv; q += gstride) {
-            VecT<T, V> xx = ldv<T, V>(x, q);
-            const VecT<T, V> pp = ldv<T, V>(p, q);
+    for (int64_t q = gtid; q < nv; q += gstride) {
+        VecT<T, V> xx = ldv<T, V>(x, q);
+        const VecT<T, V> pp = ldv<T, V>(p, q);
 #pragma unroll
-            for (int j = 0; j < V; ++j) xx.v[j] = fma(alpha, pp.v[j], xx.v[j]);
-            stv<T, V>(x, q, xx);
-        }
-        for (int64_t q = nv * V + gtid; q < rows; q += gstride) x[q] = fma(alpha, p[q], x[q]);
-        if (!ticket_last(counter)) return;
-        if (threadIdx.x == 0) {
-            sc->res = sc->snorm;
-            sc->it += 1;
-            sc->status = KS_CONVERGED;
-            sc->done = 1;
-        }
-        return;
+        for (int j = 0; j < V; ++j) xx.v[j] = fma(alpha, pp.v[j], xx.v[j]);
+        stv<T, V>(x, q, xx);
     }
-    const T omega = (T)sc->omega;
-    T acc[2] = {0, 0};
+    for (int64_t q = nv * V + gtid; q < rows; q += gstride) x[q] = fma(alpha, p[q], x[q]);
+}
+
+__device__ __forceinline__ void scalars_half(KrylovScalars* sc)
+{
+    sc->res = sc->snorm;
+    sc->it += 1;
+    sc->status = KS_CONVERGED;
+    sc->done = 1;
+}
+
+// x += alpha p + omega s ; r = s - omega t ; acc = (rh, r), (r, r)
+template <typename T, int V>
+__device__ __forceinline__ void phase_update_xr(int64_t rows, T* x, const T* p, const T* s, const T* t, T* r,
+                                                const T* rh, T alpha, T omega, int64_t gtid, int64_t gstride,
+                                                T (&acc)[2])
+{
+    const int64_t nv = rows / V;
     for (int64_t q = gtid; q < nv; q += gstride) {
         VecT<T, V> xx = ldv<T, V>(x, q);
         const VecT<T, V> pp = ldv<T, V>(p, q), ss = ldv<T, V>(s, q), tt = ldv<T, V>(t, q), hh = ldv<T, V>(rh, q);
@@ -495,45 +479,39 @@ __global__ void __launch_bounds__(KB) k_update_xr(int64_t rows, T* x, const T* p
         acc[0] = fma(rh[q], rv, acc[0]);
         acc[1] = fma(rv, rv, acc[1]);
     }
-    block_reduce_store<T, 2>(acc, partials);
-    if (!ticket_last(counter)) return;
-    double sum[2];
-    final_sums<2>(partials, sum);
-    if (threadIdx.x == 0) {
-        sc->it += 1;
-        sc->rr = sum[1];
-        sc->res = sqrt(sum[1]) / sc->bnorm;
-        if (!finite(sc->res)) { sc->status = KS_NOTFINITE; sc->done = 1; }
-        else if (sc->res < sc->tol) { sc->status = KS_CONVERGED; sc->done = 1; }
-        else if (sc->it >= sc->max_iter) { sc->status = KS_MAXITER; sc->done = 1; }
-        else if (sc->omega == 0 || sc->rho == 0) { sc->status = KS_BREAKDOWN; sc->done = 1; }
-        else if (fabs(sum[0]) <= kRestartEps * sqrt(sum[1]) * sc->rhnorm) {
-            // shadow residual (numerically) orthogonal to r: restart with rh = p = r
-            sc->restart = 1;
-            sc->beta = 0;
-            sc->rho = sum[1];
-            sc->rhnorm = sqrt(sum[1]);
-        }
-        else {
-            sc->restart = 0;
-            sc->beta = (sum[0] / sc->rho) * (sc->alpha / sc->omega);
-            sc->rho = sum[0];
-        }
+}
+
+// iteration count, convergence, restart test, beta
+__device__ __forceinline__ void scalars_beta(KrylovScalars* sc, const double (&sum)[2])
+{
+    sc->it += 1;
+    sc->rr = sum[1];
+    sc->res = sqrt(sum[1]) / sc->bnorm;
+    if (!finite(sc->res)) { sc->status = KS_NOTFINITE; sc->done = 1; }
+    else if (sc->res < sc->tol) { sc->status = KS_CONVERGED; sc->done = 1; }
+    else if (sc->it >= sc->max_iter) { sc->status = KS_MAXITER; sc->done = 1; }
+    else if (sc->omega == 0 || sc->rho == 0) { sc->status = KS_BREAKDOWN; sc->done = 1; }
+    else if (fabs(sum[0]) <= kRestartEps * sqrt(sum[1]) * sc->rhnorm) {
+        // shadow residual (numerically) orthogonal to r: restart with rh = p = r
+        sc->restart = 1;
+        sc->beta = 0;
+        sc->rho = sum[1];
+        sc->rhnorm = sqrt(sum[1]);
+    }
+    else {
+        sc->restart = 0;
+        sc->beta = (sum[0] / sc->rho) * (sc->alpha / sc->omega);
+        sc->rho = sum[0];
     }
 }
 
 // p = r + beta (p - omega v); on a restart rh = p = r
 template <typename T, int V>
-__global__ void __launch_bounds__(KB) k_update_p(int64_t rows, T* p, const T* r, const T* v, T* rh,
-                                                 const KrylovScalars* sc)
+__device__ __forceinline__ void phase_update_p(int64_t rows, T* p, const T* r, const T* v, T* rh, T beta, T omega,
+                                               bool restart, int64_t gtid, int64_t gstride)
 {
-    pdl_wait();
-    pdl_release();
-    if (*(volatile const int32_t*)&sc->done) return;
-    MHFEM_GRID_STRIDE;
-    const T beta = (T)sc->beta, omega = (T)sc->omega;
     const int64_t nv = rows / V;
-    if (sc->restart) {
+    if (restart) {
         for (int64_t q = gtid; q < nv; q += gstride) {
             const VecT<T, V> rr = ldv<T, V>(r, q);
             stv<T, V>(p, q, rr);
@@ -554,6 +532,92 @@ __global__ void __launch_bounds__(KB) k_update_p(int64_t rows, T* p, const T* r,
         stv<T, V>(p, q, pp);
     }
     for (int64_t q = nv * V + gtid; q < rows; q += gstride) p[q] = fma(beta, fma(-omega, v[q], p[q]), r[q]);
+}
+
+// ---- one kernel per phase ----------------------------------------------------------
+
+template <typename T, int WW, int RPT>
+__global__ void __launch_bounds__(KB) k_spmv_dot(const int32_t* cols, const T* vals, int W, int64_t rows,
+                                                 const T* p, const T* rh, T* v,
+                                                 KrylovScalars* sc, double* partials, uint32_t* counter)
+{
+    pdl_wait();
+    pdl_release();
+    if (*(volatile int32_t*)&sc->done) return;
+    MHFEM_GRID_STRIDE;
+    T acc[1] = {0};
+    phase_spmv_dot<T, WW, RPT>(cols, vals, W, rows, p, rh, v, gtid, gstride, acc);
+    block_reduce_store<T, 1>(acc, partials);
+    if (!ticket_last(counter)) return;
+    double s[1];
+    final_sums<1>(partials, s);
+    if (threadIdx.x == 0) scalars_alpha(sc, s);
+}
+
+template <typename T, int V>
+__global__ void __launch_bounds__(KB) k_update_s(int64_t rows, const T* r, const T* v, T* s, const KrylovScalars* sc)
+{
+    pdl_wait();
+    pdl_release();
+    if (*(volatile const int32_t*)&sc->done) return;
+    MHFEM_GRID_STRIDE;
+    phase_update_s<T, V>(rows, r, v, s, (T)sc->alpha, gtid, gstride);
+}
+
+// The half-step decision (||s|| < tol) is taken here, after the SpMV: the
+// same decision as testing ||s|| before it; t is then unused.
+template <typename T, int WW, int RPT>
+__global__ void __launch_bounds__(KB) k_spmv_dots2(const int32_t* cols, const T* vals, int W, int64_t rows,
+                                                   const T* s, T* t,
+                                                   KrylovScalars* sc, double* partials, uint32_t* counter)
+{
+    pdl_wait();
+    pdl_release();
+    if (*(volatile int32_t*)&sc->done) return;
+    MHFEM_GRID_STRIDE;
+    T acc[3] = {0, 0, 0};
+    phase_spmv_dots2<T, WW, RPT>(cols, vals, W, rows, s, t, gtid, gstride, acc);
+    block_reduce_store<T, 3>(acc, partials);
+    if (!ticket_last(counter)) return;
+    double sum[3];
+    final_sums<3>(partials, sum);
+    if (threadIdx.x == 0) scalars_omega(sc, sum);
+}
+
+template <typename T, int V>
+__global__ void __launch_bounds__(KB) k_update_xr(int64_t rows, T* x, const T* p, const T* s, const T* t,
+                                                  T* r, const T* rh,
+                                                  KrylovScalars* sc, double* partials, uint32_t* counter)
+{
+    pdl_wait();
+    pdl_release();
+    if (*(volatile int32_t*)&sc->done) return;
+    MHFEM_GRID_STRIDE;
+    const T alpha = (T)sc->alpha;
+    if (sc->half) {
+        phase_half<T, V>(rows, x, p, alpha, gtid, gstride);
+        if (!ticket_last(counter)) return;
+        if (threadIdx.x == 0) scalars_half(sc);
+        return;
+    }
+    T acc[2] = {0, 0};
+    phase_update_xr<T, V>(rows, x, p, s, t, r, rh, alpha, (T)sc->omega, gtid, gstride, acc);
+    block_reduce_store<T, 2>(acc, partials);
+    if (!ticket_last(counter)) return;
+    double sum[2];
+    final_sums<2>(partials, sum);
+    if (threadIdx.x == 0) scalars_beta(sc, sum);
+}
+
+template <typename T, int V>
+__global__ void __launch_bounds__(KB) k_update_p(int64_t rows, T* p, const T* r, const T* v, T* rh,
+                                                 const KrylovScalars* sc)
+{
+    pdl_wait();
+    pdl_release();
+    if (*(volatile const int32_t*)&sc->done) return;
+    MHFEM_GRID_STRIDE;
+    phase_update_p<T, V>(rows, p, r, v, rh, (T)sc->beta, (T)sc->omega, sc->restart != 0, gtid, gstride);
 }
 
 // ---- launch shapes ---------------------------------------------------------------
