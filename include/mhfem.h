@@ -91,7 +91,7 @@ typedef struct mhfem_solver_s* mhfem_t;
 
 typedef struct {
     int32_t dim;              /* 2: triangles, 3: tetrahedra (examples/config.h:17-21) */
-    int32_t n_eq;             /* NumberOfEquations, 1 or 2 */
+    int32_t n_eq;             /* NumberOfEquations, 1 to 3 */
     int32_t mass_lumping;     /* MassLumping::enabled = 1 (MassMatrix.h:16-19) */
     int32_t advection;        /* MHFEM_*_UPWIND / MHFEM_IMPLICIT_TRACE */
     int32_t mobility_upwind;  /* Model::do_mobility_upwind (BaseModel.h:160-161) */

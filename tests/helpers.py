@@ -6,7 +6,7 @@ import copy
 import numpy as np
 
 from mhfem import _lib as L
-from mhfem import problems
+from mhfem import meshgen, problems
 
 
 def rel_err(a, b) -> float:
@@ -69,4 +69,70 @@ def small_cases():
     q.bc_fn = bc2
     q.Z0 = rng.uniform(0, 1, 2 * C)
     cases["diffusion3d_n2"] = q
+    cases.update(three_component_cases())
+    return cases
+
+
+def three_component_cases():
+    """n = 3: tetrahedra with coupled diffusion, reaction and a w field; triangles
+    with advection on every component (implicit upwind) and coupled reaction."""
+    cases = {}
+    n = 3
+    p = problems.diffusion3d(N=3, steps=2)
+    C = p.C
+    rng = np.random.default_rng(13)
+    Nc = np.zeros((n, n, C))
+    D = np.zeros((n, n, C))
+    for i in range(n):
+        Nc[i, i] = 1.0 + i
+        D[i, i] = (1.0, 0.5, 2.0)[i] * p.coeffs["D"]
+    D[0, 1] = 0.1
+    D[1, 2] = 0.05
+    r = np.zeros((n, n, C))
+    r[0, 0], r[1, 1], r[2, 2] = 0.3, 0.2, 0.25
+    r[0, 1] = r[1, 0] = -0.05
+    r[1, 2] = r[2, 1] = -0.04
+    w = rng.uniform(-0.01, 0.01, (n, 4, C))
+    base_bc = p.bc_fn
+
+    def bc3(fv, fc):
+        t, v, d = base_bc(fv, fc)
+        return (np.concatenate([t] * n), np.concatenate([v, v + 0.1 * (t == 1), v]),
+                np.concatenate([d + 0.2, d, d + 0.1]))
+
+    q = variant(p, n_eq=n, coeffs={"N": Nc.ravel(), "D": D.ravel(), "r": r.ravel(), "w": w.ravel(), "f": 0.5})
+    q.bc_fn = bc3
+    q.Z0 = rng.uniform(0, 1, n * C)
+    cases["diffusion3d_n3"] = q
+
+    p = problems.adr2d(N=6, steps=2)
+    C = p.C
+    nf = 3
+    D2 = np.asarray(p.coeffs["D"]).reshape(2, 2, C)
+    normals = meshgen.outward_face_normals(p.coords, p.cells)
+    flux = np.einsum("cfd,d->fc", normals, np.array([1.0, 0.3]))
+    Nc = np.zeros((n, n, C))
+    D = np.zeros((n, n, C))
+    a = np.zeros((n, n, nf, C))
+    for i in range(n):
+        Nc[i, i] = 1.0
+        D[i, i] = D2[0, 0] * (1.0, 0.5, 0.8)[i]
+        a[i, i] = flux * (1.0, 0.7, 1.2)[i]
+    r = np.zeros((n, n, C))
+    r[0, 0], r[1, 1], r[2, 2] = 0.1, 0.1, 0.15
+    r[0, 1] = r[1, 0] = -0.05
+    r[1, 2] = r[2, 1] = -0.03
+    base_bc2 = p.bc_fn
+
+    def bc_adr3(fv, fc):
+        t, v, d = base_bc2(fv, fc)
+        F = fc.shape[0]
+        t0, d0 = t[:F], d[:F]
+        return np.concatenate([t0] * n), np.zeros(n * F), np.concatenate([d0, 0.5 * d0, 0 * d0])
+
+    q = variant(p, n_eq=n, advection=L.IMPLICIT_UPWIND,
+                coeffs={"N": Nc.ravel(), "D": D.ravel(), "a": a.ravel(), "r": r.ravel()})
+    q.bc_fn = bc_adr3
+    q.Z0 = np.zeros(n * C)
+    cases["adr2d_n3_implicit_upwind"] = q
     return cases

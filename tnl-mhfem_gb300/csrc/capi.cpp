@@ -135,7 +135,7 @@ mhfem_status mhfem_create(const mhfem_desc* desc, mhfem_t* out)
     if (!desc || !out) return MHFEM_ERR_INVALID_ARGUMENT;
     *out = nullptr;
     if (desc->dim != 2 && desc->dim != 3) return MHFEM_ERR_INVALID_ARGUMENT;
-    if (desc->n_eq < 1 || desc->n_eq > 2) return MHFEM_ERR_UNSUPPORTED;
+    if (desc->n_eq < 1 || desc->n_eq > 3) return MHFEM_ERR_UNSUPPORTED;
     if (desc->advection < 0 || desc->advection > 2) return MHFEM_ERR_INVALID_ARGUMENT;
     if (desc->form < 0 || desc->form > 2) return MHFEM_ERR_INVALID_ARGUMENT;
     int ndev = 0;

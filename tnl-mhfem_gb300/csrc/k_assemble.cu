@@ -132,19 +132,18 @@ int launch_assemble(const DevProblem& P, const AssemblyMap& M, EllMatrix& A, dou
 {
     if (P.rows == 0) return 0;
     const unsigned grid = (unsigned)((P.rows + 255) / 256);
-    float* v32 = A.vals32;
-    if (write32) {
-        if (P.nf == 3 && P.n == 1) k_assemble<3, 1, true><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, v32, rhs);
-        else if (P.nf == 3 && P.n == 2) k_assemble<3, 2, true><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, v32, rhs);
-        else if (P.nf == 4 && P.n == 1) k_assemble<4, 1, true><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, v32, rhs);
-        else k_assemble<4, 2, true><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, v32, rhs);
-    }
-    else {
-        if (P.nf == 3 && P.n == 1) k_assemble<3, 1, false><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, nullptr, rhs);
-        else if (P.nf == 3 && P.n == 2) k_assemble<3, 2, false><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, nullptr, rhs);
-        else if (P.nf == 4 && P.n == 1) k_assemble<4, 1, false><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, nullptr, rhs);
-        else k_assemble<4, 2, false><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, nullptr, rhs);
-    }
+#define MHFEM_ASSEMBLE(W32, V32)                                                                          \
+    do {                                                                                                  \
+        if (P.nf == 3 && P.n == 1) k_assemble<3, 1, W32><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, V32, rhs); \
+        else if (P.nf == 3 && P.n == 2) k_assemble<3, 2, W32><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, V32, rhs); \
+        else if (P.nf == 3) k_assemble<3, 3, W32><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, V32, rhs); \
+        else if (P.n == 1) k_assemble<4, 1, W32><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, V32, rhs); \
+        else if (P.n == 2) k_assemble<4, 2, W32><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, V32, rhs); \
+        else k_assemble<4, 3, W32><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, V32, rhs); \
+    } while (0)
+    if (write32) MHFEM_ASSEMBLE(true, A.vals32);
+    else MHFEM_ASSEMBLE(false, nullptr);
+#undef MHFEM_ASSEMBLE
     return 1;
 }
 

@@ -350,21 +350,49 @@ __global__ void __launch_bounds__(128) k_cell_local(const DevProblem P, const do
         for (int e = 0; e < NF; ++e) RQ[0][0][e] *= rq;
     }
     else {
-        // 2x2 Doolittle LU without pivoting
-        const double r0 = recip_newton(Q[0][0]);
-        const double l10 = Q[1][0] * r0;
-        const double u11 = fma(-l10, Q[0][1], Q[1][1]);
-        const double r1 = recip_newton(u11);
-        auto solve2 = [&](double& x0, double& x1) {
-            const double y1 = fma(-l10, x0, x1);
-            x1 = y1 * r1;
-            x0 = fma(-Q[0][1], x1, x0) * r0;
+        // Doolittle LU without pivoting, in place (U on and above the
+        // diagonal, L below), one reciprocal per pivot
+        double rp[NE];
+#pragma unroll
+        for (int k = 0; k < NE; ++k) {
+#pragma unroll
+            for (int j = k; j < NE; ++j) {
+                double u = Q[k][j];
+#pragma unroll
+                for (int q = 0; q < k; ++q) u = fma(-Q[k][q], Q[q][j], u);
+                Q[k][j] = u;
+            }
+            rp[k] = recip_newton(Q[k][k]);
+#pragma unroll
+            for (int i = k + 1; i < NE; ++i) {
+                double l = Q[i][k];
+#pragma unroll
+                for (int q = 0; q < k; ++q) l = fma(-Q[i][q], Q[q][k], l);
+                Q[i][k] = l * rp[k];
+            }
+        }
+        // x <- Q^-1 x for the NE components x[i] = X(i)
+        auto solve = [&](auto&& X) {
+#pragma unroll
+            for (int i = 1; i < NE; ++i) {
+                double y = X(i);
+#pragma unroll
+                for (int q = 0; q < i; ++q) y = fma(-Q[i][q], X(q), y);
+                X(i) = y;
+            }
+#pragma unroll
+            for (int i = NE - 1; i >= 0; --i) {
+                double x = X(i);
+#pragma unroll
+                for (int q = i + 1; q < NE; ++q) x = fma(-Q[i][q], X(q), x);
+                X(i) = x * rp[i];
+            }
         };
-        solve2(RK[0], RK[1]);
+        solve([&](int i) -> double& { return RK[i]; });
 #pragma unroll
         for (int j = 0; j < NE; ++j)
 #pragma unroll
-            for (int e = 0; e < NF; ++e) solve2(RQ[0][j][e], RQ[1][j][e]);
+            for (int e = 0; e < NF; ++e) solve([&](int i) -> double& { return RQ[i][j][e]; });
     }
 
 #pragma unroll
@@ -560,8 +588,10 @@ __global__ void k_face_average(const DevProblem P)
     do {                                                                  \
         if ((NFV) == 3 && (NEV) == 1) { constexpr int NF = 3, NE = 1; CALL; } \
         else if ((NFV) == 3 && (NEV) == 2) { constexpr int NF = 3, NE = 2; CALL; } \
+        else if ((NFV) == 3 && (NEV) == 3) { constexpr int NF = 3, NE = 3; CALL; } \
         else if ((NFV) == 4 && (NEV) == 1) { constexpr int NF = 4, NE = 1; CALL; } \
-        else { constexpr int NF = 4, NE = 2; CALL; }                      \
+        else if ((NFV) == 4 && (NEV) == 2) { constexpr int NF = 4, NE = 2; CALL; } \
+        else { constexpr int NF = 4, NE = 3; CALL; }                      \
     } while (0)
 
 static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }
@@ -592,7 +622,8 @@ int launch_face_average(const DevProblem& P, cudaStream_t s)
 {
     if (P.F == 0) return 0;
     if (P.n == 1) k_face_average<1><<<blocks_for(P.F, 256), 256, 0, s>>>(P);
-    else k_face_average<2><<<blocks_for(P.F, 256), 256, 0, s>>>(P);
+    else if (P.n == 2) k_face_average<2><<<blocks_for(P.F, 256), 256, 0, s>>>(P);
+    else k_face_average<3><<<blocks_for(P.F, 256), 256, 0, s>>>(P);
     return 1;
 }
 
