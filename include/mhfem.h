@@ -97,7 +97,13 @@ typedef struct {
     int32_t mobility_upwind;  /* Model::do_mobility_upwind (BaseModel.h:160-161) */
     int32_t form;             /* MHFEM_FORM_* */
     int32_t device;           /* CUDA device ordinal */
+    int32_t cell;             /* MHFEM_CELL_SIMPLEX (triangles, tetrahedra) or MHFEM_CELL_BOX
+                                 (rectangles, cuboids: the Quadrangle / Hexahedron topologies of
+                                 examples/config.h:13-21, axis-aligned as MassMatrix.h:152-508 assumes) */
 } mhfem_desc;
+
+#define MHFEM_CELL_SIMPLEX 0
+#define MHFEM_CELL_BOX     1
 
 typedef struct {
     double  tol;              /* convergence-residue: relative residual ||b-Ax||/||b|| */

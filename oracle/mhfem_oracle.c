@@ -29,7 +29,7 @@
 #endif
 
 #define MAXN 4   /* max equations supported by the oracle */
-#define MAXF 4   /* max faces per cell (tetrahedron) */
+#define MAXF 6   /* max faces per cell (cuboid) */
 
 void orc_set_threads(int n)
 {
@@ -70,7 +70,7 @@ static inline double m_upw_get(const orc_problem* p, int i, int64_t E)
 /* ------------------------------------------------------------------ */
 /* Topology (TNL mesh initializer semantics, restated; mesh_helpers.h:49-265) */
 
-typedef struct { int32_t v[3]; int64_t slot; } face_seed;
+typedef struct { int32_t v[4]; int64_t slot; } face_seed;
 
 static int seed_cmp(const void* A, const void* B)
 {
@@ -89,21 +89,39 @@ static int i64_cmp(const void* A, const void* B)
     return (a < b) ? -1 : (a > b);
 }
 
+/* local vertices of the faces of a box cell (see the header) */
+static const int kRectFaces[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
+static const int kCuboidFaces[6][4] = {{0, 1, 2, 3}, {0, 1, 5, 4}, {1, 2, 6, 5},
+                                       {2, 3, 7, 6}, {3, 0, 4, 7}, {4, 5, 6, 7}};
+
 int64_t orc_build_faces(int dim, int64_t C, const int32_t* cell_verts,
                         int32_t* cell_faces, int32_t* face_cells, int32_t* face_verts)
 {
-    const int nf = dim + 1;
+    return orc_build_faces_ct(dim, 0, C, cell_verts, cell_faces, face_cells, face_verts);
+}
+
+int64_t orc_build_faces_ct(int dim, int cell, int64_t C, const int32_t* cell_verts,
+                           int32_t* cell_faces, int32_t* face_cells, int32_t* face_verts)
+{
+    const int nf = cell ? 2 * dim : dim + 1;
+    const int nv = cell ? (1 << dim) : dim + 1;
+    const int fv = cell ? (1 << (dim - 1)) : dim;
     const int64_t total = C * nf;
     face_seed* seeds = (face_seed*)malloc(sizeof(face_seed) * (size_t)total);
     for (int64_t K = 0; K < C; ++K)
         for (int e = 0; e < nf; ++e) {
             face_seed s;
             int c = 0;
-            for (int v = 0; v < nf; ++v)
-                if (v != e) s.v[c++] = cell_verts[K * nf + v];
-            for (; c < 3; ++c) s.v[c] = -1;
-            /* sort the dim vertex ids (insertion sort) */
-            for (int x = 1; x < dim; ++x)
+            if (!cell) {
+                for (int v = 0; v < nv; ++v)
+                    if (v != e) s.v[c++] = cell_verts[K * nv + v];
+            }
+            else
+                for (int v = 0; v < fv; ++v)
+                    s.v[c++] = cell_verts[K * nv + (dim == 2 ? kRectFaces[e][v] : kCuboidFaces[e][v])];
+            for (; c < 4; ++c) s.v[c] = -1;
+            /* sort the fv vertex ids (insertion sort) */
+            for (int x = 1; x < fv; ++x)
                 for (int y = x; y > 0 && s.v[y - 1] > s.v[y]; --y) {
                     int32_t tmp = s.v[y]; s.v[y] = s.v[y - 1]; s.v[y - 1] = tmp;
                 }
@@ -135,7 +153,7 @@ int64_t orc_build_faces(int dim, int64_t C, const int32_t* cell_verts,
                 if (nc < 2) face_cells[2 * E + nc] = (int32_t)(slot / nf);
                 ++nc;
             }
-            for (int d = 0; d < dim; ++d) face_verts[(int64_t)E * dim + d] = seeds[g0].v[d];
+            for (int d = 0; d < fv; ++d) face_verts[(int64_t)E * fv + d] = seeds[g0].v[d];
             g0 = k;
         }
     }
@@ -180,18 +198,50 @@ static double simplex_measure(const double* const* P, int k, int dim)
     return fabs(det) / 6.0;
 }
 
+/* side lengths h_x, h_y (, h_z) of a box cell: the lowest corner v0 to the
+ * opposite corner (v2 of a rectangle, v6 of a cuboid), MassMatrix.h:178-184,
+ * 346-353 */
+static void box_sides(const orc_problem* p, int64_t K, double* h)
+{
+    const double* v0 = p->coords + (int64_t)p->cell_verts[K * p->nv] * p->dim;
+    const double* vd = p->coords + (int64_t)p->cell_verts[K * p->nv + (p->dim == 2 ? 2 : 6)] * p->dim;
+    for (int d = 0; d < p->dim; ++d) h[d] = vd[d] - v0[d];
+}
+
 double orc_cell_measure(const orc_problem* p, int64_t K)
 {
+    if (p->cell) {
+        double h[3];
+        box_sides(p, K, h);
+        double m = 1;
+        for (int d = 0; d < p->dim; ++d) m *= h[d];
+        return fabs(m);
+    }
     const double* P[4];
-    for (int v = 0; v < p->nf; ++v) P[v] = p->coords + (int64_t)p->cell_verts[K * p->nf + v] * p->dim;
+    for (int v = 0; v < p->nv; ++v) P[v] = p->coords + (int64_t)p->cell_verts[K * p->nv + v] * p->dim;
     return simplex_measure(P, p->dim, p->dim);
 }
 
 double orc_face_measure(const orc_problem* p, int64_t E, const int32_t* face_verts)
 {
+    if (p->cell && p->dim == 3) {
+        /* an axis-aligned rectangle: the product of its two nonzero extents */
+        double lo[3], hi[3];
+        for (int d = 0; d < 3; ++d) { lo[d] = 1e300; hi[d] = -1e300; }
+        for (int v = 0; v < 4; ++v) {
+            const double* X = p->coords + (int64_t)face_verts[E * 4 + v] * 3;
+            for (int d = 0; d < 3; ++d) { lo[d] = fmin(lo[d], X[d]); hi[d] = fmax(hi[d], X[d]); }
+        }
+        double ext[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+        int dmin = 0;
+        for (int d = 1; d < 3; ++d) if (ext[d] < ext[dmin]) dmin = d;
+        double m = 1;
+        for (int d = 0; d < 3; ++d) if (d != dmin) m *= ext[d];
+        return m;
+    }
     const double* P[3];
-    for (int v = 0; v < p->dim; ++v) P[v] = p->coords + (int64_t)face_verts[E * p->dim + v] * p->dim;
-    return simplex_measure(P, p->dim - 1, p->dim);
+    for (int v = 0; v < p->fv; ++v) P[v] = p->coords + (int64_t)face_verts[E * p->fv + v] * p->dim;
+    return simplex_measure(P, p->fv - 1, p->dim);
 }
 
 /* ------------------------------------------------------------------ */
@@ -235,7 +285,7 @@ static void mass_matrix_local(const orc_problem* p, int64_t K, double* M /* nf x
 {
     const int dim = p->dim;
     const double* X[4];
-    for (int v = 0; v < p->nf; ++v) X[v] = p->coords + (int64_t)p->cell_verts[K * p->nf + v] * dim;
+    for (int v = 0; v < p->nv; ++v) X[v] = p->coords + (int64_t)p->cell_verts[K * p->nv + v] * dim;
     const double meas = orc_cell_measure(p, K);
     if (dim == 2 && !p->lumping) {
         /* MassMatrix.h:538-569 */
@@ -304,9 +354,42 @@ static void mass_matrix_local(const orc_problem* p, int64_t K, double* M /* nf x
         for (int j = 0; j < i; ++j) M[i * nf + j] = M[j * nf + i];
 }
 
+/* orientation class of local face e of a box cell, the storage slot s of
+ * its value: rectangle e % 2 (horizontal 0, 2 -> 0; vertical 1, 3 -> 1),
+ * cuboid n_x (2, 4) -> 0, n_y (1, 3) -> 1, n_z (0, 5) -> 2
+ * (MassMatrix.h:216-227, 392-403) */
+static inline int box_class(int dim, int e)
+{
+    if (dim == 2) return e % 2;
+    return (e == 2 || e == 4) ? 0 : (e == 1 || e == 3) ? 1 : 2;
+}
+
 void orc_update_b(orc_problem* p)
 {
     const int nf = p->nf, n = p->n, S = p->S;
+    if (p->cell) {
+        /* MassMatrix::update for rectangles (MassMatrix.h:171-186, 249-264) and
+         * cuboids (340-362, 424-446): the same values with and without lumping */
+#pragma omp parallel for schedule(static)
+        for (int64_t K = 0; K < p->C; ++K) {
+            double h[3];
+            box_sides(p, K, h);
+            for (int i = 0; i < n; ++i)
+                for (int j = 0; j < n; ++j) {
+                    const double D = cget(p->D, IDX_ijK(p, i, j, K));
+                    if (p->dim == 2) {
+                        p->b[IDX_ijsK(p, i, j, 0, K)] = 2 * D * h[0] / h[1];
+                        p->b[IDX_ijsK(p, i, j, 1, K)] = 2 * D * h[1] / h[0];
+                    }
+                    else {
+                        p->b[IDX_ijsK(p, i, j, 0, K)] = 2 * D * h[1] * h[2] / h[0];
+                        p->b[IDX_ijsK(p, i, j, 1, K)] = 2 * D * h[0] * h[2] / h[1];
+                        p->b[IDX_ijsK(p, i, j, 2, K)] = 2 * D * h[0] * h[1] / h[2];
+                    }
+                }
+        }
+        return;
+    }
 #pragma omp parallel for schedule(static)
     for (int64_t K = 0; K < p->C; ++K) {
         double M[MAXF * MAXF];
@@ -317,7 +400,7 @@ void orc_update_b(orc_problem* p)
                 const double D = cget(p->D, IDX_ijK(p, i, j, K));
                 /* packed upper triangle, column by column (MassMatrix.h:571-592) */
                 for (int col = 0; col < nf; ++col) {
-                    double v[MAXF] = {0, 0, 0, 0};
+                    double v[MAXF] = {0, 0, 0, 0, 0, 0};
                     v[col] = 1.0;
                     lu_solve(M, nf, v);
                     for (int row = 0; row <= col; ++row)
@@ -336,15 +419,29 @@ void orc_update_b(orc_problem* p)
     }
 }
 
-/* MassMatrix::b_ijKef / b_ijKe (MassMatrix.h:600-631) */
+/* MassMatrix::b_ijKef / b_ijKe: simplices MassMatrix.h:600-631; boxes
+ * 188-227 (rectangle, lumped: diagonal), 268-319 (rectangle: 2s on the
+ * diagonal, s between the two faces of one orientation, row sum 3s),
+ * 364-403 and 448-507 (cuboid, the same with three orientations) */
 static inline double b_ef(const orc_problem* p, int i, int j, int64_t K, int e, int f)
 {
+    if (p->cell) {
+        const int ce = box_class(p->dim, e), cf = box_class(p->dim, f);
+        if (p->lumping) return e == f ? p->b[IDX_ijsK(p, i, j, ce, K)] : 0.0;
+        if (ce != cf) return 0.0;
+        const double s = p->b[IDX_ijsK(p, i, j, ce, K)];
+        return e == f ? 2 * s : s;
+    }
     if (e > f) { int t = e; e = f; f = t; }
     return p->b[IDX_ijsK(p, i, j, e + f * (f + 1) / 2, K)];
 }
 
 static inline double b_e(const orc_problem* p, int i, int j, int64_t K, int e)
 {
+    if (p->cell) {
+        const double s = p->b[IDX_ijsK(p, i, j, box_class(p->dim, e), K)];
+        return p->lumping ? s : 3 * s;
+    }
     return p->b[IDX_ijsK(p, i, j, p->S - p->nf + e, K)];
 }
 

@@ -34,10 +34,13 @@ typedef struct {
 
 typedef struct {
     /* static configuration (examples/config.h) */
-    int dim;            /* 2 = triangles, 3 = tetrahedra */
-    int nf;             /* faces per cell = dim + 1 */
+    int dim;            /* 2 or 3 */
+    int cell;           /* 0: simplices (triangles, tetrahedra); 1: boxes (rectangles, cuboids) */
+    int nf;             /* faces per cell: dim + 1 (simplex), 2 dim (box) */
+    int nv;             /* vertices per cell: dim + 1 (simplex), 2^dim (box) */
+    int fv;             /* vertices per face: dim (simplex), 2^(dim-1) (box) */
     int n;              /* number of equations */
-    int S;              /* MassMatrix::size: 9 (triangle) or 14 (tetrahedron) */
+    int S;              /* MassMatrix::size: 9 (triangle), 14 (tetrahedron), 2 (rectangle), 3 (cuboid) */
     int lumping;        /* MassLumping::enabled = 1 */
     int advection;      /* 0 explicit_upwind, 1 implicit_upwind, 2 implicit_trace */
     int mobility_upwind;/* Model::do_mobility_upwind */
@@ -77,10 +80,19 @@ typedef struct {
 } orc_problem;
 
 /* Topology: faces numbered in order of first appearance when the cells are
- * visited in ascending order and their local faces e = 0..nf-1 in order;
- * face e of a cell is the sub-simplex opposite local vertex e.  face_cells
- * lists the adjacent cells in ascending order.  Arrays must hold C*nf faces.
- * face_verts receives the sorted vertex indices of each face ([F][dim]). */
+ * visited in ascending order and their local faces e = 0..nf-1 in order.
+ * Simplices: face e is the sub-simplex opposite local vertex e.  Boxes
+ * (vertices in TNL's Quadrangle / Hexahedron order, v0 the lowest corner,
+ * counterclockwise, bottom layer first): rectangle faces bottom, right, top,
+ * left = (0,1), (1,2), (2,3), (3,0); cuboid faces bottom, front, right,
+ * back, left, top = (0,1,2,3), (0,1,5,4), (1,2,6,5), (2,3,7,6), (3,0,4,7),
+ * (4,5,6,7) (the orientations that MassMatrix.h:152-508 and
+ * BasisFunctions_RTN0.h:55-126 name).  face_cells lists the adjacent cells
+ * in ascending order.  Arrays must hold C*nf faces.  face_verts receives the
+ * sorted vertex indices of each face ([F][fv]). */
+int64_t orc_build_faces_ct(int dim, int cell, int64_t C, const int32_t* cell_verts,
+                           int32_t* cell_faces, int32_t* face_cells, int32_t* face_verts);
+/* the simplex case of orc_build_faces_ct */
 int64_t orc_build_faces(int dim, int64_t C, const int32_t* cell_verts,
                         int32_t* cell_faces, int32_t* face_cells, int32_t* face_verts);
 

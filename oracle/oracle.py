@@ -28,7 +28,8 @@ _pu8 = ct.POINTER(ct.c_uint8)
 
 class OrcProblem(ct.Structure):
     _fields_ = [
-        ("dim", ct.c_int), ("nf", ct.c_int), ("n", ct.c_int), ("S", ct.c_int), ("lumping", ct.c_int),
+        ("dim", ct.c_int), ("cell", ct.c_int), ("nf", ct.c_int), ("nv", ct.c_int), ("fv", ct.c_int),
+        ("n", ct.c_int), ("S", ct.c_int), ("lumping", ct.c_int),
         ("advection", ct.c_int), ("mobility_upwind", ct.c_int),
         ("V", ct.c_int64), ("C", ct.c_int64), ("F", ct.c_int64),
         ("coords", _pd), ("cell_verts", _pi32), ("cell_faces", _pi32), ("face_cells", _pi32),
@@ -49,8 +50,8 @@ def load():
         if not LIB_PATH.exists():
             raise RuntimeError(f"{LIB_PATH} missing: build it with tnl-mhfem_gb300/build.py")
         lib = ct.CDLL(str(LIB_PATH))
-        lib.orc_build_faces.restype = ct.c_int64
-        lib.orc_build_faces.argtypes = [ct.c_int, ct.c_int64, _pi32, _pi32, _pi32, _pi32]
+        lib.orc_build_faces_ct.restype = ct.c_int64
+        lib.orc_build_faces_ct.argtypes = [ct.c_int, ct.c_int, ct.c_int64, _pi32, _pi32, _pi32, _pi32]
         for name in ["orc_face_average", "orc_update_b", "orc_reconstruct", "orc_velocities"]:
             getattr(lib, name).argtypes = [ct.POINTER(OrcProblem)]
             getattr(lib, name).restype = None
@@ -72,17 +73,24 @@ def load():
     return _lib
 
 
-def build_faces(dim: int, cells: np.ndarray):
+def cell_shape(dim: int, cell: int = 0):
+    """(faces per cell, vertices per cell, vertices per face, MassMatrix::size)."""
+    if cell:
+        return 2 * dim, 2 ** dim, 2 ** (dim - 1), dim
+    return dim + 1, dim + 1, dim, 9 if dim == 2 else 14
+
+
+def build_faces(dim: int, cells: np.ndarray, cell: int = 0):
     """Topology by the oracle's own (sort-based) builder."""
     lib = load()
     cells = np.ascontiguousarray(cells, np.int32)
     C = cells.shape[0]
-    nf = dim + 1
+    nf, _, nfv, _ = cell_shape(dim, cell)
     cf = np.empty((C, nf), np.int32)
     fc = np.empty((C * nf, 2), np.int32)
-    fv = np.empty((C * nf, dim), np.int32)
-    F = lib.orc_build_faces(dim, C, cells.ctypes.data_as(_pi32), cf.ctypes.data_as(_pi32),
-                            fc.ctypes.data_as(_pi32), fv.ctypes.data_as(_pi32))
+    fv = np.empty((C * nf, nfv), np.int32)
+    F = lib.orc_build_faces_ct(dim, cell, C, cells.ctypes.data_as(_pi32), cf.ctypes.data_as(_pi32),
+                               fc.ctypes.data_as(_pi32), fv.ctypes.data_as(_pi32))
     return fv[:F].copy(), fc[:F].copy(), cf
 
 
@@ -94,15 +102,15 @@ class OracleModel:
     """One MHFEM problem evaluated by the CPU oracle, mirroring the solver phases."""
 
     def __init__(self, dim, n, lumping, advection, mobility_upwind, coords, cells, coeffs, bc_fn, Z0,
-                 threads: int = 0):
+                 threads: int = 0, cell: int = 0):
         self.lib = load()
         if threads:
             self.lib.orc_set_threads(threads)
-        self.dim, self.n, self.nf = dim, n, dim + 1
-        self.S = 9 if dim == 2 else 14
+        self.dim, self.n, self.cell = dim, n, int(cell)
+        self.nf, self.nv, self.fv, self.S = cell_shape(dim, self.cell)
         self.coords = np.ascontiguousarray(coords, np.float64)
         self.cells = np.ascontiguousarray(cells, np.int32)
-        self.face_verts, self.face_cells, self.cell_faces = build_faces(dim, self.cells)
+        self.face_verts, self.face_cells, self.cell_faces = build_faces(dim, self.cells, self.cell)
         self.C = self.cells.shape[0]
         self.F = self.face_cells.shape[0]
         self.V = self.coords.shape[0]
@@ -120,7 +128,7 @@ class OracleModel:
         self.bvalues = np.ascontiguousarray(values, np.float64)
         self.bdirichlet = np.ascontiguousarray(dirichlet, np.float64)
         P = OrcProblem()
-        P.dim, P.nf, P.n, P.S = dim, nf, n, S
+        P.dim, P.cell, P.nf, P.nv, P.fv, P.n, P.S = dim, self.cell, nf, self.nv, self.fv, n, S
         P.lumping, P.advection, P.mobility_upwind = int(lumping), int(advection), int(mobility_upwind)
         P.V, P.C, P.F = self.V, C, F
         P.coords = _dp(self.coords)
@@ -163,7 +171,7 @@ class OracleModel:
     def from_problem(cls, p, threads: int = 0):
         c = p.config
         m = cls(c.dim, c.n_eq, c.mass_lumping, c.advection, c.mobility_upwind, p.coords, p.cells, p.coeffs,
-                p.bc_fn, p.Z0, threads)
+                p.bc_fn, p.Z0, threads, getattr(c, "cell", 0))
         if p.source is not None:
             m.set_source(*p.source)
         return m

@@ -19,8 +19,9 @@ import pytest
 import scipy.sparse.linalg as spla
 
 from helpers import rel_err, small_cases, variant
+from mhfem import _lib as L
 from mhfem import meshgen, problems
-from oracle.oracle import OracleModel
+from oracle.oracle import OracleModel, build_faces
 
 pytestmark = []
 
@@ -90,11 +91,13 @@ def test_lumped_mass_matrix_is_spd(dim):
         assert np.linalg.eigvalsh(B).min() > 0
 
 
-def _linear_problem(dim, neumann_sign=None):
+def _linear_problem(dim, neumann_sign=None, box=False, lumping=False):
     c = np.array([0.7, -0.4, 0.25][:dim])
     c0 = 0.3
     Dval = 2.5
-    if dim == 2:
+    if box:
+        coords, cells = meshgen.square_rectangles(6) if dim == 2 else meshgen.cube_cuboids(4)
+    elif dim == 2:
         coords, cells = meshgen.square_triangles(6, 0.2, 99)
     else:
         coords, cells = meshgen.cube_tetrahedra(3, 0.15, 99)
@@ -114,7 +117,7 @@ def _linear_problem(dim, neumann_sign=None):
             vals[right] = neumann_sign * Dval * c[0]
         return tags, vals, fcen @ c + c0
 
-    cfg = problems.StaticConfig(dim=dim, n_eq=1)
+    cfg = problems.StaticConfig(dim=dim, n_eq=1, mass_lumping=lumping, cell=L.CELL_BOX if box else L.CELL_SIMPLEX)
     coeffs = {"N": 1.0, "u": 0.0, "m": 1.0, "D": Dval, "w": 0.0, "a": 0.0, "r": 0.0, "f": 0.0, "m_upw": 1.0,
               "m_bnd": 1.0}
     p = problems.Problem("linear", cfg, coords, cells, coeffs, Z0, 1e-2, 3, 1e-13, bc_fn, 0)
@@ -147,6 +150,46 @@ def test_linear_patch_neumann(dim):
         t += p.dt
     fcen = meshgen.face_centroids(p.coords, m.face_verts)
     assert rel_err(m.Z_iF, fcen @ c + c0) < 1e-10
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("lumping", [False, True])
+def test_linear_patch_boxes(dim, lumping):
+    """Rectangles and cuboids (graded, so not squares or cubes), with and
+    without lumping: the RT0 scheme of MassMatrix.h:152-508 reproduces a
+    linear solution, under Dirichlet data and under a prescribed flux."""
+    for sign in (None, -1.0):
+        p, c, c0 = _linear_problem(dim, neumann_sign=sign, box=True, lumping=lumping)
+        m = OracleModel.from_problem(p)
+        t = 0.0
+        for _ in range(p.steps):
+            m.step(t, p.dt, 1e-14)
+            t += p.dt
+        fcen = meshgen.face_centroids(p.coords, m.face_verts)
+        assert rel_err(m.Z_iF, fcen @ c + c0) < 1e-10
+        assert rel_err(m.Z_iK, meshgen.cell_centroids(p.coords, p.cells) @ c + c0) < 1e-10
+
+
+def test_box_topology():
+    """Face numbering of box cells: first appearance over (cell, local face)
+    with the local faces of the reference's Quadrangle / Hexahedron; every
+    interior face has two cells; face counts of the tensor grids."""
+    for dim, N in ((2, 3), (3, 2)):
+        coords, cells = meshgen.square_rectangles(N) if dim == 2 else meshgen.cube_cuboids(N)
+        fv, fc, cf = build_faces(dim, cells, 1)
+        F = fc.shape[0]
+        expect = 2 * N * (N + 1) if dim == 2 else 3 * N * N * (N + 1)
+        assert F == expect
+        assert (fc[:, 1] >= 0).sum() == (2 * N * (N - 1) if dim == 2 else 3 * N * N * (N - 1))
+        assert np.array_equal(cf[0], np.arange(2 * dim))  # the first cell numbers its faces 0..nf-1
+        # face e of cell 0 lies on the side the reference names it after
+        fcen = meshgen.face_centroids(coords, fv)
+        ccen = coords[cells[0]].mean(axis=0)
+        d = fcen[cf[0]] - ccen
+        if dim == 2:  # bottom, right, top, left
+            assert d[0, 1] < 0 and d[1, 0] > 0 and d[2, 1] > 0 and d[3, 0] < 0
+        else:  # bottom, front, right, back, left, top
+            assert d[0, 2] < 0 and d[1, 1] < 0 and d[2, 0] > 0 and d[3, 1] > 0 and d[4, 0] < 0 and d[5, 2] > 0
 
 
 def test_local_conservation():

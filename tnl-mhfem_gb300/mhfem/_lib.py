@@ -44,7 +44,11 @@ KERNEL_CELL_LOCAL, KERNEL_ASSEMBLE, KERNEL_SPMV_FP64, KERNEL_SPMV_FP32, KERNEL_R
 class Desc(ct.Structure):
     _fields_ = [("dim", ct.c_int32), ("n_eq", ct.c_int32), ("mass_lumping", ct.c_int32),
                 ("advection", ct.c_int32), ("mobility_upwind", ct.c_int32), ("form", ct.c_int32),
-                ("device", ct.c_int32)]
+                ("device", ct.c_int32), ("cell", ct.c_int32)]
+
+
+CELL_SIMPLEX = 0
+CELL_BOX = 1
 
 
 class SolverOpts(ct.Structure):

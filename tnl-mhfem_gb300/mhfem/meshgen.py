@@ -65,6 +65,45 @@ def cube_tetrahedra(N: int, jitter: float = 0.15, seed: int = 1234):
     return coords, cells
 
 
+def _graded_axis(N: int, amplitude: float = 0.25) -> np.ndarray:
+    """N + 1 monotone nodes on [0, 1] with non-uniform spacing (sine grading)."""
+    i = np.arange(N + 1, dtype=np.float64)
+    return i / N + amplitude / N * np.sin(2 * np.pi * i / N) / (2 * np.pi) * 2
+
+
+def square_rectangles(N: int, graded: bool = True):
+    """N x N axis-aligned rectangles on the unit square (tensor-product grid,
+    graded so the cells are not squares).  Vertex order of each cell as the
+    reference's Quadrangle: v0 lower-left, v1 lower-right, v2 upper-right,
+    v3 upper-left."""
+    x = _graded_axis(N) if graded else np.linspace(0, 1, N + 1)
+    y = _graded_axis(N, 0.15) if graded else np.linspace(0, 1, N + 1)
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    coords = np.stack([X.ravel(), Y.ravel()], axis=1)
+    vid = lambda i, j: i * (N + 1) + j
+    i, j = np.meshgrid(np.arange(N), np.arange(N), indexing="ij")
+    i, j = i.ravel(), j.ravel()
+    cells = np.stack([vid(i, j), vid(i + 1, j), vid(i + 1, j + 1), vid(i, j + 1)], axis=1).astype(np.int32)
+    return coords, cells
+
+
+def cube_cuboids(N: int, graded: bool = True):
+    """N^3 axis-aligned cuboids on the unit cube (graded tensor-product grid).
+    Vertex order as the reference's Hexahedron: the bottom rectangle
+    v0..v3 counterclockwise from the lowest corner, then the top v4..v7."""
+    ax = [(_graded_axis(N, a) if graded else np.linspace(0, 1, N + 1)) for a in (0.25, 0.15, 0.2)]
+    X, Y, Z = np.meshgrid(*ax, indexing="ij")
+    coords = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+    M = N + 1
+    vid = lambda i, j, k: (i * M + j) * M + k
+    i, j, k = np.meshgrid(np.arange(N), np.arange(N), np.arange(N), indexing="ij")
+    i, j, k = i.ravel(), j.ravel(), k.ravel()
+    cells = np.stack([vid(i, j, k), vid(i + 1, j, k), vid(i + 1, j + 1, k), vid(i, j + 1, k),
+                      vid(i, j, k + 1), vid(i + 1, j, k + 1), vid(i + 1, j + 1, k + 1), vid(i, j + 1, k + 1)],
+                     axis=1).astype(np.int32)
+    return coords, cells
+
+
 def gaussian_field(shape, corr_length: float = 0.1, seed: int = 5678) -> np.ndarray:
     """Zero-mean, unit-variance Gaussian random field on a periodic grid of
     the unit square/cube, with Gaussian covariance of the given correlation

@@ -111,6 +111,40 @@ def diffusion3d(N: int = 64, steps: int = 50, dt: float = 1e-3, tol: float = 1e-
                    _diffusion_bc(coords), N)
 
 
+def heat2d_rect(N: int = 128, steps: int = 100, dt: float = 1e-4, tol: float = 1e-12, lumping: bool = False,
+                form: int = L.FORM_FP64) -> Problem:
+    """The heat-equation workload on N x N graded rectangles (box cells)."""
+    coords, cells = meshgen.square_rectangles(N)
+    cen = meshgen.cell_centroids(coords, cells)
+    Z0 = np.exp(-50.0 * ((cen - 0.5) ** 2).sum(axis=1))
+    coeffs = {"N": 1.0, "u": 0.0, "m": 1.0, "D": 1.0, "w": 0.0, "a": 0.0, "r": 0.0, "f": 0.0, "m_upw": 1.0,
+              "m_bnd": 1.0}
+
+    def bc_fn(face_verts, face_cells):
+        F = face_cells.shape[0]
+        return (np.zeros(F, np.uint8), np.zeros(F), np.zeros(F))
+
+    cfg = StaticConfig(dim=2, n_eq=1, mass_lumping=lumping, advection=L.EXPLICIT_UPWIND, mobility_upwind=False,
+                       form=form, cell=L.CELL_BOX)
+    return Problem("heat2d_rect", cfg, coords, cells, coeffs, Z0, dt, steps, tol, bc_fn, N)
+
+
+def diffusion3d_box(N: int = 64, steps: int = 50, dt: float = 1e-3, tol: float = 1e-10, lumping: bool = False,
+                    field_seed: int = 5678, form: int = L.FORM_FP64) -> Problem:
+    """The heterogeneous-diffusion workload on N^3 graded cuboids (box cells)."""
+    coords, cells = meshgen.cube_cuboids(N)
+    g = meshgen.gaussian_field((N, N, N), 0.1, field_seed)
+    cen = meshgen.cell_centroids(coords, cells)
+    gx, gy, gz = meshgen.cell_grid_index(cen, N)
+    D = np.exp(g[gx, gy, gz])
+    coeffs = {"N": 1.0, "u": 0.0, "m": 1.0, "D": D, "w": 0.0, "a": 0.0, "r": 0.0, "f": 1.0, "m_upw": 1.0,
+              "m_bnd": 1.0}
+    cfg = StaticConfig(dim=3, n_eq=1, mass_lumping=lumping, advection=L.EXPLICIT_UPWIND, mobility_upwind=False,
+                       form=form, cell=L.CELL_BOX)
+    return Problem("diffusion3d_box", cfg, coords, cells, coeffs, np.zeros(cells.shape[0]), dt, steps, tol,
+                   _diffusion_bc(coords), N)
+
+
 def diffusion3d_source(N: int = 64, steps: int = 1000, dt: float = 1e-3, tol: float = 1e-10, seed: int = 1234,
                        field_seed: int = 5678, psi_seed: int = 9101, form: int = L.FORM_FP64) -> Problem:
     p = diffusion3d(N, steps, dt, tol, seed, field_seed, form)

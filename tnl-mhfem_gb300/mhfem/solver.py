@@ -39,6 +39,19 @@ class StaticConfig:
     mobility_upwind: bool = False
     form: int = L.FORM_FP64
     device: int = 0
+    cell: int = L.CELL_SIMPLEX  # CELL_BOX: rectangles / cuboids
+
+    @property
+    def faces_per_cell(self) -> int:
+        return 2 * self.dim if self.cell == L.CELL_BOX else self.dim + 1
+
+    @property
+    def verts_per_cell(self) -> int:
+        return 2 ** self.dim if self.cell == L.CELL_BOX else self.dim + 1
+
+    @property
+    def verts_per_face(self) -> int:
+        return 2 ** (self.dim - 1) if self.cell == L.CELL_BOX else self.dim
 
 
 COEF_IDS = {"N": L.COEF_N, "u": L.COEF_U, "m": L.COEF_M, "D": L.COEF_D, "w": L.COEF_W, "a": L.COEF_A,
@@ -52,7 +65,7 @@ class Solver:
         self.lib = L.load()
         self.config = config
         desc = L.Desc(config.dim, config.n_eq, int(config.mass_lumping), config.advection,
-                      int(config.mobility_upwind), config.form, config.device)
+                      int(config.mobility_upwind), config.form, config.device, config.cell)
         h = ct.c_void_p()
         st = self.lib.mhfem_create(ct.byref(desc), ct.byref(h))
         if st != L.OK:
@@ -89,17 +102,16 @@ class Solver:
         coords = np.ascontiguousarray(coords, dtype=np.float64)
         cells = np.ascontiguousarray(cells, dtype=np.int32)
         assert coords.ndim == 2 and coords.shape[1] == self.config.dim
-        assert cells.ndim == 2 and cells.shape[1] == self.config.dim + 1
+        assert cells.ndim == 2 and cells.shape[1] == self.config.verts_per_cell
         self._ck(self.lib.mhfem_set_mesh(self._h, coords.shape[0], _dptr(coords), cells.shape[0], _i32ptr(cells)))
         V = ct.c_int64(); C = ct.c_int64(); F = ct.c_int64()
         self._ck(self.lib.mhfem_get_sizes(self._h, ct.byref(V), ct.byref(C), ct.byref(F), None, None))
         self.V, self.C, self.F = V.value, C.value, F.value
 
     def topology(self):
-        d = self.config.dim
-        fv = np.empty((self.F, d), np.int32)
+        fv = np.empty((self.F, self.config.verts_per_face), np.int32)
         fc = np.empty((self.F, 2), np.int32)
-        cf = np.empty((self.C, d + 1), np.int32)
+        cf = np.empty((self.C, self.config.faces_per_cell), np.int32)
         self._ck(self.lib.mhfem_get_topology(self._h, _i32ptr(fv), _i32ptr(fc), _i32ptr(cf)))
         return fv, fc, cf
 
