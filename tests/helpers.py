@@ -70,6 +70,43 @@ def small_cases():
     q.Z0 = rng.uniform(0, 1, 2 * C)
     cases["diffusion3d_n2"] = q
     cases.update(three_component_cases())
+    cases.update(box_cases())
+    return cases
+
+
+def box_cases():
+    """Rectangles and cuboids: full and lumped RT0 mass matrices, mobility
+    upwinding (reconstructed velocities), advection on rectangles (explicit and
+    implicit upwind, two components) and two coupled components on cuboids."""
+    cases = {}
+    cases["heat2d_rect"] = problems.heat2d_rect(N=8, steps=3)
+    cases["heat2d_rect_lumped"] = problems.heat2d_rect(N=8, steps=2, lumping=True)
+    cases["diffusion3d_box"] = problems.diffusion3d_box(N=4, steps=3)
+    cases["diffusion3d_box_lumped"] = problems.diffusion3d_box(N=4, steps=2, lumping=True)
+    p = problems.diffusion3d_box(N=4, steps=3)
+    rng = np.random.default_rng(17)
+    cases["diffusion3d_box_mobility"] = variant(p, mobility_upwind=True,
+                                                coeffs={"m": rng.uniform(0.5, 2.0, p.C), "m_bnd": 1.5})
+    p = problems.adr2d(N=8, steps=3, box=True)
+    cases["adr2d_rect"] = p
+    cases["adr2d_rect_implicit_upwind"] = variant(p, advection=L.IMPLICIT_UPWIND, mass_lumping=False)
+    # two components on cuboids: coupled diffusion and reaction, a full w field
+    p3 = problems.diffusion3d_box(N=3, steps=2)
+    C = p3.C
+    Nc = np.zeros((2, 2, C)); Nc[0, 0] = 1.0; Nc[1, 1] = 2.0
+    D = np.zeros((2, 2, C)); D[0, 0] = p3.coeffs["D"]; D[1, 1] = 0.5 * p3.coeffs["D"]; D[0, 1] = 0.1
+    r = np.zeros((2, 2, C)); r[0, 0] = 0.3; r[0, 1] = -0.1; r[1, 0] = -0.1; r[1, 1] = 0.2
+    w = rng.uniform(-0.01, 0.01, (2, 6, C))
+    base_bc = p3.bc_fn
+
+    def bc2(fv, fc):
+        t, v, d = base_bc(fv, fc)
+        return np.concatenate([t, t]), np.concatenate([v, v + 0.1 * (t == 1)]), np.concatenate([d + 0.2, d])
+
+    q = variant(p3, n_eq=2, coeffs={"N": Nc.ravel(), "D": D.ravel(), "r": r.ravel(), "w": w.ravel(), "f": 0.5})
+    q.bc_fn = bc2
+    q.Z0 = rng.uniform(0, 1, 2 * C)
+    cases["diffusion3d_box_n2"] = q
     return cases
 
 

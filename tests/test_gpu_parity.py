@@ -47,8 +47,8 @@ def test_step_parity(name):
     p = CASES[name]
     s, m = _pair(p)
     n, C = p.n, p.C
-    nf = p.config.dim + 1
-    S = 9 if p.config.dim == 2 else 14
+    nf = p.config.faces_per_cell
+    S = m.S
     t = 0.0
     for step in range(p.steps):
         if p.config.mobility_upwind and step > 0:

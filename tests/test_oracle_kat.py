@@ -213,7 +213,7 @@ def test_row_structure_and_direct_solve(name):
     m.pre_iterate(0.0, p.dt)
     m.assemble(0.0, p.dt)
     A = m.csr()
-    n, nf = p.n, p.config.dim + 1
+    n, nf = p.n, p.config.faces_per_cell
     lens = np.diff(A.indptr)
     interior = np.repeat(m.face_cells[:, 1] >= 0, n)
     assert np.all(lens[interior] == (2 * nf - 1) * n)

@@ -56,7 +56,7 @@ def _stale(target: Path, deps: list[Path]) -> bool:
 def build_library(force: bool = False, verbose: bool = False) -> Path:
     nvcc = _nvcc()
     BUILD_DIR.mkdir(exist_ok=True)
-    headers = list(CSRC.glob("*.h")) + [REPO_DIR / "include" / "mhfem.h"]
+    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [REPO_DIR / "include" / "mhfem.h"]
     srcs = _sources()
     objs = []
     jobs = []

@@ -63,7 +63,7 @@ void invalidate_graphs(mhfem_t h)
 DevProblem make_problem(mhfem_t h)
 {
     DevProblem P{};
-    P.dim = h->dim; P.nf = h->nf; P.n = h->n; P.S = h->S;
+    P.dim = h->dim; P.cell = h->cell; P.nf = h->nf; P.n = h->n; P.S = h->S;
     P.lumping = h->desc.mass_lumping;
     P.advection = h->desc.advection;
     P.mobility_upwind = h->desc.mobility_upwind;
@@ -138,6 +138,8 @@ mhfem_status mhfem_create(const mhfem_desc* desc, mhfem_t* out)
     if (desc->n_eq < 1 || desc->n_eq > 3) return MHFEM_ERR_UNSUPPORTED;
     if (desc->advection < 0 || desc->advection > 2) return MHFEM_ERR_INVALID_ARGUMENT;
     if (desc->form < 0 || desc->form > 2) return MHFEM_ERR_INVALID_ARGUMENT;
+    if (desc->cell != MHFEM_CELL_SIMPLEX && desc->cell != MHFEM_CELL_BOX) return MHFEM_ERR_INVALID_ARGUMENT;
+    if (desc->cell == MHFEM_CELL_BOX && desc->form == MHFEM_FORM_LEARNED) return MHFEM_ERR_UNSUPPORTED;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return MHFEM_ERR_NO_DEVICE;
     if (desc->device < 0 || desc->device >= ndev) return MHFEM_ERR_NO_DEVICE;
@@ -145,9 +147,20 @@ mhfem_status mhfem_create(const mhfem_desc* desc, mhfem_t* out)
     mhfem_t h = new mhfem_solver_s();
     h->desc = *desc;
     h->dim = desc->dim;
-    h->nf = desc->dim + 1;
+    h->cell = desc->cell;
     h->n = desc->n_eq;
-    h->S = (desc->dim == 2) ? 9 : 14;
+    if (desc->cell == MHFEM_CELL_BOX) {
+        // MassMatrix<Quadrangle / Hexahedron>::size: one value per face orientation
+        h->nf = 2 * desc->dim;
+        h->nv = 1 << desc->dim;
+        h->S = desc->dim;
+    }
+    else {
+        // MassMatrix<Triangle / Tetrahedron>::size: packed upper triangle + row sums
+        h->nf = desc->dim + 1;
+        h->nv = desc->dim + 1;
+        h->S = (desc->dim == 2) ? 9 : 14;
+    }
     mhfem_default_solver_opts(&h->opts);
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete h;
@@ -189,9 +202,9 @@ mhfem_status mhfem_set_mesh(mhfem_t h, int64_t V, const double* coords, int64_t 
 {
     if (!h || !coords || !cell_verts || V <= 0 || C <= 0) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "invalid mesh arguments");
     cudaSetDevice(h->desc.device);
-    std::string msg = build_topology(h->dim, V, coords, C, cell_verts, h->topo);
+    std::string msg = build_topology(h->dim, h->cell, V, coords, C, cell_verts, h->topo);
     if (!msg.empty()) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "%s", msg.c_str());
-    const int nf = h->nf, n = h->n;
+    const int nf = h->nf, nv = h->nv, n = h->n;
     const int64_t F = h->topo.F;
     // release everything that depends on the mesh
     invalidate_graphs(h);
@@ -212,13 +225,13 @@ mhfem_status mhfem_set_mesh(mhfem_t h, int64_t V, const double* coords, int64_t 
 
     h->h_coords.assign(coords, coords + V * h->dim);
     // topology on the device, SoA with the cell index innermost
-    std::vector<int32_t> soa((size_t)C * nf);
+    std::vector<int32_t> soa((size_t)C * std::max(nf, nv));
     CK(dalloc(h, &h->coords, (size_t)V * h->dim));
     CK(cudaMemcpy(h->coords, coords, sizeof(double) * V * h->dim, cudaMemcpyHostToDevice));
     for (int64_t K = 0; K < C; ++K)
-        for (int v = 0; v < nf; ++v) soa[(size_t)v * C + K] = cell_verts[K * nf + v];
-    CK(dalloc(h, &h->cell_verts, (size_t)C * nf));
-    CK(cudaMemcpy(h->cell_verts, soa.data(), sizeof(int32_t) * C * nf, cudaMemcpyHostToDevice));
+        for (int v = 0; v < nv; ++v) soa[(size_t)v * C + K] = cell_verts[K * nv + v];
+    CK(dalloc(h, &h->cell_verts, (size_t)C * nv));
+    CK(cudaMemcpy(h->cell_verts, soa.data(), sizeof(int32_t) * C * nv, cudaMemcpyHostToDevice));
     for (int64_t K = 0; K < C; ++K)
         for (int e = 0; e < nf; ++e) soa[(size_t)e * C + K] = h->topo.cell_faces[K * nf + e];
     CK(dalloc(h, &h->cell_faces, (size_t)C * nf));
@@ -418,8 +431,19 @@ mhfem_status ensure_pattern(mhfem_t h)
         CK(dalloc(h, &h->A.vals32, (size_t)W * rows));
         CK(cudaMemset(h->A.vals32, 0, sizeof(float) * W * rows));
     }
-    CK(dalloc(h, &h->amap.qmap, (size_t)F));
-    CK(cudaMemcpy(h->amap.qmap, h->pat.qmap.data(), sizeof(uint32_t) * F, cudaMemcpyHostToDevice));
+    if (h->nf > 4) {  // 12 positions of 4 bits: one 64-bit word per face
+        uint64_t* q = nullptr;
+        CK(dalloc(h, &q, (size_t)F));
+        h->amap.qmap = q;
+        CK(cudaMemcpy(q, h->pat.qmap.data(), sizeof(uint64_t) * F, cudaMemcpyHostToDevice));
+    }
+    else {
+        const std::vector<uint32_t> q32(h->pat.qmap.begin(), h->pat.qmap.end());
+        uint32_t* q = nullptr;
+        CK(dalloc(h, &q, (size_t)F));
+        h->amap.qmap = q;
+        CK(cudaMemcpy(q, q32.data(), sizeof(uint32_t) * F, cudaMemcpyHostToDevice));
+    }
     CK(dalloc(h, &h->amap.qdiag, (size_t)F));
     CK(cudaMemcpy(h->amap.qdiag, h->pat.qdiag.data(), F, cudaMemcpyHostToDevice));
     CK(dalloc(h, &h->rhs, (size_t)rows));
@@ -780,12 +804,13 @@ mhfem_status mhfem_time_kernel(mhfem_t h, int32_t kernel, int32_t reps, double* 
     // algorithmic bytes: each array once at its size; FLOPs: FP64 (FP32 for the SpMV32) operations
     switch (kernel) {
         case MHFEM_KERNEL_CELL_LOCAL:
-            B = 4 * nf * C + 8 * d * V + (h->coef[MHFEM_COEF_D].count > 1 ? 8 * n * n * C : 0) + 8 * n * C
-              + 4 * nf * C + C + 8 * n * n * S * C + 8 * n * n * nf * C + 8 * n * C + rec;
-            FL = C * (nf == 4 ? 420.0 : 220.0) * n * n;
+            // a box cell reads two of its vertices (the lowest and the opposite corner)
+            B = 4 * (h->cell ? 2 : h->nv) * C + 8 * d * V + (h->coef[MHFEM_COEF_D].count > 1 ? 8 * n * n * C : 0)
+              + 8 * n * C + 4 * nf * C + C + 8 * n * n * S * C + 8 * n * n * nf * C + 8 * n * C + rec;
+            FL = C * (h->cell ? 4.0 * nf * nf : (nf == 4 ? 420.0 : 220.0)) * n * n;
             break;
         case MHFEM_KERNEL_ASSEMBLE:
-            B = 8 * F + 2 * F + 4 * F + F + rec + 8 * W * R + 8 * R
+            B = 8 * F + 2 * F + (nf > 4 ? 8 : 4) * F + F + rec + 8 * W * R + 8 * R
               + (h->desc.form == MHFEM_FORM_MIXED ? 4 * W * R : 0);
             FL = R * (W + 3);
             break;

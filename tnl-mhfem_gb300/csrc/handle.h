@@ -24,7 +24,7 @@ struct DevCoef {
 
 struct mhfem_solver_s {
     mhfem_desc desc{};
-    int dim = 0, nf = 0, n = 0, S = 0;
+    int dim = 0, cell = 0, nf = 0, nv = 0, n = 0, S = 0;  // nv: vertices per cell
     std::string err;
     cudaStream_t stream = nullptr;
     int sms = 0;

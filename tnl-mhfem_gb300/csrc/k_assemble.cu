@@ -11,9 +11,13 @@
 // ELL form [slot][row] (column-major across rows: a warp's loads of one slot
 // are one contiguous 256-byte segment).  The merged, ascending face order of
 // the reference's row setters is precomputed once per mesh as a 4-bit
-// position per (side, local face) ("qmap"), so the kernel does no sorting.
+// position per (side, local face) ("qmap", one 32-bit word per face for
+// up to 4 faces per cell, one 64-bit word for the 6 faces of a cuboid), so
+// the kernel does no sorting.
 // The local Schur entries come from the per-(cell, local face) records that
 // k_cell_local wrote; each record is read by exactly one row.
+#include <type_traits>
+
 #include "mhfem_internal.h"
 
 namespace mhfem {
@@ -21,8 +25,11 @@ namespace mhfem {
 // W32: also write the FP32 copy of the values (mixed form).  A template flag,
 // not a run-time test, so that the FP64-only variant carries no conversions
 // (which issue on the scarce FP64 pipe even when predicated off).
+template <int NF>
+using QmapWord = std::conditional_t<(NF > 4), uint64_t, uint32_t>;
+
 template <int NF, int NE, bool W32>
-__global__ void __launch_bounds__(256) k_assemble(const DevProblem P, const uint32_t* __restrict__ qmap,
+__global__ void __launch_bounds__(256) k_assemble(const DevProblem P, const QmapWord<NF>* __restrict__ qmap,
                                                   const uint8_t* __restrict__ qdiag, int W,
                                                   double* __restrict__ vals, float* __restrict__ vals32,
                                                   double* __restrict__ rhs)
@@ -36,7 +43,7 @@ __global__ void __launch_bounds__(256) k_assemble(const DevProblem P, const uint
     const int2 kk = __ldg(&P.face_cells[E]);
     const int e0 = __ldg(P.face_local + 2 * E);
     const int e1 = __ldg(P.face_local + 2 * E + 1);
-    const uint32_t qm = __ldg(qmap + E);
+    const QmapWord<NF> qm = __ldg(qmap + E);
     const int dslot = __ldg(qdiag + E) * NE + i;
 
     auto put = [&](int q, int j, double v) {
@@ -77,7 +84,7 @@ __global__ void __launch_bounds__(256) k_assemble(const DevProblem P, const uint
         const double rd = recip_newton(diag);
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
-            const int q = (qm >> (4 * f)) & 15u;
+            const int q = (int)((qm >> (4 * f)) & 15u);
 #pragma unroll
             for (int j = 0; j < NE; ++j) {
                 if (j == i && f == e0) continue;
@@ -106,7 +113,7 @@ __global__ void __launch_bounds__(256) k_assemble(const DevProblem P, const uint
     const double rd = recip_newton(diag);
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
-        const int q = (qm >> (4 * f)) & 15u;
+        const int q = (int)((qm >> (4 * f)) & 15u);
 #pragma unroll
         for (int j = 0; j < NE; ++j) {
             if (f == e0) {
@@ -120,7 +127,7 @@ __global__ void __launch_bounds__(256) k_assemble(const DevProblem P, const uint
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
         if (f == e1) continue;
-        const int q = (qm >> (4 * (NF + f))) & 15u;
+        const int q = (int)((qm >> (4 * (NF + f))) & 15u);
 #pragma unroll
         for (int j = 0; j < NE; ++j) put(q, j, A1[j * NF + f] * rd);
     }
@@ -132,18 +139,22 @@ int launch_assemble(const DevProblem& P, const AssemblyMap& M, EllMatrix& A, dou
 {
     if (P.rows == 0) return 0;
     const unsigned grid = (unsigned)((P.rows + 255) / 256);
-#define MHFEM_ASSEMBLE(W32, V32)                                                                          \
-    do {                                                                                                  \
-        if (P.nf == 3 && P.n == 1) k_assemble<3, 1, W32><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, V32, rhs); \
-        else if (P.nf == 3 && P.n == 2) k_assemble<3, 2, W32><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, V32, rhs); \
-        else if (P.nf == 3) k_assemble<3, 3, W32><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, V32, rhs); \
-        else if (P.n == 1) k_assemble<4, 1, W32><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, V32, rhs); \
-        else if (P.n == 2) k_assemble<4, 2, W32><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, V32, rhs); \
-        else k_assemble<4, 3, W32><<<grid, 256, 0, s>>>(P, M.qmap, M.qdiag, A.width, A.vals, V32, rhs); \
+#define MHFEM_ASSEMBLE_NF(NFV, W32, V32)                                                             \
+    do {                                                                                             \
+        if (P.n == 1) k_assemble<NFV, 1, W32><<<grid, 256, 0, s>>>(P, (const QmapWord<NFV>*)M.qmap, M.qdiag, A.width, A.vals, V32, rhs); \
+        else if (P.n == 2) k_assemble<NFV, 2, W32><<<grid, 256, 0, s>>>(P, (const QmapWord<NFV>*)M.qmap, M.qdiag, A.width, A.vals, V32, rhs); \
+        else k_assemble<NFV, 3, W32><<<grid, 256, 0, s>>>(P, (const QmapWord<NFV>*)M.qmap, M.qdiag, A.width, A.vals, V32, rhs); \
+    } while (0)
+#define MHFEM_ASSEMBLE(W32, V32)                          \
+    do {                                                  \
+        if (P.nf == 3) MHFEM_ASSEMBLE_NF(3, W32, V32);    \
+        else if (P.nf == 4) MHFEM_ASSEMBLE_NF(4, W32, V32); \
+        else MHFEM_ASSEMBLE_NF(6, W32, V32);              \
     } while (0)
     if (write32) MHFEM_ASSEMBLE(true, A.vals32);
     else MHFEM_ASSEMBLE(false, nullptr);
 #undef MHFEM_ASSEMBLE
+#undef MHFEM_ASSEMBLE_NF
     return 1;
 }
 

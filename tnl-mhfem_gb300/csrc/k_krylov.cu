@@ -88,15 +88,17 @@ static void launch_pdl(void (*kernel)(KArgs...), cudaStream_t s, Args&&... args)
     cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
-// Compile-time ELL widths of the supported cell types: (2f - 1) n - 1 for
-// triangles / tetrahedra with one or two components; other widths (meshes
-// without interior faces) take the run-time loop.
+// Compile-time ELL widths (2f - 1) n - 1 of the common cases: triangles
+// (4, 9), tetrahedra and rectangles (6, 13) with one or two components,
+// cuboids with one (10); other widths (three components, two-component
+// cuboids, meshes without interior faces) take the run-time loop.
 #define MHFEM_WIDTH_DISPATCH(W, CALL)                                   \
     do {                                                                \
         switch (W) {                                                    \
             case 4: { constexpr int WW = 4; CALL; } break;              \
             case 6: { constexpr int WW = 6; CALL; } break;              \
             case 9: { constexpr int WW = 9; CALL; } break;              \
+            case 10: { constexpr int WW = 10; CALL; } break;            \
             case 13: { constexpr int WW = 13; CALL; } break;            \
             default: { constexpr int WW = 0; CALL; } break;             \
         }                                                               \

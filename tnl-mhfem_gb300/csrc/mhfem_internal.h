@@ -69,7 +69,7 @@ __device__ __forceinline__ double recip_newton(double d)
 
 // Device-side view of a problem, passed by value to kernels.
 struct DevProblem {
-    int dim, nf, n, S, lumping, advection, mobility_upwind;
+    int dim, cell, nf, n, S, lumping, advection, mobility_upwind;  // cell: 0 simplices, 1 boxes
     int64_t V, C, F, rows;
     const double* coords;        // [V][dim]
     const int32_t* cell_verts;   // SoA [v][C]
@@ -110,7 +110,8 @@ struct EllMatrix {
 
 // Per-row assembly map: which ELL slot each (side, local face) goes to.
 struct AssemblyMap {
-    uint32_t* qmap = nullptr;    // per face: 4 bits per (side, local face): merged position q
+    void* qmap = nullptr;        // per face: 4 bits per (side, local face): merged position q;
+                                 // uint32 words up to 4 faces per cell, uint64 for cuboids
     uint8_t* qdiag = nullptr;    // per face: merged position of the face itself
 };
 

@@ -28,51 +28,83 @@ double simplex_measure(const double* const* P, int k, int dim)
     return std::fabs(det) / 6.0;
 }
 
+// local vertices of the faces of a rectangle / cuboid (TNL Quadrangle and
+// Hexahedron subentity topologies)
+const int kRectFaces[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
+const int kCuboidFaces[6][4] = {{0, 1, 2, 3}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}, {4, 5, 6, 7}};
+
+// an axis-parallel rectangle in 3D given by its four corners: the product of
+// its two nonzero extents
+double box_face_measure(const double* const* P)
+{
+    double lo[3], hi[3];
+    for (int d = 0; d < 3; ++d) lo[d] = hi[d] = P[0][d];
+    for (int v = 1; v < 4; ++v)
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = std::min(lo[d], P[v][d]);
+            hi[d] = std::max(hi[d], P[v][d]);
+        }
+    const double ext[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+    int dmin = 0;
+    for (int d = 1; d < 3; ++d)
+        if (ext[d] < ext[dmin]) dmin = d;
+    double m = 1;
+    for (int d = 0; d < 3; ++d)
+        if (d != dmin) m *= ext[d];
+    return m;
+}
+
 struct Key {
-    int32_t b, c;
+    int32_t b, c, d;
     int32_t slot;
 };
 
 }  // namespace
 
-std::string build_topology(int dim, int64_t V, const double* coords, int64_t C, const int32_t* cell_verts,
-                           HostTopology& T)
+std::string build_topology(int dim, int cell, int64_t V, const double* coords, int64_t C,
+                           const int32_t* cell_verts, HostTopology& T)
 {
     if (dim != 2 && dim != 3) return "dim must be 2 or 3";
-    const int nf = dim + 1;
+    if (cell != 0 && cell != 1) return "cell type must be 0 (simplices) or 1 (boxes)";
+    const int nf = cell ? 2 * dim : dim + 1;
+    const int nv = cell ? (1 << dim) : dim + 1;
+    const int fv = cell ? (1 << (dim - 1)) : dim;
     const int64_t N = C * nf;
     if (N >= (int64_t)INT32_MAX) return "mesh too large for int32 face slots";
-    for (int64_t q = 0; q < C * nf; ++q)
+    for (int64_t q = 0; q < C * nv; ++q)
         if (cell_verts[q] < 0 || cell_verts[q] >= V) return "cell vertex index out of range";
 
     T = HostTopology();
     T.dim = dim;
+    T.cell = cell;
     T.nf = nf;
+    T.nv = nv;
+    T.fv = fv;
     T.V = V;
     T.C = C;
 
     // 1. sorted vertex tuple of every (cell, local face) slot; bucket by its smallest vertex
-    std::vector<int32_t> fa(N), fb(N), fc(N);
+    std::vector<int32_t> fa(N), fb(N), fc(N), fd(N);
 #pragma omp parallel for schedule(static)
     for (int64_t K = 0; K < C; ++K)
         for (int e = 0; e < nf; ++e) {
-            int32_t v[3] = {-1, -1, -1};
-            int c = 0;
-            for (int q = 0; q < nf; ++q)
-                if (q != e) v[c++] = cell_verts[K * nf + q];
-            if (dim == 2) {
-                if (v[0] > v[1]) std::swap(v[0], v[1]);
+            int32_t v[4] = {-1, -1, -1, -1};
+            if (!cell) {
+                int c = 0;
+                for (int q = 0; q < nv; ++q)
+                    if (q != e) v[c++] = cell_verts[K * nv + q];
             }
-            else {
-                if (v[0] > v[1]) std::swap(v[0], v[1]);
-                if (v[1] > v[2]) std::swap(v[1], v[2]);
-                if (v[0] > v[1]) std::swap(v[0], v[1]);
-            }
+            else
+                for (int q = 0; q < fv; ++q) v[q] = cell_verts[K * nv + (dim == 2 ? kRectFaces[e][q] : kCuboidFaces[e][q])];
+            for (int x = 1; x < fv; ++x)
+                for (int y = x; y > 0 && v[y - 1] > v[y]; --y) std::swap(v[y - 1], v[y]);
             const int64_t s = K * nf + e;
             fa[s] = v[0];
             fb[s] = v[1];
             fc[s] = v[2];
-            if (v[0] == v[1] || (dim == 3 && v[1] == v[2])) fa[s] = -2;  // degenerate cell
+            fd[s] = v[3];
+            for (int x = 1; x < fv; ++x)
+                if (v[x] == v[x - 1]) fa[s] = -2;  // degenerate cell
         }
     for (int64_t s = 0; s < N; ++s)
         if (fa[s] == -2) return "degenerate cell (repeated vertex)";
@@ -83,7 +115,7 @@ std::string build_topology(int dim, int64_t V, const double* coords, int64_t C, 
     std::vector<Key> keys(N);
     {
         std::vector<int64_t> pos(start.begin(), start.end() - 1);
-        for (int64_t s = 0; s < N; ++s) keys[pos[fa[s]]++] = Key{fb[s], fc[s], (int32_t)s};
+        for (int64_t s = 0; s < N; ++s) keys[pos[fa[s]]++] = Key{fb[s], fc[s], fd[s], (int32_t)s};
     }
 
     // 2. group equal faces inside each bucket; rep = smallest slot of the group
@@ -96,11 +128,12 @@ std::string build_topology(int dim, int64_t V, const double* coords, int64_t C, 
         std::sort(k0, k1, [](const Key& x, const Key& y) {
             if (x.b != y.b) return x.b < y.b;
             if (x.c != y.c) return x.c < y.c;
+            if (x.d != y.d) return x.d < y.d;
             return x.slot < y.slot;
         });
         for (Key* g = k0; g < k1;) {
             Key* h = g + 1;
-            while (h < k1 && h->b == g->b && h->c == g->c) ++h;
+            while (h < k1 && h->b == g->b && h->c == g->c && h->d == g->d) ++h;
             if (h - g > 2) bad = 1;  // non-manifold: a face shared by more than two cells
             for (Key* q = g; q < h; ++q) rep[q->slot] = g->slot;
             g = h;
@@ -117,7 +150,7 @@ std::string build_topology(int dim, int64_t V, const double* coords, int64_t C, 
     T.cell_faces.resize(N);
     T.face_cells.assign(2 * F, -1);
     T.face_local.assign(2 * F, 0);
-    T.face_verts.resize(F * dim);
+    T.face_verts.resize(F * fv);
     for (int64_t s = 0; s < N; ++s) {
         const int32_t E = id_of_rep[rep[s]];
         T.cell_faces[s] = E;
@@ -126,9 +159,8 @@ std::string build_topology(int dim, int64_t V, const double* coords, int64_t C, 
         if (T.face_cells[2 * E] < 0) {
             T.face_cells[2 * E] = K;
             T.face_local[2 * E] = e;
-            T.face_verts[E * dim + 0] = fa[s];
-            T.face_verts[E * dim + 1] = fb[s];
-            if (dim == 3) T.face_verts[E * dim + 2] = fc[s];
+            const int32_t fvs[4] = {fa[s], fb[s], fc[s], fd[s]};
+            for (int q = 0; q < fv; ++q) T.face_verts[E * fv + q] = fvs[q];
         }
         else {
             T.face_cells[2 * E + 1] = K;
@@ -146,9 +178,9 @@ std::string build_topology(int dim, int64_t V, const double* coords, int64_t C, 
     T.face_measure.resize(F);
 #pragma omp parallel for schedule(static)
     for (int64_t E = 0; E < F; ++E) {
-        const double* P[3];
-        for (int d = 0; d < dim; ++d) P[d] = coords + (int64_t)T.face_verts[E * dim + d] * dim;
-        T.face_measure[E] = simplex_measure(P, dim - 1, dim);
+        const double* P[4];
+        for (int q = 0; q < fv; ++q) P[q] = coords + (int64_t)T.face_verts[E * fv + q] * dim;
+        T.face_measure[E] = (cell && dim == 3) ? box_face_measure(P) : simplex_measure(P, fv - 1, dim);
     }
     return std::string();
 }
@@ -170,7 +202,7 @@ void build_pattern(const HostTopology& T, int n, const uint8_t* tags, HostPatter
 #pragma omp parallel for schedule(static) reduction(+ : nnz)
     for (int64_t E = 0; E < F; ++E) {
         const int32_t K0 = T.face_cells[2 * E], K1 = T.face_cells[2 * E + 1];
-        int32_t list[8];
+        int32_t list[12];
         int L = 0;
         for (int f = 0; f < nf; ++f) list[L++] = T.cell_faces[(int64_t)K0 * nf + f];
         if (K1 >= 0)
@@ -184,11 +216,11 @@ void build_pattern(const HostTopology& T, int n, const uint8_t* tags, HostPatter
                 if (list[q] == g) return q;
             return 0;
         };
-        uint32_t qm = 0;
-        for (int f = 0; f < nf; ++f) qm |= (uint32_t)pos_of(T.cell_faces[(int64_t)K0 * nf + f]) << (4 * f);
+        uint64_t qm = 0;
+        for (int f = 0; f < nf; ++f) qm |= (uint64_t)pos_of(T.cell_faces[(int64_t)K0 * nf + f]) << (4 * f);
         if (K1 >= 0)
             for (int f = 0; f < nf; ++f)
-                qm |= (uint32_t)pos_of(T.cell_faces[(int64_t)K1 * nf + f]) << (4 * (nf + f));
+                qm |= (uint64_t)pos_of(T.cell_faces[(int64_t)K1 * nf + f]) << (4 * (nf + f));
         P.qmap[E] = qm;
         const int qd = pos_of((int32_t)E);
         P.qdiag[E] = (uint8_t)qd;

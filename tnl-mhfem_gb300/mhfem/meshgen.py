@@ -134,10 +134,24 @@ def face_centroids(coords: np.ndarray, face_verts: np.ndarray) -> np.ndarray:
 
 
 def outward_face_normals(coords: np.ndarray, cells: np.ndarray) -> np.ndarray:
-    """Outward normals scaled by the face measure, [C][nf][dim]: face e of a
-    cell is opposite local vertex e."""
-    C, nf = cells.shape
-    dim = nf - 1
+    """Outward normals scaled by the face measure, [C][nf][dim].  Simplices:
+    face e is opposite local vertex e.  Axis-aligned boxes (2^dim vertices
+    per cell): the faces of the Quadrangle (bottom, right, top, left) and
+    Hexahedron (bottom, front, right, back, left, top) orders."""
+    C, nv = cells.shape
+    dim = coords.shape[1]
+    if nv == 2 ** dim:
+        h = coords[cells[:, 2 if dim == 2 else 6]] - coords[cells[:, 0]]
+        if dim == 2:
+            out = np.zeros((C, 4, 2))
+            out[:, 0, 1] = -h[:, 0]; out[:, 1, 0] = h[:, 1]; out[:, 2, 1] = h[:, 0]; out[:, 3, 0] = -h[:, 1]
+            return out
+        out = np.zeros((C, 6, 3))
+        axy, axz, ayz = h[:, 0] * h[:, 1], h[:, 0] * h[:, 2], h[:, 1] * h[:, 2]
+        out[:, 0, 2] = -axy; out[:, 1, 1] = -axz; out[:, 2, 0] = ayz
+        out[:, 3, 1] = axz; out[:, 4, 0] = -ayz; out[:, 5, 2] = axy
+        return out
+    nf = nv
     X = coords[cells]  # [C][nf][dim]
     out = np.empty((C, nf, dim))
     for e in range(nf):

@@ -16,7 +16,10 @@ i*F + E), the initial cell values and the time stepping.
                   512^2 triangle mesh (lumped mass, explicit upwind);
 * ``diffusion3d`` with N=128 and the mixed form is the large mixed-precision case;
 * ``diffusion3d_source`` adds the time-modulated source
-                  f = 1 + 0.5 sin(2 pi t / T) psi(x) used by the learned form.
+                  f = 1 + 0.5 sin(2 pi t / T) psi(x) used by the learned form;
+* ``heat2d_rect`` / ``diffusion3d_box`` are the heat and diffusion models on
+                  graded rectangles / cuboids (box cells); ``adr2d(box=True)``
+                  the coupled model on rectangles.
 """
 from __future__ import annotations
 
@@ -158,11 +161,12 @@ def diffusion3d_source(N: int = 64, steps: int = 1000, dt: float = 1e-3, tol: fl
 
 
 def adr2d(N: int = 512, steps: int = 200, dt: float = 5e-4, tol: float = 1e-10, seed: int = 1234,
-          field_seed: int = 5678, form: int = L.FORM_FP64) -> Problem:
+          field_seed: int = 5678, form: int = L.FORM_FP64, box: bool = False) -> Problem:
+    """box=True: the same model on N x N graded rectangles."""
     n = 2
-    coords, cells = meshgen.square_triangles(N, 0.2, seed)
+    coords, cells = meshgen.square_rectangles(N) if box else meshgen.square_triangles(N, 0.2, seed)
     C = cells.shape[0]
-    nf = 3
+    nf = 4 if box else 3
     g = meshgen.gaussian_field((N, N), 0.1, field_seed)
     cen = meshgen.cell_centroids(coords, cells)
     gx, gy = meshgen.cell_grid_index(cen, N)
@@ -190,8 +194,9 @@ def adr2d(N: int = 512, steps: int = 200, dt: float = 5e-4, tol: float = 1e-10, 
         return tags.ravel(), np.zeros(n * F), dirichlet.ravel()
 
     cfg = StaticConfig(dim=2, n_eq=2, mass_lumping=True, advection=L.EXPLICIT_UPWIND, mobility_upwind=False,
-                       form=form)
-    return Problem("adr2d", cfg, coords, cells, coeffs, np.zeros(n * C), dt, steps, tol, bc_fn, N)
+                       form=form, cell=L.CELL_BOX if box else L.CELL_SIMPLEX)
+    return Problem("adr2d_rect" if box else "adr2d", cfg, coords, cells, coeffs, np.zeros(n * C), dt, steps, tol,
+                   bc_fn, N)
 
 
 WORKLOADS = {
@@ -199,6 +204,8 @@ WORKLOADS = {
     "diffusion3d": diffusion3d,
     "adr2d": adr2d,
     "diffusion3d_source": diffusion3d_source,
+    "heat2d_rect": heat2d_rect,
+    "diffusion3d_box": diffusion3d_box,
 }
 
 
