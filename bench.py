@@ -54,6 +54,7 @@ def parse_args():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-box", action="store_true", help="skip the cuboid (box cell) leg")
     ap.add_argument("--learned-train", type=int, default=200,
                     help="online training steps of the learned form before its timed steps")
     ap.add_argument("--profile-run", action="store_true",
@@ -184,6 +185,56 @@ def run_reference_arm(args, rank, world):
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def kernel_table(s, L, hbm_peak):
+    """CUDA-event times of the step's kernels (algorithmic bytes / FLOPs from the library)."""
+    out = {}
+    for name, kid, reps in [("cell_local", L.KERNEL_CELL_LOCAL, 20), ("assemble", L.KERNEL_ASSEMBLE, 20),
+                            ("reconstruct", L.KERNEL_RECONSTRUCT, 20), ("spmv_fp64", L.KERNEL_SPMV_FP64, 50)]:
+        r = s.time_kernel(kid, reps=reps)
+        gbs = r["bytes"] / (r["ms"] * 1e-3) / 1e9
+        out[name] = {"ms": r["ms"], "gbs": gbs, "hbm_frac": gbs / hbm_peak,
+                     "fp64_tflops": r["flops"] / (r["ms"] * 1e-3) / 1e12}
+    return out
+
+
+def box_leg(args, dev, world):
+    """The heterogeneous-diffusion model on (2 grid)^3 graded cuboids (box
+    cells: closed-form RT0 inverse, 6 faces per cell, ELL width 10), FP64
+    form, the same warm-up and timed steps as the headline."""
+    import torch
+
+    from mhfem import _lib as L
+    from mhfem import problems
+
+    N = 2 * args.grid
+    p = problems.diffusion3d_box(N=N)
+    p.config.device = dev
+    s = problems.make_solver(p, check_every=8)
+    ext = torch.cuda.ExternalStream(s.stream(), device=dev)
+    t = 0.0
+    for _ in range(args.warmup):
+        s.step(t, p.dt)
+        t += p.dt
+    it0, _, _ = s.totals()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(ext)
+    for _ in range(args.steps):
+        s.step(t, p.dt)
+        t += p.dt
+    e1.record(ext)
+    e1.synchronize()
+    el = max_over_ranks(e0.elapsed_time(e1), world)
+    it1, _, _ = s.totals()
+    hbm_peak, _ = measured_peaks()
+    out = {"workload": f"diffusion3d_box_{N}", "cells": s.C, "faces": s.F, "tol": p.tol, "dt": p.dt,
+           "value": world * args.steps / (el / 1e3), "unit": UNIT, "ms_per_step": el / args.steps,
+           "iterations_per_step": (it1 - it0) / args.steps, "kernels": kernel_table(s, L, hbm_peak)}
+    s.close()
+    return out
 
 
 def learned_leg(args, dev, world):
@@ -392,13 +443,7 @@ def main():
     hbm_peak, peak_kind = measured_peaks()
     spmv = s.time_kernel(L.KERNEL_SPMV_FP64, reps=50)
     achieved = spmv["bytes"] / (spmv["ms"] * 1e-3) / 1e9
-    kernels = {}
-    for name, kid in [("cell_local", L.KERNEL_CELL_LOCAL), ("assemble", L.KERNEL_ASSEMBLE),
-                      ("reconstruct", L.KERNEL_RECONSTRUCT)]:
-        r = s.time_kernel(kid, reps=20)
-        kernels[name] = {"ms": r["ms"], "gbs": r["bytes"] / (r["ms"] * 1e-3) / 1e9,
-                         "hbm_frac": r["bytes"] / (r["ms"] * 1e-3) / 1e9 / hbm_peak,
-                         "fp64_tflops": r["flops"] / (r["ms"] * 1e-3) / 1e12}
+    kernels = kernel_table(s, L, hbm_peak)
     kernels["spmv_fp64"] = {"ms": spmv["ms"], "gbs": achieved, "hbm_frac": achieved / hbm_peak,
                             "fp64_tflops": spmv["flops"] / (spmv["ms"] * 1e-3) / 1e12}
     traffic = None
@@ -471,6 +516,9 @@ def main():
 
     if not args.no_learned:
         forms["learned"] = learned_leg(args, dev, world)
+    other_cells = None
+    if not args.no_box:
+        other_cells = {"cuboids": box_leg(args, dev, world)}
 
     e2e = None
     if not args.no_e2e:
@@ -525,6 +573,7 @@ def main():
                      "peak_kind": peak_kind, "bytes_per_launch": spmv["bytes"], "ms_per_launch": spmv["ms"]},
         "kernels": kernels,
         "forms": forms,
+        "other_cells": other_cells,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": gpu_launches,

@@ -22,8 +22,8 @@ diffusivity = 1e-3
 """
 
 
-def _write_case(tmp_path, N=6):
-    coords, cells = meshgen.square_triangles(N)
+def _write_case(tmp_path, N=6, box=False):
+    coords, cells = meshgen.square_rectangles(N) if box else meshgen.square_triangles(N)
     vtkio.write_vtu(tmp_path / "mesh.vtu", coords, cells, {})
     assert init.main(["--mesh", str(tmp_path / "mesh.vtu"), "--output", str(tmp_path / "initial.vtu"),
                       "--output-boundary", str(tmp_path / "boundary.bcs")]) == 0
@@ -75,12 +75,19 @@ def test_init_matches_reference_formula(tmp_path):
     assert b.dofSize == 3 * 36 + 2 * 6 and np.all(b.tags == 0)
 
 
+def test_init_counts_box_faces(tmp_path):
+    _write_case(tmp_path, N=6, box=True)
+    b = bcstorage.BoundaryConditionsStorage.load(tmp_path / "boundary.bcs")
+    assert b.dofSize == 2 * 6 * 7
+
+
 @pytest.mark.gpu
-def test_driver_end_to_end(tmp_path):
+@pytest.mark.parametrize("box", [False, True])
+def test_driver_end_to_end(tmp_path, box):
     from mhfem import problems, run
     from oracle.oracle import OracleModel
 
-    coords, cells = _write_case(tmp_path)
+    coords, cells = _write_case(tmp_path, box=box)
     rc = run.main(["--config", str(tmp_path / "config.ini"), "--log-file", str(tmp_path / "log.txt"),
                    "--verbose", "0"])
     assert rc == 0
@@ -88,11 +95,12 @@ def test_driver_end_to_end(tmp_path):
     files = sorted(out.glob("data_*.vtu"))
     assert [f.name for f in files] == [f"data_{k:05d}.vtu" for k in range(4)]
     log = (tmp_path / "log.txt").read_text()
+    assert ("rectangles" if box else "triangles") in log
     assert "Total number of time steps:" in log and "Total number of linear solver iterations:" in log
     z_gpu = vtkio.read_cell_data(files[-1], "Z")
     # the same model through the oracle: heat equation, D = 1e-3, dt = 5e-4, 6 steps
     z0 = vtkio.read_cell_data(tmp_path / "initial.vtu", "InitialCondition[Z0]")
-    p = problems.heat2d(N=6)
+    p = problems.heat2d_rect(N=6) if box else problems.heat2d(N=6)
     p.coords, p.cells, p.Z0 = coords, cells, z0
     p.coeffs["D"] = 1e-3
     m = OracleModel.from_problem(p)

@@ -145,6 +145,41 @@ def test_adr2d_full_size():
     s.close()
 
 
+def test_box_full_size():
+    """Box cells at full size: 128^2 graded rectangles (3 steps) and 64^3
+    graded cuboids (2 steps) against the oracle; the pattern bit-exact."""
+    for p in (problems.heat2d_rect(N=128, steps=3), problems.diffusion3d_box(N=64, steps=2)):
+        s, m = _pair(p, check_every=8)
+        t = 0.0
+        for _ in range(p.steps):
+            s.step(t, p.dt)
+            m.step(t, p.dt, 1e-13)
+            t += p.dt
+        zf, zk = s.state()
+        assert rel_err(zf, m.Z_iF) < TOL_STATE, p.name
+        assert rel_err(zk, m.Z_iK) < TOL_STATE, p.name
+        rowptr, cols, _, _ = s.system()
+        assert np.array_equal(rowptr, m.rowptr) and np.array_equal(cols, m.cols)
+        s.close()
+
+
+def test_mixed_box():
+    """Mixed precision on 32^3 cuboids: error against the FP64 oracle."""
+    p = problems.diffusion3d_box(N=32, steps=3, form=L.FORM_MIXED)
+    s = problems.make_solver(p)
+    m = OracleModel.from_problem(p)
+    t = 0.0
+    for _ in range(p.steps):
+        st = s.step(t, p.dt)
+        m.step(t, p.dt, 1e-13)
+        assert st["sweeps"] >= 1 and st["residual"] < p.tol
+        t += p.dt
+    zf, zk = s.state()
+    assert rel_err(zf, m.Z_iF) < 1e-8
+    assert rel_err(zk, m.Z_iK) < 1e-8
+    s.close()
+
+
 def test_mixed_128_cube():
     """Mixed precision on the 128^3 cube (12,582,912 tetrahedra, 25,264,128
     faces), where the CPU oracle is too slow: 2 steps at tol 1e-12, face
@@ -223,3 +258,22 @@ def test_nan_coefficient_is_reported():
         s.step(0.0, p.dt)
     assert ei.value.status in (L.ERR_NONPOSITIVE_DIAGONAL, L.ERR_NOT_FINITE)
     s.close()
+
+
+def test_box_vertex_order_is_checked():
+    """Box cells must be axis-aligned with their vertices counterclockwise from
+    the lowest corner (the closed-form mass matrix reads the side lengths and
+    face orientations from that order): another order is refused at
+    mhfem_set_mesh with an error, not solved wrongly."""
+    from mhfem import meshgen
+    from mhfem.solver import Solver, StaticConfig
+
+    for dim in (2, 3):
+        coords, cells = meshgen.square_rectangles(4) if dim == 2 else meshgen.cube_cuboids(3)
+        rot = [1, 2, 3, 0] if dim == 2 else [1, 2, 3, 0, 5, 6, 7, 4]
+        s = Solver(StaticConfig(dim=dim, n_eq=1, cell=L.CELL_BOX))
+        with pytest.raises(L.MhfemError) as ei:
+            s.setMesh(coords, cells[:, rot])
+        assert ei.value.status == L.ERR_INVALID_ARGUMENT
+        s.setMesh(coords, cells)  # the canonical order is accepted
+        s.close()

@@ -41,6 +41,30 @@ def test_create_without_device_fails_loudly():
     assert lib.mhfem_create(ct.byref(desc), ct.byref(h)) == L.ERR_NO_DEVICE
 
 
+def test_create_validates_the_cell_type():
+    """An unknown cell type is an invalid argument; box cells with the learned
+    form (whose face features are defined for simplices) are unsupported.
+    Both are refused before any device is touched."""
+    lib = L.load()
+    h = ct.c_void_p()
+    bad = L.Desc(3, 1, 0, 0, 0, L.FORM_FP64, 0, 7)
+    assert lib.mhfem_create(ct.byref(bad), ct.byref(h)) == L.ERR_INVALID_ARGUMENT
+    learned_box = L.Desc(3, 1, 0, 0, 0, L.FORM_LEARNED, 0, L.CELL_BOX)
+    assert lib.mhfem_create(ct.byref(learned_box), ct.byref(h)) == L.ERR_UNSUPPORTED
+
+
+def test_box_mesh_counts():
+    for dim, N in ((2, 5), (3, 4)):
+        coords, cells = meshgen.square_rectangles(N) if dim == 2 else meshgen.cube_cuboids(N)
+        assert cells.shape == (N ** dim, 2 ** dim)
+        fv, fc, cf = build_faces(dim, cells, L.CELL_BOX)
+        assert fc.shape[0] == dim * N ** (dim - 1) * (N + 1)
+        assert fv.shape[1] == 2 ** (dim - 1)
+        h = coords[cells[:, 2 if dim == 2 else 6]] - coords[cells[:, 0]]
+        assert np.all(h > 0)  # v0 is the lowest corner, the opposite corner the highest
+        assert abs(np.prod(h, axis=1).sum() - 1.0) < 1e-12
+
+
 @pytest.mark.parametrize("N", [1, 3, 8])
 def test_triangle_mesh_counts(N):
     coords, cells = meshgen.square_triangles(N)

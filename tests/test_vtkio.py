@@ -4,11 +4,18 @@ import pytest
 
 from mhfem import meshgen, vtkio
 
+MESHES = {
+    "triangles": lambda: meshgen.square_triangles(5),
+    "tetrahedra": lambda: meshgen.cube_tetrahedra(3),
+    "rectangles": lambda: meshgen.square_rectangles(5),
+    "cuboids": lambda: meshgen.cube_cuboids(3),
+}
+
 
 @pytest.mark.parametrize("compress", [True, False])
-@pytest.mark.parametrize("dim", [2, 3])
-def test_vtu_roundtrip(tmp_path, dim, compress):
-    coords, cells = meshgen.square_triangles(5) if dim == 2 else meshgen.cube_tetrahedra(3)
+@pytest.mark.parametrize("kind", sorted(MESHES))
+def test_vtu_roundtrip(tmp_path, kind, compress):
+    coords, cells = MESHES[kind]()
     z = np.random.default_rng(0).standard_normal(cells.shape[0])
     f = tmp_path / "m.vtu"
     vtkio.write_vtu(f, coords, cells, {"InitialCondition[Z0]": z, "Z": 2 * z}, time=0.5, cycle=3,
@@ -21,10 +28,44 @@ def test_vtu_roundtrip(tmp_path, dim, compress):
         vtkio.read_cell_data(f, "missing")
 
 
-@pytest.mark.parametrize("dim", [2, 3])
-def test_legacy_vtk_roundtrip(tmp_path, dim):
-    coords, cells = meshgen.square_triangles(4) if dim == 2 else meshgen.cube_tetrahedra(2)
+@pytest.mark.parametrize("kind", sorted(MESHES))
+def test_legacy_vtk_roundtrip(tmp_path, kind):
+    coords, cells = MESHES[kind]()
     f = tmp_path / "m.vtk"
     vtkio.write_legacy_vtk(f, coords, cells)
     c2, k2 = vtkio.read_mesh(f)
     assert np.allclose(c2, coords, rtol=0, atol=1e-15) and np.array_equal(k2, cells)
+
+
+def _legacy_with_types(path, coords, cells, ctype):
+    pts = np.zeros((coords.shape[0], 3))
+    pts[:, :coords.shape[1]] = coords
+    C, nv = cells.shape
+    with open(path, "w") as fh:
+        fh.write("# vtk DataFile Version 2.0\nt\nASCII\nDATASET UNSTRUCTURED_GRID\n")
+        fh.write(f"POINTS {pts.shape[0]} double\n")
+        np.savetxt(fh, pts, fmt="%.17g")
+        fh.write(f"CELLS {C} {C * (nv + 1)}\n")
+        np.savetxt(fh, np.hstack([np.full((C, 1), nv), cells]), fmt="%d")
+        fh.write(f"CELL_TYPES {C}\n")
+        np.savetxt(fh, np.full((C, 1), ctype), fmt="%d")
+
+
+@pytest.mark.parametrize("kind", ["rectangles", "cuboids"])
+def test_pixels_and_voxels_take_the_box_vertex_order(tmp_path, kind):
+    """VTK pixels / voxels number their corners lexicographically; the reader
+    returns them in the quadrilateral / hexahedron order the box cells use."""
+    coords, cells = MESHES[kind]()
+    lex = [0, 1, 3, 2] if kind == "rectangles" else [0, 1, 3, 2, 4, 5, 7, 6]
+    f = tmp_path / "p.vtk"
+    _legacy_with_types(f, coords, cells[:, lex], vtkio.VTK_PIXEL if kind == "rectangles" else vtkio.VTK_VOXEL)
+    c2, k2 = vtkio.read_mesh(f)
+    assert np.array_equal(k2, cells)
+
+
+def test_mixed_cell_kinds_are_refused(tmp_path):
+    coords, cells = meshgen.square_triangles(2)
+    f = tmp_path / "x.vtk"
+    _legacy_with_types(f, coords, cells, vtkio.VTK_QUAD)  # 3 vertices declared as quadrilaterals
+    with pytest.raises(ValueError):
+        vtkio.read_mesh(f)

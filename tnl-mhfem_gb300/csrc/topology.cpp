@@ -108,6 +108,37 @@ std::string build_topology(int dim, int cell, int64_t V, const double* coords, i
         }
     for (int64_t s = 0; s < N; ++s)
         if (fa[s] == -2) return "degenerate cell (repeated vertex)";
+    if (cell) {
+        // The closed-form box mass matrix takes the side lengths from v0 to
+        // v2 / v6 and the orientation of face e from the vertex order, so
+        // a box must be axis-aligned with its vertices in that order:
+        // vertex q sits at v0 + (bit 0 of q^(q>>1)) hx ex + (bit 1 of q) hy ey
+        // + (bit 2 of q) hz ez, all h > 0.
+        int64_t bad_cell = -1;
+#pragma omp parallel for schedule(static) reduction(max : bad_cell)
+        for (int64_t K = 0; K < C; ++K) {
+            const double* x0 = coords + (int64_t)cell_verts[K * nv] * dim;
+            const double* xo = coords + (int64_t)cell_verts[K * nv + nv - 2] * dim;  // v2 / v6
+            double h[3] = {0, 0, 0}, ext = 0;
+            for (int d = 0; d < dim; ++d) {
+                h[d] = xo[d] - x0[d];
+                ext = std::max(ext, std::fabs(h[d]));
+            }
+            bool ok = true;
+            for (int d = 0; d < dim; ++d) ok = ok && h[d] > 0;
+            for (int q = 0; q < nv && ok; ++q) {
+                const int bits[3] = {(q ^ (q >> 1)) & 1, (q >> 1) & 1, (q >> 2) & 1};
+                const double* xq = coords + (int64_t)cell_verts[K * nv + q] * dim;
+                for (int d = 0; d < dim; ++d)
+                    if (std::fabs(xq[d] - x0[d] - bits[d] * h[d]) > 1e-12 * ext) ok = false;
+            }
+            if (!ok) bad_cell = std::max(bad_cell, K);
+        }
+        if (bad_cell >= 0)
+            return "box cell " + std::to_string(bad_cell) +
+                   " is not axis-aligned with its vertices counterclockwise from the lowest corner "
+                   "(bottom face before the top face)";
+    }
 
     std::vector<int64_t> start(V + 1, 0);
     for (int64_t s = 0; s < N; ++s) start[fa[s] + 1]++;

@@ -30,10 +30,8 @@ def boundary_condition(num_faces: int) -> BoundaryConditionsStorage:
     return bcs
 
 
-def count_faces(cells: np.ndarray) -> int:
-    nf = cells.shape[1]
-    f = np.sort(np.stack([np.delete(cells, e, axis=1) for e in range(nf)], axis=1).reshape(-1, nf - 1), axis=1)
-    return int(np.unique(f, axis=0).shape[0])
+def count_faces(cells: np.ndarray, box: bool = False) -> int:
+    return meshgen.count_faces(cells, box)
 
 
 def main(argv=None) -> int:
@@ -50,7 +48,7 @@ def main(argv=None) -> int:
     coords, cells = load_mesh(a.mesh, "auto", Path("."))
     ic = initial_condition(coords, cells, a.alpha, a.beta, a.gamma)
     vtkio.write_vtu(a.output, coords, cells, {"InitialCondition[Z0]": ic}, cycle=0)
-    boundary_condition(count_faces(cells)).save(a.output_boundary)
+    boundary_condition(count_faces(cells, meshgen.is_box_mesh(coords, cells))).save(a.output_boundary)
     return 0
 
 

@@ -104,6 +104,29 @@ def cube_cuboids(N: int, graded: bool = True):
     return coords, cells
 
 
+# local vertices of the faces of a rectangle / cuboid (TNL Quadrangle and
+# Hexahedron subentity order)
+BOX_FACES = {2: [[0, 1], [1, 2], [2, 3], [3, 0]],
+             3: [[0, 1, 2, 3], [0, 1, 5, 4], [1, 2, 6, 5], [2, 3, 7, 6], [3, 0, 4, 7], [4, 5, 6, 7]]}
+
+
+def is_box_mesh(coords: np.ndarray, cells: np.ndarray) -> bool:
+    """2^dim vertices per cell: rectangles / cuboids (else simplices)."""
+    return cells.shape[1] == 2 ** coords.shape[1]
+
+
+def count_faces(cells: np.ndarray, box: bool = False) -> int:
+    """Number of distinct faces (sorted vertex tuples) of a conforming mesh."""
+    nv = cells.shape[1]
+    if box:
+        dim = 2 if nv == 4 else 3
+        f = np.stack([cells[:, q] for q in BOX_FACES[dim]], axis=1)
+    else:
+        f = np.stack([np.delete(cells, e, axis=1) for e in range(nv)], axis=1)
+    f = np.sort(f.reshape(-1, f.shape[-1]), axis=1)
+    return int(np.unique(f, axis=0).shape[0])
+
+
 def gaussian_field(shape, corr_length: float = 0.1, seed: int = 5678) -> np.ndarray:
     """Zero-mean, unit-variance Gaussian random field on a periodic grid of
     the unit square/cube, with Gaussian covariance of the given correlation

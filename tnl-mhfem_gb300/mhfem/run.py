@@ -14,7 +14,9 @@ It mirrors the reference's command line and control flow:
 The model is the heat equation of examples/HeatEquation (N = 1, D =
 `diffusivity`, all other coefficients 0, constant mobility).  The mesh key
 also accepts ``synthetic:square:N`` and ``synthetic:cube:N`` for the jittered
-meshes of mhfem.meshgen.  `--exec cuda` is the only execution mode.  The
+simplex meshes of mhfem.meshgen, and ``synthetic:rect:N`` / ``synthetic:cuboid:N``
+for its graded box meshes; meshes of quadrilaterals / hexahedra (2^dim
+vertices per cell) run with box cells.  `--exec cuda` is the only execution mode.  The
 library has no CPU implementation, so `--exec host` is refused.
 """
 from __future__ import annotations
@@ -40,7 +42,11 @@ def load_mesh(spec: str, fmt: str, base: Path):
             return meshgen.square_triangles(int(n))
         if kind == "cube":
             return meshgen.cube_tetrahedra(int(n))
-        raise ValueError(f"unknown synthetic mesh {kind!r} (square, cube)")
+        if kind == "rect":
+            return meshgen.square_rectangles(int(n))
+        if kind == "cuboid":
+            return meshgen.cube_cuboids(int(n))
+        raise ValueError(f"unknown synthetic mesh {kind!r} (square, cube, rect, cuboid)")
     return vtkio.read_mesh(base / spec, fmt)
 
 
@@ -72,9 +78,10 @@ def run(cfg: config.Config, log: Logger, device: int = 0) -> dict:
     out_dir.mkdir(parents=True, exist_ok=True)
     coords, cells = load_mesh(cfg["mesh"], cfg["mesh-format"], base)
     dim = coords.shape[1]
+    box = meshgen.is_box_mesh(coords, cells)
     static = StaticConfig(dim=dim, n_eq=1, mass_lumping=cfg["mass-lumping"] == "enabled",
                           advection=L.EXPLICIT_UPWIND, mobility_upwind=False, form=FORMS[cfg["solver-form"]],
-                          device=device)
+                          device=device, cell=L.CELL_BOX if box else L.CELL_SIMPLEX)
     s = Solver(static)
     s.setMesh(coords, cells)
     # heat-equation model coefficients (HeatEquationModel.h:114-133)
@@ -104,7 +111,8 @@ def run(cfg: config.Config, log: Logger, device: int = 0) -> dict:
     log.param("Device type:", "CUDA (sm_103a)")
     log.param("Real type:", "double")
     log.param("Index type:", "int")
-    log.param("Mesh type:", "triangles" if dim == 2 else "tetrahedra")
+    log.param("Mesh type:", ("rectangles" if dim == 2 else "cuboids") if box else
+              ("triangles" if dim == 2 else "tetrahedra"))
     log.param("Sparse matrix:", "ELL (off-diagonal part, unit diagonal)")
     log.param("Mass lumping:", cfg["mass-lumping"])
     log.param("Advection discretization:", "explicit upwind")

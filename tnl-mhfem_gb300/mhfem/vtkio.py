@@ -3,8 +3,11 @@
 * ``read_mesh(path)``: legacy VTK (``.vtk``, ASCII or binary
   UNSTRUCTURED_GRID) or XML VTU (``.vtu``, ascii / base64 binary / raw
   appended data, optionally zlib-compressed), as TNL's mesh readers accept
-  them (control.h:20-47, configSetup.h:16-21).  Triangle (VTK type 5) and
-  tetrahedron (10) cells.
+  them (control.h:20-47, configSetup.h:16-21).  Triangle (VTK type 5),
+  tetrahedron (10), quadrilateral (9) and hexahedron (12) cells, and the
+  axis-aligned pixel (8) and voxel (11) cells, whose vertices are reordered
+  into the quadrilateral / hexahedron order (VTK numbers a pixel's corners
+  in lexicographic order, a quadrilateral's counterclockwise).
 * ``read_cell_data(path, name)``: a cell array from a VTU file, e.g. the
   initial condition ``InitialCondition[Z0]`` (Solver.hpp:296-306).
 * ``write_vtu(path, coords, cells, cell_data, ...)``: the snapshot files
@@ -24,17 +27,49 @@ import numpy as np
 
 VTK_TRIANGLE = 5
 VTK_TETRA = 10
+VTK_PIXEL = 8
+VTK_QUAD = 9
+VTK_VOXEL = 11
+VTK_HEXAHEDRON = 12
+# (dimension, vertices per cell, order into the quadrilateral / hexahedron numbering) per cell type
+_CELL_TYPES = {VTK_TRIANGLE: (2, 3, None), VTK_TETRA: (3, 4, None), VTK_QUAD: (2, 4, None),
+               VTK_HEXAHEDRON: (3, 8, None), VTK_PIXEL: (2, 4, [0, 1, 3, 2]),
+               VTK_VOXEL: (3, 8, [0, 1, 3, 2, 4, 5, 7, 6])}
 _NP_OF = {"Float32": np.float32, "Float64": np.float64, "Int8": np.int8, "UInt8": np.uint8, "Int16": np.int16,
           "UInt16": np.uint16, "Int32": np.int32, "UInt32": np.uint32, "Int64": np.int64, "UInt64": np.uint64}
 _VTK_OF = {np.dtype(v).str[1:]: k for k, v in _NP_OF.items()}
 
 
-def _mesh_dim(coords3: np.ndarray, types: np.ndarray) -> int:
-    if np.all(types == VTK_TETRA):
-        return 3
-    if np.all(types == VTK_TRIANGLE):
-        return 2
-    raise ValueError("only meshes of triangles (VTK 5) or tetrahedra (VTK 10) are supported")
+def _cells_of(types: np.ndarray, conn: np.ndarray):
+    """Dimension and the [C][nv] cell array of a mesh of one cell kind
+    (pixels / voxels reordered into the quadrilateral / hexahedron order)."""
+    types = np.asarray(types)
+    kinds = set(int(t) for t in np.unique(types))
+    if not kinds or not kinds <= set(_CELL_TYPES):
+        raise ValueError("supported cells: triangles (VTK 5), tetrahedra (10), quadrilaterals (9), "
+                         "hexahedra (12), pixels (8), voxels (11)")
+    shapes = {_CELL_TYPES[k][:2] for k in kinds}
+    if len(shapes) != 1:
+        raise ValueError("mixed cell kinds are not supported")
+    dim, nv = shapes.pop()
+    conn = np.asarray(conn, np.int64)
+    if conn.size != types.size * nv:
+        raise ValueError(f"connectivity does not match the cell types ({nv} vertices per cell)")
+    cells = conn.reshape(-1, nv).copy()
+    for k in kinds:
+        order = _CELL_TYPES[k][2]
+        if order is not None:
+            sel = types == k
+            cells[sel] = cells[sel][:, order]
+    return dim, cells
+
+
+def _cell_type(dim: int, nv: int) -> int:
+    if nv == dim + 1:
+        return VTK_TRIANGLE if dim == 2 else VTK_TETRA
+    if nv == 2 ** dim:
+        return VTK_QUAD if dim == 2 else VTK_HEXAHEDRON
+    raise ValueError(f"no VTK cell with {nv} vertices in {dim}D")
 
 
 # ---- legacy VTK -------------------------------------------------------------
@@ -86,19 +121,22 @@ def _read_legacy(path: Path):
         elif head == "CELLS":
             ncell, size = int(key[1]), int(key[2])
             raw = read_values(size, "i4").astype(np.int64)
-            conn, q = [], 0
+            conn, sizes, q = [], [], 0
             for _ in range(ncell):
                 k = int(raw[q])
                 conn.append(raw[q + 1:q + 1 + k])
+                sizes.append(k)
                 q += 1 + k
-            cells = conn
+            if len(set(sizes)) > 1:
+                raise ValueError("mixed cell sizes are not supported")
+            cells = np.concatenate(conn) if conn else np.zeros(0, np.int64)
         elif head == "CELL_TYPES":
             types = read_values(int(key[1]), "i4")
             break
     if coords is None or cells is None or types is None:
         raise ValueError(f"{path}: POINTS, CELLS or CELL_TYPES missing")
-    dim = _mesh_dim(coords, types)
-    return coords[:, :dim].copy(), np.array(cells, dtype=np.int32)
+    dim, cells = _cells_of(types, cells)
+    return coords[:, :dim].copy(), cells.astype(np.int32)
 
 
 # ---- VTU ------------------------------------------------------------------------
@@ -181,9 +219,9 @@ def _read_vtu(path: Path):
     conn = v.named("Cells", "connectivity").astype(np.int64)
     offs = v.named("Cells", "offsets").astype(np.int64)
     types = v.named("Cells", "types").astype(np.int64)
-    dim = _mesh_dim(pts, types)
-    cells = conn.reshape(-1, dim + 1)
-    if not np.array_equal(offs, np.arange(1, cells.shape[0] + 1) * (dim + 1)):
+    dim, cells = _cells_of(types, conn)
+    nv = cells.shape[1]
+    if not np.array_equal(offs, np.arange(1, cells.shape[0] + 1) * nv):
         raise ValueError("mixed cell sizes are not supported")
     return pts[:, :dim].copy(), cells.astype(np.int32)
 
@@ -215,7 +253,7 @@ def write_vtu(path, coords: np.ndarray, cells: np.ndarray, cell_data: dict, time
     dim = coords.shape[1]
     pts = np.zeros((coords.shape[0], 3))
     pts[:, :dim] = coords
-    ctype = VTK_TRIANGLE if nv == 3 else VTK_TETRA
+    ctype = _cell_type(dim, nv)
     arrays = []  # (section, name, ncomp, ndarray)
     arrays.append(("Points", "Points", 3, pts.ravel()))
     arrays.append(("Cells", "connectivity", 1, cells.ravel()))
@@ -269,7 +307,7 @@ def write_legacy_vtk(path, coords: np.ndarray, cells: np.ndarray) -> None:
     C, nv = cells.shape
     pts = np.zeros((coords.shape[0], 3))
     pts[:, :coords.shape[1]] = coords
-    ctype = VTK_TRIANGLE if nv == 3 else VTK_TETRA
+    ctype = _cell_type(coords.shape[1], nv)
     with open(path, "w") as fh:
         fh.write("# vtk DataFile Version 2.0\nmhfem mesh\nASCII\nDATASET UNSTRUCTURED_GRID\n")
         fh.write(f"POINTS {pts.shape[0]} double\n")
