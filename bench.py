@@ -262,26 +262,39 @@ def learned_leg(args, dev, world):
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     zf, zk = sl.state()
-    pf = problems.diffusion3d_source(N=args.grid, steps=total, form=L.FORM_FP64)
-    pf.config.device = dev
-    sf = problems.make_solver(pf, check_every=8)
-    sf.setInitialCondition(zk, zf)
+
+    def from_state(form):
+        q = problems.diffusion3d_source(N=args.grid, steps=total, form=form)
+        q.config.device = dev
+        sq = problems.make_solver(q, check_every=8)
+        sq.setInitialCondition(zk, zf)
+        return sq
+
+    sf = from_state(L.FORM_FP64)
+    # the trained network in a second learned solver whose solve from the
+    # guess is the mixed-precision refinement; the plain mixed form beside it
+    slm = from_state(L.FORM_LEARNED)
+    slm.learned_options(train_steps=0, mixed_solve=True)
+    slm.set_learned_params(sl.learned_params())
+    smx = from_state(L.FORM_MIXED)
+    arms = (("learned", sl), ("fp64", sf), ("learned_mixed", slm), ("mixed", smx))
     for _ in range(args.warmup):
-        sl.step(t, pl.dt)
-        sf.step(t, pf.dt)
+        for _, sol in arms:
+            sol.step(t, pl.dt)
         t += pl.dt
     res = {}
-    for name, sol in (("learned", sl), ("fp64", sf)):
+    for name, sol in arms:
         ext = torch.cuda.ExternalStream(sol.stream(), device=dev)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         tt = t
-        its, used, rg, rw = [], 0, [], []
+        its, used, rg, rw, sw = [], 0, [], [], []
         torch.cuda.synchronize()
         e0.record(ext)
         for _ in range(args.steps):
             st = sol.step(tt, pl.dt)
             its.append(st["iterations"])
+            sw.append(st["sweeps"])
             used += st["guess_used"]
             if st["guess_residual"] > 0:
                 rg.append(st["guess_residual"])
@@ -290,15 +303,17 @@ def learned_leg(args, dev, world):
         e1.record(ext)
         e1.synchronize()
         res[name] = {"ms": e0.elapsed_time(e1) / args.steps, "iters": float(np.mean(its)), "used": used,
+                     "sweeps": float(np.mean(sw)), "state": sol.state()[0],
                      "its": [int(v) for v in its],
                      "guess_res": float(np.exp(np.mean(np.log(rg)))) if rg else None,
                      "warm_res": float(np.exp(np.mean(np.log(rw)))) if rw else None}
-    zl, _ = sl.state()
-    zp, _ = sf.state()
-    err = float(np.abs(zl - zp).max() / max(np.abs(zp).max(), 1e-300))
+    zp = res["fp64"]["state"]
+    rel = lambda a: float(np.abs(a - zp).max() / max(np.abs(zp).max(), 1e-300))
+    err = rel(res["learned"]["state"])
     status = sl.learned_status()
-    sl.close()
-    sf.close()
+    for _, sol in arms:
+        sol.close()
+    lm, mx = res["learned_mixed"], res["mixed"]
     return {"value": world * 1e3 / res["learned"]["ms"], "ms_per_step": res["learned"]["ms"],
             "workload": f"diffusion3d_source_{args.grid} (f = 1 + 0.5 sin(2 pi t/T) psi, T = 1000 dt)",
             "fp64_same_steps": {"value": world * 1e3 / res["fp64"]["ms"], "ms_per_step": res["fp64"]["ms"],
@@ -314,7 +329,17 @@ def learned_leg(args, dev, world):
             "train_steps": args.learned_train, "train_seconds": train_s,
             "train_phase_iterations_per_step": float(np.mean(train_iters)) if train_iters else None,
             "final_training_loss": status["last_loss"],
-            "rel_err_face_traces_vs_fp64": err}
+            "rel_err_face_traces_vs_fp64": err,
+            # the same network, its guess followed by the mixed-precision refinement
+            "with_mixed_solve": {
+                "value": world * 1e3 / lm["ms"], "ms_per_step": lm["ms"],
+                "speedup_vs_fp64": res["fp64"]["ms"] / lm["ms"],
+                "inner_fp32_iterations_per_step": lm["iters"], "sweeps_per_step": lm["sweeps"],
+                "guess_accepted_steps": lm["used"], "rel_err_face_traces_vs_fp64": rel(lm["state"]),
+                "mixed_form_same_steps": {"value": world * 1e3 / mx["ms"], "ms_per_step": mx["ms"],
+                                          "speedup_vs_fp64": res["fp64"]["ms"] / mx["ms"],
+                                          "inner_fp32_iterations_per_step": mx["iters"],
+                                          "sweeps_per_step": mx["sweeps"]}}}
 
 
 def profile_other_form(args, dev):

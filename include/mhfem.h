@@ -243,10 +243,12 @@ mhfem_status mhfem_time_kernel(mhfem_t h, int32_t kernel, int32_t reps, double* 
  * No counterpart in the reference: a message-passing network over the face
  * adjacency graph (3 layers, hidden width 64, BF16 weights, FP32
  * accumulation on the tensor cores) predicts the initial guess of each
- * FP64 BiCGStab solve.  The guess is used only when its relative residual is
- * below the previous-step warm start's; the solve always runs to the same
+ * solve (FP64 BiCGStab, or with `mixed_solve` the mixed-precision
+ * refinement).  The guess is used only when its relative residual is below
+ * the previous-step warm start's; the solve always runs to the same FP64
  * tolerance.  The network is trained online on the first `train_steps`
- * steps.  Only n_eq = 1 is supported. */
+ * steps, or takes parameters from mhfem_learned_set_params.  Only n_eq = 1
+ * and simplex cells are supported. */
 typedef struct {
     int32_t train_steps;          /* online training steps (default 200)            */
     int32_t train_iters;          /* Adam iterations per training step (default 2)  */
@@ -256,6 +258,11 @@ typedef struct {
     double  lr_final;             /* learning rate at the last training step, as a
                                      fraction of learning_rate, reached by a cosine
                                      decay over the training steps (1: constant)     */
+    int32_t mixed_solve;          /* 1: solve from the guess with the mixed-precision
+                                     refinement of MHFEM_FORM_MIXED (FP32 inner
+                                     BiCGStab, FP64 residuals, the same FP64
+                                     tolerance) instead of FP64 BiCGStab; the handle
+                                     then also keeps the FP32 copy of the matrix      */
 } mhfem_learned_opts;
 
 #define MHFEM_LEARNED_FEATURES 16
@@ -263,6 +270,8 @@ mhfem_status mhfem_learned_set_options(mhfem_t h, const mhfem_learned_opts* opts
 /* FP32 master parameters, flat: W0 [16][64], b0 [64], then W_l [128][64], b_l [64]
  * for l = 1..3, then wd [64], bd [1]. */
 mhfem_status mhfem_learned_get_params(mhfem_t h, float* params, int64_t count);
+/* Parameters from elsewhere (e.g. a network trained on an earlier run of the
+ * same model): the guess is tried from the next step on, trained or not. */
 mhfem_status mhfem_learned_set_params(mhfem_t h, const float* params, int64_t count);
 /* Network output for given features [F][16] on the handle's face graph. */
 mhfem_status mhfem_learned_forward(mhfem_t h, const float* features, float* out);

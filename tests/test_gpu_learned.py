@@ -134,3 +134,55 @@ def test_learned_warm_start_reduces_iterations():
     assert np.mean(it_l) < 0.9 * np.mean(it_f), (np.mean(it_l), np.mean(it_f))
     sl.close()
     sf.close()
+
+
+def test_learned_guess_with_mixed_solve():
+    """A network trained on one solver, loaded into a second one whose solve
+    from the guess is the mixed-precision refinement: the guess is used, the
+    FP64 residual meets the tolerance in every step, the traces agree with
+    the plain FP64 form, and the inner FP32 iterations fall below those of
+    the mixed form started from the previous step."""
+    N, train, use = 12, 40, 12
+    src = (0.5, 60 * 1e-3)
+    pl = problems.diffusion3d_source(N=N, steps=train + use, form=L.FORM_LEARNED)
+    pl.source = src
+    sl = problems.make_solver(pl)
+    sl.learned_options(train_steps=train, train_iters=4, learning_rate=2e-3)
+    t = 0.0
+    for _ in range(train):
+        sl.step(t, pl.dt)
+        t += pl.dt
+    zf0, zk0 = sl.state()
+    params = sl.learned_params()
+    sl.close()
+
+    def make(form):
+        p = problems.diffusion3d_source(N=N, steps=train + use, form=form)
+        p.source = src
+        s = problems.make_solver(p)
+        s.setInitialCondition(zk0, zf0)
+        return p, s
+
+    pm, sm = make(L.FORM_LEARNED)
+    sm.learned_options(train_steps=0, mixed_solve=True)
+    sm.set_learned_params(params)
+    pmx, smx = make(L.FORM_MIXED)
+    pf, sf = make(L.FORM_FP64)
+    inner_l, inner_m, used = [], [], 0
+    for k in range(use):
+        a = sm.step(t, pl.dt)
+        b = smx.step(t, pl.dt)
+        sf.step(t, pl.dt)
+        assert a["residual"] < pl.tol and a["sweeps"] >= 1
+        if k >= 1:  # the first step has no history for the network's features
+            inner_l.append(a["iterations"])
+            inner_m.append(b["iterations"])
+            used += a["guess_used"]
+        t += pl.dt
+    zl, _ = sm.state()
+    zf, _ = sf.state()
+    assert rel_err(zl, zf) < 1e-7
+    assert used >= (use - 1) // 2
+    assert np.mean(inner_l) < np.mean(inner_m), (np.mean(inner_l), np.mean(inner_m))
+    for s in (sm, smx, sf):
+        s.close()

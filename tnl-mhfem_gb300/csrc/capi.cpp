@@ -162,6 +162,7 @@ mhfem_status mhfem_create(const mhfem_desc* desc, mhfem_t* out)
         h->S = (desc->dim == 2) ? 9 : 14;
     }
     mhfem_default_solver_opts(&h->opts);
+    h->fp32_copy = (desc->form == MHFEM_FORM_MIXED);
     if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete h;
         return MHFEM_ERR_CUDA;
@@ -427,7 +428,7 @@ mhfem_status ensure_pattern(mhfem_t h)
     CK(cudaMemcpy(h->A.cols, h->pat.ell_cols.data(), sizeof(int32_t) * W * rows, cudaMemcpyHostToDevice));
     CK(dalloc(h, &h->A.vals, (size_t)W * rows));
     CK(cudaMemset(h->A.vals, 0, sizeof(double) * W * rows));
-    if (h->desc.form == MHFEM_FORM_MIXED) {
+    if (h->fp32_copy) {
         CK(dalloc(h, &h->A.vals32, (size_t)W * rows));
         CK(cudaMemset(h->A.vals32, 0, sizeof(float) * W * rows));
     }
@@ -458,7 +459,7 @@ mhfem_status ensure_pattern(mhfem_t h)
     Wk.grid = krylov_grid();
     CK(dalloc(h, &Wk.r, (size_t)rows)); CK(dalloc(h, &Wk.rh, (size_t)rows)); CK(dalloc(h, &Wk.p, (size_t)rows));
     CK(dalloc(h, &Wk.v, (size_t)rows)); CK(dalloc(h, &Wk.s, (size_t)rows)); CK(dalloc(h, &Wk.t, (size_t)rows));
-    if (h->desc.form == MHFEM_FORM_MIXED) {
+    if (h->fp32_copy) {
         CK(dalloc(h, &Wk.r32, (size_t)rows)); CK(dalloc(h, &Wk.rh32, (size_t)rows)); CK(dalloc(h, &Wk.p32, (size_t)rows));
         CK(dalloc(h, &Wk.v32, (size_t)rows)); CK(dalloc(h, &Wk.s32, (size_t)rows)); CK(dalloc(h, &Wk.t32, (size_t)rows));
         CK(dalloc(h, &Wk.x32, (size_t)rows));
@@ -544,9 +545,9 @@ mhfem_status mhfem::run_fp64(mhfem_t h, double tol, int max_iter, int* iters, do
     return status_from_krylov(h, *h->W.host_sc, "FP64 BiCGStab");
 }
 
-namespace {
-
-mhfem_status run_mixed(mhfem_t h, int* iters, int* sweeps, double* res)
+// FP32 inner BiCGStab on the FP32 copy of the matrix, FP64 outer residuals
+// and corrections, until the FP64 residual meets the tolerance.
+mhfem_status mhfem::run_mixed(mhfem_t h, int* iters, int* sweeps, double* res)
 {
     const auto t0 = std::chrono::steady_clock::now();
     KrylovScalars init{};
@@ -589,8 +590,6 @@ mhfem_status run_mixed(mhfem_t h, int* iters, int* sweeps, double* res)
     }
 }
 
-}  // namespace
-
 extern "C" {
 
 mhfem_status mhfem_setup_linear_system(mhfem_t h)
@@ -627,7 +626,7 @@ mhfem_status mhfem_assemble(mhfem_t h, double t, double tau)
     if (!h->pattern_ready) return fail(h, MHFEM_ERR_STATE, "mhfem_pre_iterate must run before mhfem_assemble");
     cudaSetDevice(h->desc.device);
     DevProblem P = make_problem(h);
-    h->launches += launch_assemble(P, h->amap, h->A, h->rhs, h->desc.form == MHFEM_FORM_MIXED, h->stream);
+    h->launches += launch_assemble(P, h->amap, h->A, h->rhs, h->fp32_copy, h->stream);
     cudaEventRecord(h->ev[2], h->stream);
     CK(cudaGetLastError());
     return MHFEM_OK;
@@ -656,7 +655,7 @@ mhfem_status mhfem_solve(mhfem_t h, mhfem_step_stats* stats)
         stats->ms_guess = 0;
     }
     if (h->desc.form == MHFEM_FORM_MIXED) st = run_mixed(h, &iters, &sweeps, &res);
-    else if (h->desc.form == MHFEM_FORM_LEARNED) st = learned_solve(h, &iters, &res, stats);
+    else if (h->desc.form == MHFEM_FORM_LEARNED) st = learned_solve(h, &iters, &sweeps, &res, stats);
     else st = run_fp64(h, h->opts.tol, h->opts.max_iter, &iters, &res);
     cudaEventRecord(h->ev[3], h->stream);
     h->total_iters += iters;
@@ -811,12 +810,12 @@ mhfem_status mhfem_time_kernel(mhfem_t h, int32_t kernel, int32_t reps, double* 
             break;
         case MHFEM_KERNEL_ASSEMBLE:
             B = 8 * F + 2 * F + (nf > 4 ? 8 : 4) * F + F + rec + 8 * W * R + 8 * R
-              + (h->desc.form == MHFEM_FORM_MIXED ? 4 * W * R : 0);
+              + (h->fp32_copy ? 4 * W * R : 0);
             FL = R * (W + 3);
             break;
         case MHFEM_KERNEL_SPMV_FP64: B = R * (12 * W + 24); FL = 2 * R * (W + 1); break;
         case MHFEM_KERNEL_SPMV_FP32:
-            if (h->desc.form != MHFEM_FORM_MIXED) return fail(h, MHFEM_ERR_STATE, "FP32 SpMV needs the mixed form");
+            if (!h->fp32_copy) return fail(h, MHFEM_ERR_STATE, "FP32 SpMV needs the FP32 matrix (mixed form or mixed learned solve)");
             B = R * (8 * W + 12); FL = 2 * R * (W + 1); break;
         case MHFEM_KERNEL_RECONSTRUCT:
             B = 4 * nf * C + 8 * n * F + 8 * n * n * nf * C + 8 * n * C + 8 * n * C;
@@ -835,7 +834,7 @@ mhfem_status mhfem_time_kernel(mhfem_t h, int32_t kernel, int32_t reps, double* 
         switch (kernel) {
             case MHFEM_KERNEL_CELL_LOCAL: launch_cell_local(P, h->cur_tau > 0 ? h->cur_tau : 1.0, h->stream); break;
             case MHFEM_KERNEL_ASSEMBLE:
-                launch_assemble(P, h->amap, h->A, h->rhs, h->desc.form == MHFEM_FORM_MIXED, h->stream); break;
+                launch_assemble(P, h->amap, h->A, h->rhs, h->fp32_copy, h->stream); break;
             case MHFEM_KERNEL_SPMV_FP64: krylov_spmv_dot_once(h->A, h->W, false, h->stream); break;
             case MHFEM_KERNEL_SPMV_FP32: krylov_spmv_dot_once(h->A, h->W, true, h->stream); break;
             case MHFEM_KERNEL_RECONSTRUCT: launch_reconstruct(P, h->stream); break;

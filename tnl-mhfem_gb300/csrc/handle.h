@@ -64,6 +64,9 @@ struct mhfem_solver_s {
     mhfem::KrylovWork W;
 
     mhfem_solver_opts opts{};
+    // the matrix keeps an FP32 copy and the FP32 Krylov vectors exist: the
+    // mixed form, or the learned form with its mixed solve
+    bool fp32_copy = false;
     int64_t total_iters = 0, total_steps = 0, launches = 0;
     double cur_t = 0, cur_tau = 0;
 
@@ -126,8 +129,10 @@ inline void dfree(mhfem_t h, T*& p)
 
 // FP64 BiCGStab from the current Z_iF (capi.cpp).
 mhfem_status run_fp64(mhfem_t h, double tol, int max_iter, int* iters, double* res);
-// Learned form (learned.cpp): the gate, the FP64 solve and online training.
-mhfem_status learned_solve(mhfem_t h, int* iters, double* res, mhfem_step_stats* stats);
+// Mixed-precision refinement from the current Z_iF (capi.cpp); needs fp32_copy.
+mhfem_status run_mixed(mhfem_t h, int* iters, int* sweeps, double* res);
+// Learned form (learned.cpp): the gate, the solve (FP64 or mixed) and online training.
+mhfem_status learned_solve(mhfem_t h, int* iters, int* sweeps, double* res, mhfem_step_stats* stats);
 void learned_release(mhfem_t h);
 // Marks the network state stale (the pattern changed); the parameters are kept.
 void learned_invalidate(mhfem_t h);

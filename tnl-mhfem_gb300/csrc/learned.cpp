@@ -58,7 +58,9 @@ struct LearnedState {
     int trained_steps = 0;
     int adam_t = 0;
     bool params_set = false;
+    bool params_loaded = false;  // given by mhfem_learned_set_params: usable before any training
     // options
+    int mixed_solve = 0;  // solve from the guess with the mixed-precision refinement
     int train_steps = 200;
     int train_iters = 2;
     float lr = 1e-3f;
@@ -375,7 +377,7 @@ static mhfem_status train_once(mhfem_t h, int iters)
     return MHFEM_OK;
 }
 
-mhfem_status learned_solve(mhfem_t h, int* iters, double* res, mhfem_step_stats* stats)
+mhfem_status learned_solve(mhfem_t h, int* iters, int* sweeps, double* res, mhfem_step_stats* stats)
 {
     mhfem_status st = learned_prepare(h);
     if (st) return st;
@@ -385,7 +387,7 @@ mhfem_status learned_solve(mhfem_t h, int* iters, double* res, mhfem_step_stats*
     LCK(cudaMemcpyAsync(L->Zn, h->Z_iF, sizeof(double) * F, cudaMemcpyDeviceToDevice, s));
     const bool have_hist = L->hist >= 1;
     const bool training = L->trained_steps < L->train_steps;
-    const bool infer = have_hist && (!training || L->use_during_training) && L->trained_steps > 0;
+    const bool infer = have_hist && (!training || L->use_during_training) && (L->trained_steps > 0 || L->params_loaded);
     MpnnInputs in{};
     in.Zn = L->Zn;
     in.Zn1 = L->Zn1;
@@ -433,7 +435,7 @@ mhfem_status learned_solve(mhfem_t h, int* iters, double* res, mhfem_step_stats*
         h->launches += (kMpnnLayers + 1) + 2;
     }
     if (h->guess_timed) cudaEventRecord(h->ev[6], s);
-    st = run_fp64(h, h->opts.tol, h->opts.max_iter, iters, res);
+    st = L->mixed_solve ? run_mixed(h, iters, sweeps, res) : run_fp64(h, h->opts.tol, h->opts.max_iter, iters, res);
     if (st) return st;
     int used = 0;
     double r_warm = -1, r_guess = -1;
@@ -497,6 +499,12 @@ mhfem_status mhfem_learned_set_options(mhfem_t h, const mhfem_learned_opts* o)
     L->lr = (float)o->learning_rate;
     L->lr_final = o->lr_final;
     L->use_during_training = o->use_during_training;
+    L->mixed_solve = o->mixed_solve ? 1 : 0;
+    if (h->desc.form == MHFEM_FORM_LEARNED && (L->mixed_solve != 0) != h->fp32_copy) {
+        // the FP32 matrix copy and work vectors follow; the pattern is rebuilt at the next step
+        h->fp32_copy = L->mixed_solve != 0;
+        h->pattern_ready = false;
+    }
     if (o->seed != 0 && o->seed != L->seed) {
         L->seed = o->seed;
         L->params_set = false;
@@ -530,6 +538,7 @@ mhfem_status mhfem_learned_set_params(mhfem_t h, const float* params, int64_t co
     publish(h);
     LCK(cudaStreamSynchronize(h->stream));
     L->params_set = true;
+    L->params_loaded = true;
     return MHFEM_OK;
 }
 

@@ -59,7 +59,8 @@ class SolverOpts(ct.Structure):
 
 class LearnedOpts(ct.Structure):
     _fields_ = [("train_steps", ct.c_int32), ("train_iters", ct.c_int32), ("learning_rate", ct.c_double),
-                ("use_during_training", ct.c_int32), ("seed", ct.c_uint64), ("lr_final", ct.c_double)]
+                ("use_during_training", ct.c_int32), ("seed", ct.c_uint64), ("lr_final", ct.c_double),
+                ("mixed_solve", ct.c_int32)]
 
 
 LEARNED_FEATURES = 16

@@ -228,8 +228,10 @@ class Solver:
 
     # -- learned warm start (MHFEM_FORM_LEARNED) ------------------------
     def learned_options(self, train_steps: int = 200, train_iters: int = 2, learning_rate: float = 1e-3,
-                        use_during_training: bool = False, seed: int = 0, lr_final: float = 1.0) -> None:
-        o = L.LearnedOpts(train_steps, train_iters, learning_rate, int(use_during_training), seed, lr_final)
+                        use_during_training: bool = False, seed: int = 0, lr_final: float = 1.0,
+                        mixed_solve: bool = False) -> None:
+        o = L.LearnedOpts(train_steps, train_iters, learning_rate, int(use_during_training), seed, lr_final,
+                          int(mixed_solve))
         self._ck(self.lib.mhfem_learned_set_options(self._h, ct.byref(o)))
 
     def learned_num_params(self) -> int:
