@@ -88,6 +88,8 @@ typedef struct mhfem_solver_s* mhfem_t;
 #define MHFEM_ARRAY_Z_UPW   4  /* Z_ijE_upw (E,j,i)       */
 #define MHFEM_ARRAY_V       5  /* v_iKe (i,e,K)           */
 #define MHFEM_ARRAY_RHS     6  /* scaled right-hand side, rows E*n+i */
+#define MHFEM_ARRAY_Z_IF    7  /* face traces Z_iF (E,i)  */
+#define MHFEM_ARRAY_Z_IK    8  /* cell values Z_iK (i,K)  */
 
 typedef struct {
     int32_t dim;              /* 2: triangles, 3: tetrahedra (examples/config.h:17-21) */
@@ -152,16 +154,47 @@ mhfem_status mhfem_get_sizes(mhfem_t h, int64_t* V, int64_t* C, int64_t* F,
                              int64_t* rows, int64_t* nnz);
 
 /* Topology as built (getCellsForFace / getFacesForCell, mesh_helpers.h:49-160):
- * face_verts [F][dim] (sorted vertex ids), face_cells [F][2] (ascending, -1 on
- * the boundary), cell_faces [C][dim+1].  Any pointer may be NULL. */
+ * face_verts [F][vertices per face] (sorted vertex ids: d for simplices,
+ * 2^(d-1) for boxes), face_cells [F][2] (ascending, -1 on the boundary),
+ * cell_faces [C][faces per cell] (d+1 or 2d).  Any pointer may be NULL. */
 mhfem_status mhfem_get_topology(mhfem_t h, int32_t* face_verts, int32_t* face_cells,
                                 int32_t* cell_faces);
 
 /* Replaces the model writing its coefficient arrays in Model::init
  * (HeatEquationModel.h:114-133).  count == 1 gives a uniform coefficient
  * (UniformCoefficient.h:8-52); otherwise count must equal the full size of
- * the layout listed beside the MHFEM_COEF_* identifier. */
+ * the layout listed beside the MHFEM_COEF_* identifier.  data may be host or
+ * device memory (the copy is ordered on the handle's stream). */
 mhfem_status mhfem_set_coeff(mhfem_t h, int32_t which, const double* data, int64_t count);
+
+/* ---- model hooks (custom models) -----------------------------------------
+ * The reference's models are compile-time C++ classes whose device
+ * functions the Solver calls inside preIterate: updateNonLinearTerms per
+ * cell before the mass-matrix update (Solver.hpp:616-625) and
+ * updateVectorCoefficients after it (Solver.hpp:641-652); BaseModel's
+ * preIterate / postIterate run around each step (BaseModel.h:147-166).
+ * Here a model is host code that launches its own kernels: a hook is called
+ * on the calling thread at a fixed point of the step with the handle's CUDA
+ * stream, and updates the coefficient arrays on the device in place
+ * (mhfem_coeff_device), reading the state (mhfem_array_device), with work
+ * ordered on that stream.  The cell kernel fuses the mass-matrix update with
+ * everything after it, so a vector coefficient whose projection depends on
+ * b sees the previous step's b.  Writes through these pointers bypass the
+ * host copies that mhfem_set_coeff keeps: the learned form's static
+ * features keep the values last passed to mhfem_set_coeff. */
+typedef void (*mhfem_hook)(void* user, double t, double tau, void* stream);
+#define MHFEM_HOOK_PRE_ITERATE  0  /* start of mhfem_pre_iterate, before upwinding and the cell kernel */
+#define MHFEM_HOOK_POST_ITERATE 1  /* end of mhfem_post_iterate, after the reconstruction */
+/* fn == NULL removes the hook. */
+mhfem_status mhfem_set_hook(mhfem_t h, int32_t point, mhfem_hook fn, void* user);
+/* The device array of a coefficient as currently stored (count 1: uniform,
+ * a single value; pass a full array to mhfem_set_coeff first to make it
+ * per-cell).  Asking for MHFEM_COEF_A or MHFEM_COEF_U switches the explicit
+ * advection terms on for every later step (exact zeros leave the results
+ * unchanged). */
+mhfem_status mhfem_coeff_device(mhfem_t h, int32_t which, double** data, int64_t* count);
+/* The device array of a scheme or state array (MHFEM_ARRAY_*). */
+mhfem_status mhfem_array_device(mhfem_t h, int32_t which, double** data, int64_t* count);
 
 /* Time-modulated source (a model hook of updateNonLinearTerms,
  * Solver.hpp:616-625): before each step at time t,

@@ -135,9 +135,13 @@ class OracleModel:
         P.cell_verts = self.cells.ctypes.data_as(_pi32)
         P.cell_faces = self.cell_faces.ctypes.data_as(_pi32)
         P.face_cells = self.face_cells.ctypes.data_as(_pi32)
+        # the coefficient arrays the restatement reads; a test may change their
+        # values in place between steps (a model's updateNonLinearTerms)
+        self.coeff_arrays = {}
         for name in ["N", "u", "m", "D", "w", "a", "r", "f", "m_bnd"]:
             arr = np.ascontiguousarray(np.atleast_1d(np.asarray(coeffs.get(name, 0.0), np.float64)).ravel())
             self._keep.append(arr)
+            self.coeff_arrays[name] = arr
             setattr(P, name, Coef(_dp(arr), int(arr.size > 1)))
         m_upw = np.ascontiguousarray(np.atleast_1d(np.asarray(coeffs.get("m_upw", 1.0), np.float64)).ravel())
         if mobility_upwind:

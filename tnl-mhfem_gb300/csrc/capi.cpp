@@ -34,19 +34,68 @@ int64_t coef_size(mhfem_t h, int which)
     return -1;
 }
 
+bool is_device_pointer(const void* p)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();  // a plain host pointer on older drivers: clear the error
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// Copies a coefficient (host or device source) into its device array and
+// keeps a host copy (the learned form's static features, the zero test of
+// the explicit advection switch).
 mhfem_status set_coef_device(mhfem_t h, int which, const double* data, int64_t count)
 {
     if (h->coef[which].count != count || !h->coef[which].p) {
         dfree(h, h->coef[which].p);
         CK(dalloc(h, &h->coef[which].p, (size_t)count));
     }
-    CK(cudaMemcpyAsync(h->coef[which].p, data, sizeof(double) * count, cudaMemcpyHostToDevice, h->stream));
+    const bool dev = is_device_pointer(data);
+    h->h_coef[which].resize(count);
+    CK(cudaMemcpyAsync(h->coef[which].p, data, sizeof(double) * count,
+                       dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+    if (dev)
+        CK(cudaMemcpyAsync(h->h_coef[which].data(), data, sizeof(double) * count, cudaMemcpyDeviceToHost, h->stream));
+    else
+        std::copy(data, data + count, h->h_coef[which].begin());
     h->coef[which].count = count;
-    h->h_coef[which].assign(data, data + count);
-    bool nz = false;
-    for (int64_t q = 0; q < count && !nz; ++q) nz = (data[q] != 0.0);
-    h->coef_nonzero[which] = nz;
     CK(cudaStreamSynchronize(h->stream));
+    bool nz = false;
+    for (int64_t q = 0; q < count && !nz; ++q) nz = (h->h_coef[which][q] != 0.0);
+    h->coef_nonzero[which] = nz;
+    return MHFEM_OK;
+}
+
+// The device array behind an MHFEM_ARRAY_* identifier and its size.
+mhfem_status array_ptr(mhfem_t h, int32_t which, double** p, int64_t* size)
+{
+    const int64_t n = h->n, nf = h->nf, C = h->topo.C, F = h->topo.F;
+    switch (which) {
+        case MHFEM_ARRAY_B: *p = h->b; *size = n * n * h->S * C; break;
+        case MHFEM_ARRAY_R_IJKE: *p = h->R_ijKe; *size = n * n * nf * C; break;
+        case MHFEM_ARRAY_R_IK: *p = h->R_iK; *size = n * C; break;
+        case MHFEM_ARRAY_M_UPW: *p = h->m_upw; *size = n * F; break;
+        case MHFEM_ARRAY_Z_UPW: *p = h->Z_upw; *size = n * n * F; break;
+        case MHFEM_ARRAY_V: *p = h->v_iKe; *size = n * nf * C; break;
+        case MHFEM_ARRAY_RHS: *p = h->rhs; *size = n * F; break;
+        case MHFEM_ARRAY_Z_IF: *p = h->Z_iF; *size = n * F; break;
+        case MHFEM_ARRAY_Z_IK: *p = h->Z_iK; *size = n * C; break;
+        default: return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "unknown array %d", which);
+    }
+    if (!*p) return fail(h, MHFEM_ERR_STATE, "array %d is not allocated in this configuration", which);
+    return MHFEM_OK;
+}
+
+mhfem_status run_hook(mhfem_t h, int point, double t, double tau)
+{
+    const auto& k = h->hooks[point];
+    if (!k.fn) return MHFEM_OK;
+    k.fn(k.user, t, tau, (void*)h->stream);
+    cudaSetDevice(h->desc.device);
+    CK(cudaGetLastError());
     return MHFEM_OK;
 }
 
@@ -609,6 +658,7 @@ mhfem_status mhfem_pre_iterate(mhfem_t h, double t, double tau)
     if ((st = ensure_pattern(h)) != MHFEM_OK) return st;
     h->cur_t = t;
     h->cur_tau = tau;
+    if ((st = run_hook(h, MHFEM_HOOK_PRE_ITERATE, t, tau)) != MHFEM_OK) return st;
     DevProblem P = make_problem(h);
     cudaEventRecord(h->ev[0], h->stream);
     h->launches += launch_upwind(P, h->stream);
@@ -671,12 +721,44 @@ mhfem_status mhfem_post_iterate(mhfem_t h, double t, double tau)
 {
     mhfem_status st = require_ready(h);
     if (st) return st;
-    (void)t; (void)tau;
     cudaSetDevice(h->desc.device);
     DevProblem P = make_problem(h);
     h->launches += launch_reconstruct(P, h->stream);
     cudaEventRecord(h->ev[4], h->stream);
     CK(cudaGetLastError());
+    return run_hook(h, MHFEM_HOOK_POST_ITERATE, t, tau);
+}
+
+mhfem_status mhfem_set_hook(mhfem_t h, int32_t point, mhfem_hook fn, void* user)
+{
+    if (!h) return MHFEM_ERR_INVALID_ARGUMENT;
+    if (point != MHFEM_HOOK_PRE_ITERATE && point != MHFEM_HOOK_POST_ITERATE)
+        return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "unknown hook point %d", point);
+    h->hooks[point].fn = fn;
+    h->hooks[point].user = user;
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_coeff_device(mhfem_t h, int32_t which, double** data, int64_t* count)
+{
+    mhfem_status st = require_ready(h);
+    if (st) return st;
+    if (which < 0 || which >= NCOEF || !data) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "invalid coefficient id %d", which);
+    if (!h->coef[which].p) return fail(h, MHFEM_ERR_STATE, "coefficient %d has no storage", which);
+    *data = h->coef[which].p;
+    if (count) *count = h->coef[which].count;
+    if (which == MHFEM_COEF_A || which == MHFEM_COEF_U) h->coef_nonzero[which] = true;
+    return MHFEM_OK;
+}
+
+mhfem_status mhfem_array_device(mhfem_t h, int32_t which, double** data, int64_t* count)
+{
+    mhfem_status st = require_ready(h);
+    if (st) return st;
+    if (!data) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "null output");
+    int64_t size = 0;
+    if ((st = array_ptr(h, which, data, &size)) != MHFEM_OK) return st;
+    if (count) *count = size;
     return MHFEM_OK;
 }
 
@@ -718,20 +800,9 @@ mhfem_status mhfem_get_array(mhfem_t h, int32_t which, double* out, int64_t coun
 {
     mhfem_status st = require_ready(h);
     if (st) return st;
-    const int64_t n = h->n, nf = h->nf, C = h->topo.C, F = h->topo.F;
-    const double* src = nullptr;
+    double* src = nullptr;
     int64_t size = 0;
-    switch (which) {
-        case MHFEM_ARRAY_B: src = h->b; size = n * n * h->S * C; break;
-        case MHFEM_ARRAY_R_IJKE: src = h->R_ijKe; size = n * n * nf * C; break;
-        case MHFEM_ARRAY_R_IK: src = h->R_iK; size = n * C; break;
-        case MHFEM_ARRAY_M_UPW: src = h->m_upw; size = n * F; break;
-        case MHFEM_ARRAY_Z_UPW: src = h->Z_upw; size = n * n * F; break;
-        case MHFEM_ARRAY_V: src = h->v_iKe; size = n * nf * C; break;
-        case MHFEM_ARRAY_RHS: src = h->rhs; size = n * F; break;
-        default: return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "unknown array %d", which);
-    }
-    if (!src) return fail(h, MHFEM_ERR_STATE, "array %d is not allocated in this configuration", which);
+    if ((st = array_ptr(h, which, &src, &size)) != MHFEM_OK) return st;
     if (!out || count != size) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "array %d has %lld values", which, (long long)size);
     cudaSetDevice(h->desc.device);
     CK(cudaMemcpyAsync(out, src, sizeof(double) * size, cudaMemcpyDeviceToHost, h->stream));

@@ -74,6 +74,10 @@ struct mhfem_solver_s {
     int g64_iters = 0, g32_iters = 0;
 
     cudaEvent_t ev[7] = {};  // phase boundaries 0..4; 5, 6: the learned guess
+    struct Hook {
+        mhfem_hook fn = nullptr;
+        void* user = nullptr;
+    } hooks[2];              // MHFEM_HOOK_PRE_ITERATE, MHFEM_HOOK_POST_ITERATE
     bool guess_timed = false;
     std::vector<void*> allocs;
 

@@ -37,7 +37,10 @@ EXPLICIT_UPWIND, IMPLICIT_UPWIND, IMPLICIT_TRACE = 0, 1, 2
 FORM_FP64, FORM_MIXED, FORM_LEARNED = 0, 1, 2
 
 COEF_N, COEF_U, COEF_M, COEF_D, COEF_W, COEF_A, COEF_R, COEF_F, COEF_M_UPW, COEF_M_BND, COEF_PSI = range(11)
-ARRAY_B, ARRAY_R_IJKE, ARRAY_R_IK, ARRAY_M_UPW, ARRAY_Z_UPW, ARRAY_V, ARRAY_RHS = range(7)
+ARRAY_B, ARRAY_R_IJKE, ARRAY_R_IK, ARRAY_M_UPW, ARRAY_Z_UPW, ARRAY_V, ARRAY_RHS, ARRAY_Z_IF, ARRAY_Z_IK = range(9)
+HOOK_PRE_ITERATE, HOOK_POST_ITERATE = 0, 1
+# void hook(void* user, double t, double tau, void* stream)
+HOOK = ct.CFUNCTYPE(None, ct.c_void_p, ct.c_double, ct.c_double, ct.c_void_p)
 KERNEL_CELL_LOCAL, KERNEL_ASSEMBLE, KERNEL_SPMV_FP64, KERNEL_SPMV_FP32, KERNEL_RECONSTRUCT = range(5)
 
 
@@ -92,6 +95,9 @@ SIGNATURES = [
     ("mhfem_get_topology", ct.c_int32, [_P, _pi32, _pi32, _pi32]),
     ("mhfem_set_coeff", ct.c_int32, [_P, ct.c_int32, _pd, ct.c_int64]),
     ("mhfem_set_source_modulation", ct.c_int32, [_P, ct.c_double, ct.c_double]),
+    ("mhfem_set_hook", ct.c_int32, [_P, ct.c_int32, HOOK, _P]),
+    ("mhfem_coeff_device", ct.c_int32, [_P, ct.c_int32, ct.POINTER(_P), _pi64]),
+    ("mhfem_array_device", ct.c_int32, [_P, ct.c_int32, ct.POINTER(_P), _pi64]),
     ("mhfem_set_bc", ct.c_int32, [_P, _pu8, _pd, _pd]),
     ("mhfem_set_initial_condition", ct.c_int32, [_P, _pd]),
     ("mhfem_set_state", ct.c_int32, [_P, _pd, _pd]),

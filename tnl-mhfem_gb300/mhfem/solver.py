@@ -57,7 +57,22 @@ class StaticConfig:
 COEF_IDS = {"N": L.COEF_N, "u": L.COEF_U, "m": L.COEF_M, "D": L.COEF_D, "w": L.COEF_W, "a": L.COEF_A,
             "r": L.COEF_R, "f": L.COEF_F, "m_upw": L.COEF_M_UPW, "m_bnd": L.COEF_M_BND, "psi": L.COEF_PSI}
 ARRAY_IDS = {"b": L.ARRAY_B, "R_ijKe": L.ARRAY_R_IJKE, "R_iK": L.ARRAY_R_IK, "m_upw": L.ARRAY_M_UPW,
-             "Z_upw": L.ARRAY_Z_UPW, "v_iKe": L.ARRAY_V, "rhs": L.ARRAY_RHS}
+             "Z_upw": L.ARRAY_Z_UPW, "v_iKe": L.ARRAY_V, "rhs": L.ARRAY_RHS, "Z_iF": L.ARRAY_Z_IF,
+             "Z_iK": L.ARRAY_Z_IK}
+
+
+class DeviceArray:
+    """A library-owned FP64 device array, exposed through
+    ``__cuda_array_interface__`` (so ``torch.as_tensor(a, device="cuda")``
+    or any CUDA array library views it without a copy)."""
+
+    def __init__(self, ptr: int, count: int):
+        self.ptr, self.count = ptr, count
+
+    @property
+    def __cuda_array_interface__(self):
+        return {"shape": (self.count,), "typestr": "<f8", "data": (self.ptr, False), "version": 2,
+                "strides": None}
 
 
 class Solver:
@@ -213,6 +228,32 @@ class Solver:
         it = ct.c_int64(); ts = ct.c_int64(); kl = ct.c_int64()
         self._ck(self.lib.mhfem_get_totals(self._h, ct.byref(it), ct.byref(ts), ct.byref(kl)))
         return it.value, ts.value, kl.value
+
+    def set_hook(self, point: int, fn) -> None:
+        """Model hook: fn(t, tau, stream) is called at `point` (HOOK_PRE_ITERATE:
+        before upwinding and the cell kernel; HOOK_POST_ITERATE: after the
+        reconstruction) with the library's stream, on which its device work
+        must be ordered.  None removes it."""
+        if not hasattr(self, "_hooks"):
+            self._hooks = {}
+        if fn is None:
+            cb = ct.cast(None, L.HOOK)
+        else:
+            cb = L.HOOK(lambda user, t, tau, stream: fn(t, tau, stream or 0))
+        self._hooks[point] = cb  # keep the callback alive as long as the solver
+        self._ck(self.lib.mhfem_set_hook(self._h, point, cb, None))
+
+    def coeff_device(self, name: str) -> DeviceArray:
+        """The device storage of a coefficient (size 1 when uniform)."""
+        p = ct.c_void_p(); n = ct.c_int64()
+        self._ck(self.lib.mhfem_coeff_device(self._h, COEF_IDS[name], ct.byref(p), ct.byref(n)))
+        return DeviceArray(p.value, n.value)
+
+    def array_device(self, name: str) -> DeviceArray:
+        """The device storage of a scheme / state array (b, R_ijKe, R_iK, m_upw, Z_upw, v_iKe, rhs, Z_iF, Z_iK)."""
+        p = ct.c_void_p(); n = ct.c_int64()
+        self._ck(self.lib.mhfem_array_device(self._h, ARRAY_IDS[name], ct.byref(p), ct.byref(n)))
+        return DeviceArray(p.value, n.value)
 
     def stream(self) -> int:
         """The library's CUDA stream handle (for CUDA events on that stream)."""
