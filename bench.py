@@ -59,7 +59,7 @@ def parse_args():
                     help="online training steps of the learned form before its timed steps")
     ap.add_argument("--profile-run", action="store_true",
                     help="only the warm-up and timed steps (for an ncu launch list)")
-    ap.add_argument("--profile-form", choices=["fp64", "mixed", "learned"], default="fp64",
+    ap.add_argument("--profile-form", choices=["fp64", "mixed", "learned", "box"], default="fp64",
                     help="form used by --profile-run (learned: --learned-train training steps first)")
     return ap.parse_args()
 
@@ -343,7 +343,8 @@ def learned_leg(args, dev, world):
 
 
 def profile_other_form(args, dev):
-    """Warm-up + timed steps of the mixed or learned form only (for ncu launch lists)."""
+    """Warm-up + timed steps of the mixed or learned form, or of the FP64 form on
+    (2 grid)^3 cuboids ("box"), only (for ncu launch lists)."""
     import torch
 
     from mhfem import _lib as L
@@ -351,6 +352,8 @@ def profile_other_form(args, dev):
 
     if args.profile_form == "mixed":
         p = problems.diffusion3d(N=args.grid, form=L.FORM_MIXED)
+    elif args.profile_form == "box":
+        p = problems.diffusion3d_box(N=2 * args.grid)
     else:
         p = problems.diffusion3d_source(N=args.grid, steps=1000, form=L.FORM_LEARNED)
     p.config.device = dev
