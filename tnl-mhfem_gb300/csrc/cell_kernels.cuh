@@ -706,9 +706,9 @@ __global__ void k_face_average(const DevProblem P)
 
 #define MHFEM_NE_DISPATCH(CTV, NEV, CALL)                                        \
     do {                                                                          \
-        if ((NEV) == 1) { constexpr int CT = (CTV), NE = 1; constexpr int NF = ct_nf(CT); CALL; } \
-        else if ((NEV) == 2) { constexpr int CT = (CTV), NE = 2; constexpr int NF = ct_nf(CT); CALL; } \
-        else { constexpr int CT = (CTV), NE = 3; constexpr int NF = ct_nf(CT); CALL; } \
+        if ((NEV) == 1) { constexpr int CT = (CTV), NE = 1; constexpr int NF = ct_nf(CT); (void)NF; CALL; } \
+        else if ((NEV) == 2) { constexpr int CT = (CTV), NE = 2; constexpr int NF = ct_nf(CT); (void)NF; CALL; } \
+        else { constexpr int CT = (CTV), NE = 3; constexpr int NF = ct_nf(CT); (void)NF; CALL; } \
     } while (0)
 
 static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs - 1) / bs); }

@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(256) k_assemble(const DevProblem P, const Qmap
         // the entries at run-time positions are re-read from the record (an
         // L1 hit), which keeps A in registers and costs no FP64 selects
         const double diag = __ldg(r0 + i * NF + e0);
-        if (!(diag > 0)) atomicOr(P.err_flags, 1);
+        if (!positive_bits(diag)) atomicOr(P.err_flags, 1);
         const double rd = recip_newton(diag);
 #pragma unroll
         for (int f = 0; f < NF; ++f) {
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(256) k_assemble(const DevProblem P, const Qmap
 #pragma unroll
     for (int j = 0; j < NE; ++j) a1e[j] = __ldg(r1 + j * NF + e1);
     const double diag = __ldg(r0 + i * NF + e0) + __ldg(r1 + i * NF + e1);
-    if (!(diag > 0)) atomicOr(P.err_flags, 1);
+    if (!positive_bits(diag)) atomicOr(P.err_flags, 1);
     const double rd = recip_newton(diag);
 #pragma unroll
     for (int f = 0; f < NF; ++f) {

@@ -470,21 +470,21 @@ __device__ __forceinline__ void phase_spmv_dots2(const int32_t* cols, const T* v
             t[q] = y;
             cur = nxt;
         }
-        return;
     }
-    for (int64_t q = gtid; q < rows / RPT; q += gstride) {
-        T y[RPT], sv[RPT];
-        spmv_rows<T, WW, RPT>(cols, vals, W, rows, q, s, y, sv);
-        VecT<T, RPT> yv;
+    else
+        for (int64_t q = gtid; q < rows / RPT; q += gstride) {
+            T y[RPT], sv[RPT];
+            spmv_rows<T, WW, RPT>(cols, vals, W, rows, q, s, y, sv);
+            VecT<T, RPT> yv;
 #pragma unroll
-        for (int j = 0; j < RPT; ++j) {
-            yv.v[j] = y[j];
-            acc[0] = fma(y[j], sv[j], acc[0]);
-            acc[1] = fma(y[j], y[j], acc[1]);
-            acc[2] = fma(sv[j], sv[j], acc[2]);
+            for (int j = 0; j < RPT; ++j) {
+                yv.v[j] = y[j];
+                acc[0] = fma(y[j], sv[j], acc[0]);
+                acc[1] = fma(y[j], y[j], acc[1]);
+                acc[2] = fma(sv[j], sv[j], acc[2]);
+            }
+            stv<T, RPT>(t, q, yv);
         }
-        stv<T, RPT>(t, q, yv);
-    }
 }
 
 // ||s||, the half-step test, omega = (t, s) / (t, t)

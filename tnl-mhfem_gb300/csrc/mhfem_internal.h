@@ -36,16 +36,18 @@ enum : int32_t { KS_RUNNING = 0, KS_CONVERGED = 1, KS_MAXITER = 2, KS_BREAKDOWN 
 // 1 / d in FP64 for the row scaling of the assembly and the LU pivots of the
 // cell kernel.  GB300 issues FP64 at 1/57 of the FP32 rate and both kernels
 // are bound by their FP64 pipe, where an IEEE FP64 division costs about as
-// much as the rest of a face row.  Newton-Raphson reciprocal iteration
-// (r <- r + r (1 - d r), quadratic convergence) from an FP32 reciprocal
-// estimate: 2^-22 -> 2^-44 -> below FP64 rounding after two steps, i.e.
-// within an ulp or two of the correctly rounded quotient (the GPU parity
-// tests bound the local quantities and the assembled values at 1e-12
-// relative against the oracle's IEEE division).  The FP32 operand and the
-// FP32 estimate move between the two IEEE formats by integer bit operations
-// (sign, rebiased exponent, truncated mantissa), so the FP64 pipe only sees
-// the four fused multiply-adds.  Magnitudes outside [2^-100, 2^100] (and 0,
-// inf, NaN) take the IEEE division.
+// much as the rest of a face row.  One third-order step from an FP32
+// reciprocal estimate r0: with u = 1 - d r0, 1/d = r0 / (1 - u) = r0 (1 + u
+// + u^2 + ...), truncated after u^2 (Halley's iteration for f(r) = 1/r - d,
+// cubic convergence): r = r0 + r0 (u + u^2).  The estimate's relative error
+// is below 2^-22, so the truncation error is below 2^-66, under FP64
+// rounding: the result is within an ulp of the correctly rounded quotient
+// (the GPU parity tests bound the local quantities and the assembled values
+// at 1e-12 relative against the oracle's IEEE division).  The FP32 operand
+// and the FP32 estimate move between the two IEEE formats by integer bit
+// operations (sign, rebiased exponent, truncated mantissa), so the FP64
+// pipe only sees three fused multiply-adds.  Magnitudes outside
+// [2^-100, 2^100] (and 0, inf, NaN) take the IEEE division.
 static __device__ __noinline__ double recip_ieee(double d) { return 1.0 / d; }
 
 __device__ __forceinline__ double recip_newton(double d)
@@ -59,11 +61,17 @@ __device__ __forceinline__ double recip_newton(double d)
     const unsigned long long r64 = ((unsigned long long)(rb & 0x80000000u) << 32) |
                                    ((unsigned long long)(((rb >> 23) & 0xffu) - 127u + 1023u) << 52) |
                                    ((unsigned long long)(rb & 0x7fffffu) << 29);
-    double r = __longlong_as_double((long long)r64);
-    double t = fma(-d, r, 1.0);
-    r = fma(r, t, r);
-    t = fma(-d, r, 1.0);
-    return fma(r, t, r);
+    const double r = __longlong_as_double((long long)r64);
+    const double u = fma(-d, r, 1.0);
+    return fma(r, fma(u, u, u), r);
+}
+
+// d > 0 (including +inf; false for zero, negatives and NaN) as an integer
+// test on the bit pattern, which keeps the compare off the FP64 pipe.
+__device__ __forceinline__ bool positive_bits(double d)
+{
+    const long long b = __double_as_longlong(d);
+    return b > 0 && b <= 0x7ff0000000000000LL;
 }
 #endif
 
