@@ -341,42 +341,57 @@ __device__ __forceinline__ void spmv_rows(const int32_t* __restrict__ cols, cons
     }
 }
 
-// One ELL row (compile-time width) held in registers: the pipelined
-// one-row-per-thread SpMV loads the next row of its grid-stride sequence
-// before gathering for the current one, so the two memory round trips of a
-// row (ELL entries, then the gathered x) overlap with the neighbouring row's.
-// Measured on GB300: at width 10 (cuboids) 172.8 against 198.9 us per
-// launch on 6.3M rows (79% against 69% of HBM); at width 6 (tetrahedra) the
-// doubled registers cost more occupancy than the overlap gains (60.2
-// against 58.2 us), so only width 10 takes it.
-constexpr bool spmv_pipelined(int WW, int RPT) { return RPT == 1 && WW == 10; }
-template <typename T, int WW>
-struct EllRow {
-    int32_t c[WW];
-    T a[WW];
+// Pipelined SpMV: a thread loads the ELL entries of its next group of rows
+// (grid-stride sequence) before gathering for the current group, so the two
+// memory round trips of a row (ELL entries, then the gathered x) overlap
+// with the neighbouring group's.  It doubles the registers that hold ELL
+// entries, so it pays where latency, not the FP64 pipe, bounds the kernel
+// (measured on GB300):
+//  - FP64, width 10 (cuboids): 172.8 against 198.9 us per launch on 6.3M rows
+//    (79% against 69% of HBM);
+//  - FP32, 4 rows per thread (the mixed form's inner solve, tetrahedra):
+//    5.37 against 4.87 TB/s, mixed form 1.69x against 1.59x the FP64 form;
+//  - FP64, width 6 (tetrahedra): slower (60.2 against 58.2 us), kept plain.
+template <typename T>
+constexpr bool spmv_pipelined(int WW, int RPT)
+{
+    return (sizeof(T) == 8 && RPT == 1 && WW == 10) || (sizeof(T) == 4 && RPT == 4 && (WW == 4 || WW == 6));
+}
+
+// RPT consecutive rows of the ELL matrix (one 16-byte word per slot when RPT > 1)
+template <typename T, int WW, int RPT>
+struct EllRows {
+    VecT<int32_t, RPT> c[WW];
+    VecT<T, RPT> a[WW];
 };
 
-template <typename T, int WW>
+template <typename T, int WW, int RPT>
 __device__ __forceinline__ void ell_load(const int32_t* __restrict__ cols, const T* __restrict__ vals, int64_t rows,
-                                         int64_t q, EllRow<T, WW>& e)
+                                         int64_t q, EllRows<T, WW, RPT>& e)
 {
 #pragma unroll
     for (int k = 0; k < WW; ++k) {
-        e.c[k] = __ldg(cols + (int64_t)k * rows + q);
-        e.a[k] = __ldg(vals + (int64_t)k * rows + q);
+        e.c[k] = ldv<int32_t, RPT>(cols + (int64_t)k * rows, q);
+        e.a[k] = ldv<T, RPT>(vals + (int64_t)k * rows, q);
     }
 }
 
-template <typename T, int WW>
-__device__ __forceinline__ T ell_apply(const EllRow<T, WW>& e, const T* __restrict__ x, T self)
+template <typename T, int WW, int RPT>
+__device__ __forceinline__ void ell_apply(const EllRows<T, WW, RPT>& e, const T* __restrict__ x,
+                                          const VecT<T, RPT>& self, T (&y)[RPT])
 {
-    T xg[WW];
+    T xg[WW][RPT];
 #pragma unroll
-    for (int k = 0; k < WW; ++k) xg[k] = x[e.c[k]];
-    T acc = self;
+    for (int k = 0; k < WW; ++k)
 #pragma unroll
-    for (int k = 0; k < WW; ++k) acc = fma(e.a[k], xg[k], acc);
-    return acc;
+        for (int j = 0; j < RPT; ++j) xg[k][j] = x[e.c[k].v[j]];
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) {
+        T acc = self.v[j];
+#pragma unroll
+        for (int k = 0; k < WW; ++k) acc = fma(e.a[k].v[j], xg[k][j], acc);
+        y[j] = acc;
+    }
 }
 
 // Grid-stride bounds: threads of the whole grid, this thread's first index.
@@ -396,17 +411,24 @@ __device__ __forceinline__ void phase_spmv_dot(const int32_t* cols, const T* val
                                                const T* p, const T* rh, T* v, int64_t gtid, int64_t gstride,
                                                T (&acc)[1])
 {
-    if constexpr (spmv_pipelined(WW, RPT)) {
+    if constexpr (spmv_pipelined<T>(WW, RPT)) {
+        const int64_t ng = rows / RPT;
         int64_t q = gtid;
-        EllRow<T, WW> cur;
-        if (q < rows) ell_load<T, WW>(cols, vals, rows, q, cur);
-        for (; q < rows; q += gstride) {
-            EllRow<T, WW> nxt;
+        EllRows<T, WW, RPT> cur;
+        if (q < ng) ell_load<T, WW, RPT>(cols, vals, rows, q, cur);
+        for (; q < ng; q += gstride) {
+            EllRows<T, WW, RPT> nxt;
             const int64_t qn = q + gstride;
-            if (qn < rows) ell_load<T, WW>(cols, vals, rows, qn, nxt);
-            const T y = ell_apply<T, WW>(cur, p, p[q]);
-            v[q] = y;
-            acc[0] = fma(rh[q], y, acc[0]);
+            if (qn < ng) ell_load<T, WW, RPT>(cols, vals, rows, qn, nxt);
+            T y[RPT];
+            ell_apply<T, WW, RPT>(cur, p, ldv<T, RPT>(p, q), y);
+            VecT<T, RPT> yv;
+#pragma unroll
+            for (int j = 0; j < RPT; ++j) yv.v[j] = y[j];
+            stv<T, RPT>(v, q, yv);
+            const VecT<T, RPT> h = ldv<T, RPT>(rh, q);
+#pragma unroll
+            for (int j = 0; j < RPT; ++j) acc[0] = fma(h.v[j], y[j], acc[0]);
             cur = nxt;
         }
     }
@@ -454,20 +476,27 @@ template <typename T, int WW, int RPT>
 __device__ __forceinline__ void phase_spmv_dots2(const int32_t* cols, const T* vals, int W, int64_t rows,
                                                  const T* s, T* t, int64_t gtid, int64_t gstride, T (&acc)[3])
 {
-    if constexpr (spmv_pipelined(WW, RPT)) {
+    if constexpr (spmv_pipelined<T>(WW, RPT)) {
+        const int64_t ng = rows / RPT;
         int64_t q = gtid;
-        EllRow<T, WW> cur;
-        if (q < rows) ell_load<T, WW>(cols, vals, rows, q, cur);
-        for (; q < rows; q += gstride) {
-            EllRow<T, WW> nxt;
+        EllRows<T, WW, RPT> cur;
+        if (q < ng) ell_load<T, WW, RPT>(cols, vals, rows, q, cur);
+        for (; q < ng; q += gstride) {
+            EllRows<T, WW, RPT> nxt;
             const int64_t qn = q + gstride;
-            if (qn < rows) ell_load<T, WW>(cols, vals, rows, qn, nxt);
-            const T sq = s[q];
-            const T y = ell_apply<T, WW>(cur, s, sq);
-            acc[0] = fma(y, sq, acc[0]);
-            acc[1] = fma(y, y, acc[1]);
-            acc[2] = fma(sq, sq, acc[2]);
-            t[q] = y;
+            if (qn < ng) ell_load<T, WW, RPT>(cols, vals, rows, qn, nxt);
+            const VecT<T, RPT> sv = ldv<T, RPT>(s, q);
+            T y[RPT];
+            ell_apply<T, WW, RPT>(cur, s, sv, y);
+            VecT<T, RPT> yv;
+#pragma unroll
+            for (int j = 0; j < RPT; ++j) {
+                yv.v[j] = y[j];
+                acc[0] = fma(y[j], sv.v[j], acc[0]);
+                acc[1] = fma(y[j], y[j], acc[1]);
+                acc[2] = fma(sv.v[j], sv.v[j], acc[2]);
+            }
+            stv<T, RPT>(t, q, yv);
             cur = nxt;
         }
     }
