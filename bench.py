@@ -55,6 +55,7 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-box", action="store_true", help="skip the cuboid (box cell) leg")
+    ap.add_argument("--no-gmres", action="store_true", help="skip the GMRES leg")
     ap.add_argument("--learned-train", type=int, default=200,
                     help="online training steps of the learned form before its timed steps")
     ap.add_argument("--profile-run", action="store_true",
@@ -235,6 +236,39 @@ def box_leg(args, dev, world):
            "iterations_per_step": (it1 - it0) / args.steps, "kernels": kernel_table(s, L, hbm_peak)}
     s.close()
     return out
+
+
+def gmres_leg(args, dev, world):
+    """The FP64 form with restarted GMRES (the reference example's solver keys:
+    CGS, restart 30) on the same workload, warm-up and timed steps."""
+    import torch
+
+    from mhfem import problems
+
+    p = problems.diffusion3d(N=args.grid)
+    p.config.device = dev
+    s = problems.make_solver(p, check_every=8)
+    s.setup(tol=p.tol, max_iter=100000, check_every=8, linear_solver="gmres", gmres_restart=30, gmres_variant="cgs")
+    ext = torch.cuda.ExternalStream(s.stream(), device=dev)
+    t = 0.0
+    for _ in range(args.warmup):
+        s.step(t, p.dt)
+        t += p.dt
+    it0, _, _ = s.totals()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(ext)
+    for _ in range(args.steps):
+        s.step(t, p.dt)
+        t += p.dt
+    e1.record(ext)
+    e1.synchronize()
+    el = max_over_ranks(e0.elapsed_time(e1), world)
+    it1, _, _ = s.totals()
+    s.close()
+    return {"solver": "GMRES(30), classical Gram-Schmidt", "value": world * args.steps / (el / 1e3), "unit": UNIT,
+            "ms_per_step": el / args.steps, "iterations_per_step": (it1 - it0) / args.steps}
 
 
 def learned_leg(args, dev, world):
@@ -544,6 +578,8 @@ def main():
 
     if not args.no_learned:
         forms["learned"] = learned_leg(args, dev, world)
+    if not args.no_gmres:
+        forms["fp64_gmres"] = gmres_leg(args, dev, world)
     other_cells = None
     if not args.no_box:
         other_cells = {"cuboids": box_leg(args, dev, world)}

@@ -116,7 +116,18 @@ typedef struct {
     double  timeout_s;        /* host wall-clock limit of one solve (<= 0: none) */
     int32_t inner_adaptive;   /* mixed form: relax the last sweeps' inner tolerance to what the outer
                                  tolerance still needs (never tighter than inner_tol) */
+    int32_t linear_solver;    /* linear-solver (configSetup.h:32-38): MHFEM_SOLVER_BICGSTAB (default)
+                                 or MHFEM_SOLVER_GMRES; the FP64 and learned forms' solve (the mixed
+                                 form's inner solve is FP32 BiCGStab) */
+    int32_t gmres_restart;    /* gmres-restarting-max: restart length, 1 to 32 (default 30) */
+    int32_t gmres_variant;    /* gmres-variant: MHFEM_GMRES_CGS (default) or MHFEM_GMRES_CGSR
+                                 (classical Gram-Schmidt with one reorthogonalization pass) */
 } mhfem_solver_opts;
+
+#define MHFEM_SOLVER_BICGSTAB 0
+#define MHFEM_SOLVER_GMRES    1
+#define MHFEM_GMRES_CGS       0
+#define MHFEM_GMRES_CGSR      1
 
 typedef struct {
     int32_t iterations;       /* Krylov iterations (mixed: FP32 inner iterations, summed) */

@@ -36,7 +36,16 @@ def test_config_schema(tmp_path):
     cfg = config.parse(tmp_path / "config.ini")
     assert cfg["diffusivity"] == 1e-3 and cfg["convergence-residue"] == 1e-12
     assert cfg["initial-time"] == 0.0 and cfg["mesh-format"] == "auto"
-    assert any("BiCGStab" in n for n in cfg.notices)  # gmres requested
+    # the example's solver keys: GMRES with classical Gram-Schmidt, restart 30
+    assert cfg["_solver"] == "gmres" and cfg["_gmres_variant"] == "cgs" and cfg["_gmres_restart"] == 30
+    (tmp_path / "mgs.ini").write_text(CONFIG.replace("gmres-variant = CGS", "gmres-variant = MGS")
+                                      .replace("gmres-restarting-max = 30", "gmres-restarting-max = 50"))
+    c2 = config.parse(tmp_path / "mgs.ini")
+    assert c2["_gmres_variant"] == "cgsr" and c2["_gmres_restart"] == 32
+    assert any("CGSR" in n for n in c2.notices) and any("32" in n for n in c2.notices)
+    (tmp_path / "tfqmr.ini").write_text(CONFIG.replace("linear-solver = gmres", "linear-solver = tfqmr"))
+    c3 = config.parse(tmp_path / "tfqmr.ini")
+    assert c3["_solver"] == "bicgstab" and any("BiCGStab" in n for n in c3.notices)
     (tmp_path / "bad.ini").write_text(CONFIG + "no-such-key = 1\n")
     with pytest.raises(config.ConfigError, match="unknown"):
         config.parse(tmp_path / "bad.ini")

@@ -277,3 +277,56 @@ def test_box_vertex_order_is_checked():
         assert ei.value.status == L.ERR_INVALID_ARGUMENT
         s.setMesh(coords, cells)  # the canonical order is accepted
         s.close()
+
+
+GMRES_CASES = ["heat2d", "diffusion3d", "adr2d", "diffusion3d_box", "adr2d_rect_implicit_upwind", "diffusion3d_n3"]
+
+
+@pytest.mark.parametrize("variant", ["cgs", "cgsr"])
+@pytest.mark.parametrize("name", GMRES_CASES)
+def test_gmres_step_parity(name, variant):
+    """Restarted GMRES (the reference example's linear-solver = gmres) to a
+    relative residual of 1e-13: face traces and cell values within 1e-10 of
+    the oracle after every step, like the BiCGStab form."""
+    p = CASES[name]
+    s, m = _pair(p)
+    s.setup(tol=1e-13, max_iter=20000, check_every=4, linear_solver="gmres", gmres_restart=30,
+            gmres_variant=variant)
+    t = 0.0
+    for step in range(p.steps):
+        st = s.step(t, p.dt)
+        m.step(t, p.dt, 1e-13)
+        zf, zk = s.state()
+        assert st["residual"] < 1e-13 and st["iterations"] > 0
+        assert rel_err(zf, m.Z_iF) < TOL_STATE, f"step {step}: Z_iF"
+        assert rel_err(zk, m.Z_iK) < TOL_STATE, f"step {step}: Z_iK"
+        t += p.dt
+    s.close()
+
+
+def test_gmres_heat2d_full_size():
+    """The 128^2 heat-equation workload with the reference example's solver
+    keys (GMRES, CGS, restart 30) at tol 1e-12, 3 steps against the oracle."""
+    p = problems.heat2d(N=128, steps=3)
+    s, m = _pair(p, check_every=8)
+    s.setup(tol=1e-12, max_iter=20000, check_every=8, linear_solver="gmres", gmres_restart=30, gmres_variant="cgs")
+    t = 0.0
+    for _ in range(p.steps):
+        st = s.step(t, p.dt)
+        m.step(t, p.dt, 1e-13)
+        assert st["residual"] < 1e-12
+        t += p.dt
+    zf, zk = s.state()
+    assert rel_err(zf, m.Z_iF) < 1e-9
+    assert rel_err(zk, m.Z_iK) < 1e-9
+    s.close()
+
+
+def test_gmres_not_converged_is_reported():
+    p = problems.diffusion3d(N=6, steps=1)
+    s = problems.make_solver(p)
+    s.setup(tol=1e-14, max_iter=3, check_every=1, linear_solver="gmres", gmres_restart=2)
+    with pytest.raises(L.MhfemError) as ei:
+        s.step(0.0, p.dt)
+    assert ei.value.status == L.ERR_NOT_CONVERGED
+    s.close()

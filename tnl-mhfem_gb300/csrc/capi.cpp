@@ -105,7 +105,8 @@ void invalidate_graphs(mhfem_t h)
 {
     if (h->g64) cudaGraphExecDestroy(h->g64);
     if (h->g32) cudaGraphExecDestroy(h->g32);
-    h->g64 = h->g32 = nullptr;
+    if (h->ggm) cudaGraphExecDestroy(h->ggm);
+    h->g64 = h->g32 = h->ggm = nullptr;
     h->g64_iters = h->g32_iters = 0;
 }
 
@@ -177,6 +178,9 @@ void mhfem_default_solver_opts(mhfem_solver_opts* o)
     o->check_every = 8;
     o->timeout_s = 0;
     o->inner_adaptive = 1;
+    o->linear_solver = MHFEM_SOLVER_BICGSTAB;
+    o->gmres_restart = 30;
+    o->gmres_variant = MHFEM_GMRES_CGS;
 }
 
 mhfem_status mhfem_create(const mhfem_desc* desc, mhfem_t* out)
@@ -234,6 +238,7 @@ mhfem_status mhfem_destroy(mhfem_t h)
     for (void* p : h->allocs) cudaFree(p);
     h->allocs.clear();
     if (h->W.host_sc) cudaFreeHost(h->W.host_sc);
+    if (h->G.host) cudaFreeHost(h->G.host);
     if (h->host_err) cudaFreeHost(h->host_err);
     for (auto& e : h->ev)
         if (e) cudaEventDestroy(e);
@@ -270,6 +275,9 @@ mhfem_status mhfem_set_mesh(mhfem_t h, int64_t V, const double* coords, int64_t 
     KrylovScalars* keep = h->W.host_sc;
     h->W = KrylovWork();
     h->W.host_sc = keep;
+    GmresCtl* keep_gm = h->G.host;
+    h->G = GmresWork();
+    h->G.host = keep_gm;
     h->pattern_ready = false;
     h->has_bc = h->has_state = false;
 
@@ -442,7 +450,14 @@ mhfem_status mhfem_set_solver(mhfem_t h, const mhfem_solver_opts* o)
     if (!h || !o) return MHFEM_ERR_INVALID_ARGUMENT;
     if (!(o->tol > 0) || o->max_iter < 1 || o->check_every < 1 || !(o->inner_tol > 0) || o->max_sweeps < 1)
         return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "invalid solver options");
-    const bool regraph = (o->check_every != h->opts.check_every);
+    if (o->linear_solver != MHFEM_SOLVER_BICGSTAB && o->linear_solver != MHFEM_SOLVER_GMRES)
+        return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "unknown linear solver %d", o->linear_solver);
+    if (o->gmres_restart < 1 || o->gmres_restart > kGmresMaxM)
+        return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "gmres restart must be 1 to %d", kGmresMaxM);
+    if (o->gmres_variant != MHFEM_GMRES_CGS && o->gmres_variant != MHFEM_GMRES_CGSR)
+        return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "unknown gmres variant %d", o->gmres_variant);
+    const bool regraph = (o->check_every != h->opts.check_every) || (o->gmres_restart != h->opts.gmres_restart) ||
+                         (o->gmres_variant != h->opts.gmres_variant);
     h->opts = *o;
     if (regraph) invalidate_graphs(h);
     return MHFEM_OK;
@@ -520,6 +535,11 @@ mhfem_status ensure_pattern(mhfem_t h)
     CK(dalloc(h, &Wk.sc32, (size_t)1));
     CK(cudaMemset(Wk.sc, 0, sizeof(KrylovScalars)));
     CK(cudaMemset(Wk.sc32, 0, sizeof(KrylovScalars)));
+    // the GMRES basis follows the row count: reallocated at the next GMRES solve
+    dfree(h, h->G.U);
+    dfree(h, h->G.partials);
+    dfree(h, h->G.st);
+    h->G.m = 0;
     h->pattern_ready = true;
     return MHFEM_OK;
 }
@@ -567,11 +587,86 @@ double elapsed_s(std::chrono::steady_clock::time_point t0)
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
 
+mhfem_status status_from_gmres(mhfem_t h, const GmresCtl& c)
+{
+    switch (c.status) {
+        case KS_CONVERGED: return MHFEM_OK;
+        case KS_MAXITER:
+            return fail(h, MHFEM_ERR_NOT_CONVERGED,
+                        "MHFEM error: the linear system solver did not converge (%d iterations, GMRES, residual %.3e)",
+                        c.it, c.res);
+        case KS_NOTFINITE: return fail(h, MHFEM_ERR_NOT_FINITE, "GMRES: non-finite value after %d iterations", c.it);
+    }
+    return fail(h, MHFEM_ERR_STATE, "GMRES: unexpected status %d", c.status);
+}
+
+// Restarted GMRES from the current Z_iF: CUDA graphs of check_every Arnoldi
+// iterations between host checks; at the end of each cycle the host runs the
+// small solve, the update of x and the restart from the true residual.
+mhfem_status run_gmres(mhfem_t h, double tol, int max_iter, int* iters, double* res)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    const int m = h->opts.gmres_restart;
+    const int64_t rows = h->A.rows;
+    GmresWork& G = h->G;
+    if (G.m != m || !G.U) {
+        dfree(h, G.U);
+        dfree(h, G.partials);
+        dfree(h, G.st);
+        if (h->ggm) { cudaGraphExecDestroy(h->ggm); h->ggm = nullptr; }
+        CK(dalloc(h, &G.U, (size_t)(m + 1) * rows));
+        CK(dalloc(h, &G.partials, (size_t)krylov_grid() * kGmStride));
+        CK(dalloc(h, &G.st, (size_t)1));
+        G.m = m;
+    }
+    if (!G.host) CK(cudaMallocHost((void**)&G.host, sizeof(GmresCtl)));
+    GmresState init{};
+    init.tol = tol;
+    init.m = m;
+    init.max_iter = max_iter;
+    CK(cudaMemcpyAsync(G.st, &init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
+    gmres_init(h->A, h->rhs, h->Z_iF, G, h->W, true, h->stream);
+    h->launches += 1;
+    CK(cudaMemcpyAsync(G.host, &G.st->ctl, sizeof(GmresCtl), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaGetLastError());
+    const bool reorth = h->opts.gmres_variant == MHFEM_GMRES_CGSR;
+    if (!h->ggm) {
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        gmres_iterate(h->A, G, h->W, h->opts.check_every, reorth, h->stream);
+        cudaMemcpyAsync(G.host, &G.st->ctl, sizeof(GmresCtl), cudaMemcpyDeviceToHost, h->stream);
+        CK(cudaStreamEndCapture(h->stream, &g));
+        const cudaError_t e = cudaGraphInstantiate(&h->ggm, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(h, MHFEM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    }
+    while (!G.host->done) {
+        if (G.host->cycle_end) {
+            gmres_update(h->Z_iF, G, rows, h->stream);
+            gmres_init(h->A, h->rhs, h->Z_iF, G, h->W, false, h->stream);
+            h->launches += 3;
+            CK(cudaMemcpyAsync(G.host, &G.st->ctl, sizeof(GmresCtl), cudaMemcpyDeviceToHost, h->stream));
+        }
+        else {
+            CK(cudaGraphLaunch(h->ggm, h->stream));
+            h->launches += (reorth ? 4 : 2) * h->opts.check_every;
+        }
+        CK(cudaStreamSynchronize(h->stream));
+        if (h->opts.timeout_s > 0 && elapsed_s(t0) > h->opts.timeout_s)
+            return fail(h, MHFEM_ERR_TIMEOUT, "Krylov solve exceeded %.1f s", h->opts.timeout_s);
+    }
+    *iters = G.host->it;
+    *res = G.host->res;
+    return status_from_gmres(h, *G.host);
+}
+
 }  // namespace
 
 // Runs FP64 BiCGStab from the current Z_iF until the device flag says done.
 mhfem_status mhfem::run_fp64(mhfem_t h, double tol, int max_iter, int* iters, double* res)
 {
+    if (h->opts.linear_solver == MHFEM_SOLVER_GMRES) return run_gmres(h, tol, max_iter, iters, res);
     const auto t0 = std::chrono::steady_clock::now();
     krylov_init_fp64(h->A, h->rhs, h->Z_iF, h->W, tol, max_iter, h->stream);
     CK(cudaMemcpyAsync(h->W.host_sc, h->W.sc, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, h->stream));

@@ -62,6 +62,7 @@ struct mhfem_solver_s {
     int32_t* err_flags = nullptr;
     int32_t* host_err = nullptr;
     mhfem::KrylovWork W;
+    mhfem::GmresWork G;
 
     mhfem_solver_opts opts{};
     // the matrix keeps an FP32 copy and the FP32 Krylov vectors exist: the
@@ -70,7 +71,7 @@ struct mhfem_solver_s {
     int64_t total_iters = 0, total_steps = 0, launches = 0;
     double cur_t = 0, cur_tau = 0;
 
-    cudaGraphExec_t g64 = nullptr, g32 = nullptr;
+    cudaGraphExec_t g64 = nullptr, g32 = nullptr, ggm = nullptr;  // ggm: GMRES iterations
     int g64_iters = 0, g32_iters = 0;
 
     cudaEvent_t ev[7] = {};  // phase boundaries 0..4; 5, 6: the learned guess

@@ -1,0 +1,305 @@
+// Restarted GMRES on the unit-diagonal face system (sm_103a), FP64.
+//
+// The reference's own example configuration selects it
+// (examples/HeatEquation/config.ini: linear-solver = gmres, gmres-variant =
+// CGS, gmres-restarting-max = 30) through the solver factory of
+// Solver::setup (Solver.hpp:192-204; configSetup.h:32-62).  TNL's
+// implementation is not in the reference tree; this restates the published
+// algorithm (Saad and Schultz, "GMRES: a generalized minimal residual
+// algorithm for solving nonsymmetric linear systems", 1986): Arnoldi with
+// classical Gram-Schmidt (optionally one reorthogonalization pass), Givens
+// rotations of the Hessenberg matrix, the least-squares solution at the end
+// of a cycle and restarts from the true residual.  The restart length is
+// fixed (gmres-restarting-max); TNL's adaptive choice between
+// gmres-restarting-min and -max is not reproduced, which changes iteration
+// counts, not the converged solution.
+//
+// Design for GB300:
+//  - the basis is stored unnormalized (v_i = inv_i u_i), so no pass only
+//    scales a vector: an Arnoldi iteration is two kernels (four with the
+//    reorthogonalization):
+//      k_gm_arnoldi: z = A u_j (unit-diagonal SpMV) stored as u_{j+1}, with
+//                    the j+1 dot products (z, u_i) in the same pass;
+//      k_gm_orth:    u_{j+1} -= sum_i c_i u_i and ||u_{j+1}||^2;
+//    the last block of k_gm_orth rotates the new Hessenberg column on the
+//    device and decides whether the cycle ends, so an iteration needs no
+//    host round trip;
+//  - reductions are deterministic (fixed grid, one partial per block, the
+//    last block sums them in a fixed order);
+//  - every iteration kernel returns at once when the cycle has ended or the
+//    solve is done, so the host replays a CUDA graph of several iterations
+//    between checks.
+#include <initializer_list>
+
+#include "krylov_common.cuh"
+
+namespace mhfem {
+
+constexpr int kGmDots = kGmresMaxM + 1;
+static_assert(kGmDots <= kGmStride && kGmDots <= KB, "GMRES dot products per block");
+
+// r = b - A x -> u_0 and the restart scalars; first: also ||b|| and it = 0.
+// The true residual decides convergence (the rotated estimate only ends a
+// cycle early).
+template <int WW>
+__global__ void __launch_bounds__(KB) k_gm_init(const int32_t* cols, const double* vals, int W, int64_t rows,
+                                                const double* b, const double* x, double* U, GmresState* st,
+                                                int first, double* partials, uint32_t* counter)
+{
+    double acc[2] = {0, 0};
+    for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB) {
+        const double bq = b[q];
+        const double r = bq - spmv_row<double, WW>(cols, vals, W, rows, q, x);
+        U[q] = r;
+        acc[0] = fma(r, r, acc[0]);
+        acc[1] = fma(bq, bq, acc[1]);
+    }
+    block_reduce_store<double, 2>(acc, partials);
+    if (!ticket_last(counter)) return;
+    double s[2];
+    final_sums<2>(partials, s);
+    if (threadIdx.x == 0) {
+        GmresCtl& c = st->ctl;
+        if (first) {
+            double bn = sqrt(s[1]);
+            if (bn == 0) bn = 1;
+            c.bnorm = bn;
+            c.it = 0;
+            c.status = KS_RUNNING;
+            c.done = 0;
+        }
+        const double beta = sqrt(s[0]);
+        c.res = beta / c.bnorm;
+        st->g[0] = beta;
+        st->inv[0] = beta > 0 ? 1.0 / beta : 0.0;
+        st->j = 0;
+        c.cycle_end = 0;
+        if (!finite(c.res)) { c.status = KS_NOTFINITE; c.done = 1; }
+        else if (c.res < st->tol) { c.status = KS_CONVERGED; c.done = 1; }
+        else if (c.it >= st->max_iter) { c.status = KS_MAXITER; c.done = 1; }
+    }
+}
+
+// The dot products are taken in chunks of kGmChunk basis vectors: a pass
+// over the rows per chunk with kGmChunk accumulators per thread (re-reading
+// the row's z, 8 bytes, per chunk), which keeps registers low and the
+// per-row work exact.
+constexpr int kGmChunk = 8;
+
+// Block sums of the per-thread dot products of one chunk into
+// partials[block][c0 .. c0 + n - 1]: warp shuffles, then thread k adds value
+// k over the warps in order.
+__device__ __forceinline__ void gm_block_dots(const double (&acc)[kGmChunk], int c0, int n, double* partials)
+{
+    __shared__ double sh[KB / 32][kGmChunk];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < kGmChunk; ++k) {
+        double v = acc[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[warp][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < n) {
+        double s = 0;
+        for (int w = 0; w < KB / 32; ++w) s += sh[w][threadIdx.x];
+        partials[(int64_t)blockIdx.x * kGmStride + c0 + threadIdx.x] = s;
+    }
+    __syncthreads();  // sh is reused by the next chunk
+}
+
+// The last block sums value i (i <= j) over the blocks in a fixed order:
+// warp w takes i = w, w + 8, ...; its lanes stride over the blocks.
+__device__ __forceinline__ void gm_final_dots(const double* partials, int j, double* out)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nb = (int)gridDim.x;
+    for (int i = warp; i <= j; i += KB / 32) {
+        double s = 0;
+        for (int b = lane; b < nb; b += 32) s += __ldcg(partials + (int64_t)b * kGmStride + i);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) out[i] = s;
+    }
+    __syncthreads();
+}
+
+// SPMV: z = A u_j -> u_{j+1}, d_i = (z, u_i); else (the reorthogonalization
+// pass) d_i = (u_{j+1}, u_i).  The last block turns d into the Hessenberg
+// entries h_ij = (A v_j, v_i) = inv_j inv_i d_i (added to them on the second
+// pass) and the multipliers c_i = inv_i^2 d_i of the orthogonalization.
+template <int WW, bool SPMV>
+__global__ void __launch_bounds__(KB) k_gm_arnoldi(const int32_t* cols, const double* vals, int W, int64_t rows,
+                                                   double* U, GmresState* st, double* partials, uint32_t* counter)
+{
+    pdl_wait();
+    if (st->ctl.done || st->ctl.cycle_end) {
+        pdl_release();
+        return;
+    }
+    const int j = st->j;
+    const double* uj = U + (int64_t)j * rows;
+    double* un = U + (int64_t)(j + 1) * rows;
+    for (int c0 = 0; c0 <= j; c0 += kGmChunk) {
+        const int n = (j + 1 - c0 < kGmChunk) ? j + 1 - c0 : kGmChunk;
+        double acc[kGmChunk];
+#pragma unroll
+        for (int k = 0; k < kGmChunk; ++k) acc[k] = 0;
+        for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB) {
+            double z;
+            if (SPMV && c0 == 0) {  // the first chunk forms z = A u_j; later chunks re-read it
+                z = spmv_row<double, WW>(cols, vals, W, rows, q, uj);
+                un[q] = z;
+            }
+            else
+                z = un[q];
+            if (n == kGmChunk) {
+#pragma unroll
+                for (int k = 0; k < kGmChunk; ++k) acc[k] = fma(z, U[(int64_t)(c0 + k) * rows + q], acc[k]);
+            }
+            else
+                for (int k = 0; k < n; ++k) acc[k] = fma(z, U[(int64_t)(c0 + k) * rows + q], acc[k]);
+        }
+        gm_block_dots(acc, c0, n, partials);
+    }
+    pdl_release();
+    if (!ticket_last(counter)) return;
+    __shared__ double d[kGmDots];
+    gm_final_dots(partials, j, d);
+    if (threadIdx.x == 0) {
+        const double invj = st->inv[j];
+        for (int i = 0; i <= j; ++i) {
+            const double invi = st->inv[i];
+            const double h = invj * invi * d[i];
+            if constexpr (SPMV) st->H[i][j] = h;
+            else st->H[i][j] += h;
+            st->c[i] = invi * invi * d[i];
+        }
+    }
+}
+
+// u_{j+1} -= sum_i c_i u_i.  FINAL: ||u_{j+1}||, h_{j+1,j} = inv_j ||u_{j+1}||,
+// the earlier Givens rotations applied to column j and a new one that zeroes
+// h_{j+1,j}, the rotated right-hand side g and the residual estimate
+// |g_{j+1}| / ||b||; the cycle ends on that estimate, after m columns, on a
+// breakdown (u_{j+1} = 0: the solution lies in the current space) or at the
+// iteration cap.
+template <bool FINAL>
+__global__ void __launch_bounds__(KB) k_gm_orth(int64_t rows, double* U, GmresState* st, double* partials,
+                                                uint32_t* counter)
+{
+    pdl_wait();
+    if (st->ctl.done || st->ctl.cycle_end) {
+        pdl_release();
+        return;
+    }
+    const int j = st->j;
+    __shared__ double c[kGmDots];
+    if (threadIdx.x <= j) c[threadIdx.x] = st->c[threadIdx.x];
+    __syncthreads();
+    double* un = U + (int64_t)(j + 1) * rows;
+    double acc[1] = {0};
+    for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB) {
+        double t = un[q];
+#pragma unroll 4
+        for (int i = 0; i <= j; ++i) t = fma(-c[i], U[(int64_t)i * rows + q], t);
+        un[q] = t;
+        if constexpr (FINAL) acc[0] = fma(t, t, acc[0]);
+    }
+    pdl_release();
+    if constexpr (FINAL) {
+        block_reduce_store<double, 1>(acc, partials);
+        if (!ticket_last(counter)) return;
+        double s[1];
+        final_sums<1>(partials, s);
+        if (threadIdx.x == 0) {
+            GmresCtl& C = st->ctl;
+            const double nrm = sqrt(s[0]);
+            const double hn = st->inv[j] * nrm;  // h_{j+1,j}
+            for (int k = 0; k < j; ++k) {
+                const double a = st->H[k][j], b = st->H[k + 1][j];
+                st->H[k][j] = st->cs[k] * a + st->sn[k] * b;
+                st->H[k + 1][j] = -st->sn[k] * a + st->cs[k] * b;
+            }
+            const double a = st->H[j][j];
+            const double den = sqrt(a * a + hn * hn);
+            const double cs = den > 0 ? a / den : 1.0, sn = den > 0 ? hn / den : 0.0;
+            st->cs[j] = cs;
+            st->sn[j] = sn;
+            st->H[j][j] = den;
+            st->g[j + 1] = -sn * st->g[j];
+            st->g[j] = cs * st->g[j];
+            st->inv[j + 1] = nrm > 0 ? 1.0 / nrm : 0.0;
+            const double res = fabs(st->g[j + 1]) / C.bnorm;
+            C.res = res;
+            C.it += 1;
+            st->j = j + 1;
+            if (!finite(res) || !finite(den)) { C.status = KS_NOTFINITE; C.done = 1; }
+            else if (res < st->tol || j + 1 >= st->m || nrm == 0 || C.it >= st->max_iter) C.cycle_end = 1;
+        }
+    }
+}
+
+// End of a cycle: back substitution R y = g over the k = j columns, then the
+// multipliers of x += sum_i y_i v_i = sum_i (y_i inv_i) u_i.
+__global__ void k_gm_solve(GmresState* st)
+{
+    if (threadIdx.x != 0 || st->ctl.done) return;
+    const int k = st->j;
+    double y[kGmresMaxM];
+    for (int i = k - 1; i >= 0; --i) {
+        double s = st->g[i];
+        for (int l = i + 1; l < k; ++l) s -= st->H[i][l] * y[l];
+        y[i] = s / st->H[i][i];
+    }
+    for (int i = 0; i < kGmDots; ++i) st->c[i] = (i < k) ? y[i] * st->inv[i] : 0.0;
+}
+
+__global__ void __launch_bounds__(KB) k_gm_update_x(int64_t rows, const double* U, double* x, const GmresState* st)
+{
+    if (st->ctl.done) return;
+    const int k = st->j;
+    __shared__ double c[kGmDots];
+    if (threadIdx.x < kGmDots) c[threadIdx.x] = st->c[threadIdx.x];
+    __syncthreads();
+    for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB) {
+        double t = x[q];
+#pragma unroll 4
+        for (int i = 0; i < k; ++i) t = fma(c[i], U[(int64_t)i * rows + q], t);
+        x[q] = t;
+    }
+}
+
+// ---- launchers --------------------------------------------------------------
+
+void gmres_init(const EllMatrix& A, const double* b, const double* x, GmresWork& G, KrylovWork& W, bool first,
+                cudaStream_t s)
+{
+    MHFEM_WIDTH_DISPATCH(A.width, (k_gm_init<WW><<<occ_grid(k_gm_init<WW>), KB, 0, s>>>(
+                                      A.cols, A.vals, A.width, A.rows, b, x, G.U, G.st, first ? 1 : 0, W.partials,
+                                      W.counters)));
+}
+
+void gmres_iterate(const EllMatrix& A, GmresWork& G, KrylovWork& W, int iters, bool reorth, cudaStream_t s)
+{
+    for (int it = 0; it < iters; ++it) {
+        MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_gm_arnoldi<WW, true>, s, (const int32_t*)A.cols,
+                                                 (const double*)A.vals, A.width, A.rows, G.U, G.st, G.partials,
+                                                 W.counters));
+        if (reorth) {
+            launch_pdl(k_gm_orth<false>, s, A.rows, G.U, G.st, W.partials, W.counters);
+            launch_pdl(k_gm_arnoldi<0, false>, s, (const int32_t*)A.cols, (const double*)A.vals, A.width, A.rows,
+                       G.U, G.st, G.partials, W.counters);
+        }
+        launch_pdl(k_gm_orth<true>, s, A.rows, G.U, G.st, W.partials, W.counters);
+    }
+}
+
+void gmres_update(double* x, GmresWork& G, int64_t rows, cudaStream_t s)
+{
+    k_gm_solve<<<1, 32, 0, s>>>(G.st);
+    k_gm_update_x<<<occ_grid(k_gm_update_x), KB, 0, s>>>(rows, G.U, x, G.st);
+}
+
+}  // namespace mhfem

@@ -1,0 +1,238 @@
+#pragma once
+// Building blocks shared by the Krylov solvers (k_krylov.cu: BiCGStab, FP64
+// and FP32; k_gmres.cu: restarted GMRES): launch shapes, deterministic
+// block reductions with a last-block ticket, programmatic dependent launch,
+// the unit-diagonal ELL row product and vector access helpers.
+#include <mutex>
+#include <unordered_map>
+#include <utility>
+
+#include "mhfem_internal.h"
+
+namespace mhfem {
+
+constexpr int KB = 256;
+
+// Grid of a grid-stride kernel: as many CTAs of KB threads as can be resident
+// at once on every SM (fixed per kernel and device, so reductions stay
+// deterministic).
+template <typename Kern>
+static int occ_grid(Kern kernel)
+{
+    static std::mutex mu;
+    static std::unordered_map<const void*, int> cache;
+    static int sms = 0;
+    std::lock_guard<std::mutex> lock(mu);
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 152;
+    }
+    auto it = cache.find((const void*)kernel);
+    if (it != cache.end()) return it->second;
+    int nb = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, KB, 0);
+    const int g = sms * (nb > 0 ? (nb < 8 ? nb : 8) : 1);
+    cache[(const void*)kernel] = g;
+    return g;
+}
+
+// Launches an iteration kernel (one wave, occ_grid CTAs) with programmatic
+// stream serialization, so that its CTAs are scheduled while the preceding
+// kernel of the iteration drains (the kernel itself waits for that kernel's
+// results with griddepcontrol.wait).  Captured into a CUDA graph this becomes
+// a programmatic dependency edge.
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*kernel)(KArgs...), cudaStream_t s, Args&&... args)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)occ_grid(kernel));
+    cfg.blockDim = dim3(KB);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+// Compile-time ELL widths (2f - 1) n - 1 of the common cases: triangles
+// (4, 9), tetrahedra and rectangles (6, 13) with one or two components,
+// cuboids with one (10); other widths (three components, two-component
+// cuboids, meshes without interior faces) take the run-time loop.
+#define MHFEM_WIDTH_DISPATCH(W, CALL)                                   \
+    do {                                                                \
+        switch (W) {                                                    \
+            case 4: { constexpr int WW = 4; CALL; } break;              \
+            case 6: { constexpr int WW = 6; CALL; } break;              \
+            case 9: { constexpr int WW = 9; CALL; } break;              \
+            case 10: { constexpr int WW = 10; CALL; } break;            \
+            case 13: { constexpr int WW = 13; CALL; } break;            \
+            default: { constexpr int WW = 0; CALL; } break;             \
+        }                                                               \
+    } while (0)
+// restart threshold of |(rh, r)| relative to ||r|| ||rh|| (same as the oracle)
+constexpr double kRestartEps = 1e-14;
+
+// Per-block partial sums: up to kPartStride values per block.
+constexpr int kPartStride = 8;
+
+template <typename T, int NV>
+__device__ __forceinline__ void block_reduce_store(T (&acc)[NV], double* partials)
+{
+    static_assert(NV <= kPartStride, "too many partial sums");
+    __shared__ double sh[KB / 32][kPartStride];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        T v = acc[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[warp][q] = (double)v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            double s = 0;
+            for (int w = 0; w < KB / 32; ++w) s += sh[w][q];
+            partials[(int64_t)blockIdx.x * kPartStride + q] = s;
+        }
+    }
+}
+
+// Returns true in the last block to finish; that block then sees every
+// partial.  Thread 0 wrote this block's partial, so only thread 0 fences
+// before taking its ticket (the other threads' stores need no ordering: the
+// last block reads partials only).  The counter is reset for the next launch.
+__device__ __forceinline__ bool ticket_last(uint32_t* counter)
+{
+    __shared__ bool last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const uint32_t prev = atomicAdd(counter, 1u);
+        last = (prev == gridDim.x - 1);
+        if (last) *counter = 0;
+    }
+    __syncthreads();
+    return last;
+}
+
+// Deterministic sum of the partials by the last block (fixed order): every
+// thread issues its (at most four per pass) partial loads together, the warp
+// sums them with shuffles and warp 0 adds the eight warp sums in order.
+template <int NV>
+__device__ __forceinline__ void final_sums(const double* partials, double (&out)[NV])
+{
+    __shared__ double sh[KB / 32][kPartStride];
+    double acc[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) acc[q] = 0;
+    const int nb = (int)gridDim.x;
+    for (int b0 = threadIdx.x; b0 < nb; b0 += 4 * KB) {
+        double v[4][NV];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int b = b0 + j * KB;
+#pragma unroll
+            for (int q = 0; q < NV; ++q) v[j][q] = (b < nb) ? __ldcg(partials + (int64_t)b * kPartStride + q) : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int q = 0; q < NV; ++q) acc[q] += v[j][q];
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        double v = acc[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[warp][q] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        double t = 0;
+#pragma unroll
+        for (int w = 0; w < KB / 32; ++w) t += sh[w][q];
+        out[q] = t;
+    }
+}
+
+// Programmatic dependent launch: the iteration kernels are launched with
+// programmatic stream serialization, so the next kernel's CTAs are scheduled
+// while this one drains.  pdl_wait() blocks until the preceding kernel has
+// completed and its writes are visible (a no-op for an ordinary launch);
+// every kernel calls it before its first global access and releases its
+// dependent right after.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// y_r = x_r + sum_k vals[k][r] x[cols[k][r]] (unit diagonal).  With a
+// compile-time width WW every column and value load of the row is issued
+// before the gathers, so all of a row's memory accesses are in flight at once.
+template <typename T, int WW>
+__device__ __forceinline__ T spmv_row(const int32_t* __restrict__ cols, const T* __restrict__ vals, int W,
+                                      int64_t rows, int64_t r, const T* __restrict__ x)
+{
+    if constexpr (WW > 0) {
+        int32_t c[WW];
+        T v[WW];
+#pragma unroll
+        for (int k = 0; k < WW; ++k) {
+            c[k] = __ldg(cols + (int64_t)k * rows + r);
+            v[k] = __ldg(vals + (int64_t)k * rows + r);
+        }
+        T xg[WW];
+#pragma unroll
+        for (int k = 0; k < WW; ++k) xg[k] = x[c[k]];
+        T y = x[r];
+#pragma unroll
+        for (int k = 0; k < WW; ++k) y = fma(v[k], xg[k], y);
+        return y;
+    }
+    else {
+        T y = x[r];
+        for (int k = 0; k < W; ++k) {
+            const int64_t o = (int64_t)k * rows + r;
+            y = fma(__ldg(vals + o), x[__ldg(cols + o)], y);
+        }
+        return y;
+    }
+}
+
+__device__ __forceinline__ bool finite(double v) { return isfinite(v); }
+
+// ---- vector access -------------------------------------------------------------
+//
+// The iteration kernels move V consecutive rows per thread and access (float4,
+// double2: 16-byte loads and stores) so that enough bytes are in flight per SM
+// to saturate HBM; the SpMVs of the FP32 solve also process RPT consecutive
+// rows per thread, loading each ELL slot of the RPT rows as one 16-byte word.
+// The host picks V and RPT from the pointers' alignment and the row count.
+
+template <typename T, int V>
+struct alignas(sizeof(T) * V) VecT {
+    T v[V];
+};
+
+template <typename T, int V>
+__device__ __forceinline__ VecT<T, V> ldv(const T* p, int64_t q)
+{
+    return *reinterpret_cast<const VecT<T, V>*>(p + q * V);
+}
+
+template <typename T, int V>
+__device__ __forceinline__ void stv(T* p, int64_t q, const VecT<T, V>& x)
+{
+    *reinterpret_cast<VecT<T, V>*>(p + q * V) = x;
+}
+
+static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+}  // namespace mhfem

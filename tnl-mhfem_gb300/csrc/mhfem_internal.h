@@ -150,6 +150,48 @@ struct KrylovWork {
 
 void krylov_init_fp64(const EllMatrix& A, const double* b, double* x, KrylovWork& W,
                       double tol, int max_iter, cudaStream_t s);
+
+// ---- restarted GMRES (k_gmres.cu) ---------------------------------------------
+
+constexpr int kGmresMaxM = 32;  // longest restart cycle
+constexpr int kGmStride = 40;   // partial sums per block of the Arnoldi dot products (>= kGmresMaxM + 1)
+
+// The part of the GMRES state the host polls (one small copy per check).
+struct GmresCtl {
+    int32_t it, done, status, cycle_end;
+    double res;    // ||b - A x|| / ||b|| at the last restart, or the rotated estimate inside a cycle
+    double bnorm;
+};
+
+// Device state of one GMRES solve.  The basis is stored unnormalized:
+// v_i = inv[i] * u_i.  H holds the Hessenberg columns of the cycle, rotated
+// in place into the triangular factor; g is the rotated right-hand side.
+struct GmresState {
+    GmresCtl ctl;
+    double tol;
+    int32_t m, j, max_iter, pad;
+    double inv[kGmresMaxM + 1];
+    double c[kGmresMaxM + 1];  // multipliers of u_i in the current orthogonalization / x update
+    double H[kGmresMaxM + 1][kGmresMaxM];
+    double cs[kGmresMaxM], sn[kGmresMaxM];
+    double g[kGmresMaxM + 1];
+};
+
+struct GmresWork {
+    int m = 0;
+    double* U = nullptr;          // [m + 1][rows] basis
+    double* partials = nullptr;   // [grid][kGmStride]
+    GmresState* st = nullptr;     // device
+    GmresCtl* host = nullptr;     // pinned mirror of st->ctl
+};
+
+// r = b - A x into u_0 and the restart scalars; first: also ||b|| and it = 0
+void gmres_init(const EllMatrix& A, const double* b, const double* x, GmresWork& G, KrylovWork& W,
+                bool first, cudaStream_t s);
+// `iters` Arnoldi iterations (each returns at once after the cycle ended)
+void gmres_iterate(const EllMatrix& A, GmresWork& G, KrylovWork& W, int iters, bool reorth, cudaStream_t s);
+// end of a cycle: solve the triangular system and update x
+void gmres_update(double* x, GmresWork& G, int64_t rows, cudaStream_t s);
 void krylov_iterate_fp64(const EllMatrix& A, double* x, KrylovWork& W, int iters, cudaStream_t s);
 
 // mixed: outer residual r = b - A x (FP64) -> sc; scale into r32; inner FP32 solve; x += scale*e

@@ -57,7 +57,12 @@ CELL_BOX = 1
 class SolverOpts(ct.Structure):
     _fields_ = [("tol", ct.c_double), ("max_iter", ct.c_int32), ("inner_tol", ct.c_double),
                 ("max_sweeps", ct.c_int32), ("check_every", ct.c_int32), ("timeout_s", ct.c_double),
-                ("inner_adaptive", ct.c_int32)]
+                ("inner_adaptive", ct.c_int32), ("linear_solver", ct.c_int32), ("gmres_restart", ct.c_int32),
+                ("gmres_variant", ct.c_int32)]
+
+
+SOLVER_BICGSTAB, SOLVER_GMRES = 0, 1
+GMRES_CGS, GMRES_CGSR = 0, 1
 
 
 class LearnedOpts(ct.Structure):

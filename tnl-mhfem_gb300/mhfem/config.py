@@ -54,6 +54,7 @@ SCHEMA = {
 }
 
 LINEAR_SOLVERS = {"bicgstab", "bicgstabl", "gmres", "cg", "tfqmr", "idrs", "sor", "jacobi"}
+GMRES_VARIANTS = {"CGS", "CGSR", "MGS", "MGSR", "CWY"}
 PRECONDITIONERS = {"none", "diagonal", "ilu0", "ilut"}
 MESH_FORMATS = {"auto", "vtk", "vtu", "ng"}
 
@@ -104,9 +105,29 @@ def parse(path, overrides: dict | None = None) -> Config:
     solver = values["linear-solver"].lower()
     if solver not in LINEAR_SOLVERS:
         raise ConfigError(f"linear-solver {solver!r} is not a TNL solver name")
-    if solver != "bicgstab":
-        notices.append(f"linear-solver = {solver}: this library's Krylov solver is BiCGStab; it runs with the "
-                       "same convergence-residue and max-iterations")
+    # the solver this library runs: BiCGStab or restarted GMRES (the others map to BiCGStab)
+    values["_solver"], values["_gmres_restart"], values["_gmres_variant"] = "bicgstab", 30, "cgs"
+    if solver == "gmres":
+        values["_solver"] = "gmres"
+        variant = (values["gmres-variant"] or "CGS").upper()
+        if variant not in GMRES_VARIANTS:
+            raise ConfigError(f"gmres-variant {variant!r} is not one of {sorted(GMRES_VARIANTS)}")
+        if variant in ("MGS", "MGSR", "CWY"):
+            notices.append(f"gmres-variant = {variant}: runs as CGSR (classical Gram-Schmidt with one "
+                           "reorthogonalization pass, which keeps the basis as orthogonal as MGS does)")
+            variant = "CGSR"
+        values["_gmres_variant"] = variant.lower()
+        restart = values["gmres-restarting-max"] or 30
+        if restart > 32:
+            notices.append(f"gmres-restarting-max = {restart}: restarts after 32 iterations (the longest cycle)")
+            restart = 32
+        if values["gmres-restarting-min"] is not None and values["gmres-restarting-min"] != restart:
+            notices.append("gmres-restarting-min/-step: the restart length is fixed at gmres-restarting-max "
+                           f"({restart})")
+        values["_gmres_restart"] = int(restart)
+    elif solver != "bicgstab":
+        notices.append(f"linear-solver = {solver}: this library's Krylov solvers are BiCGStab and GMRES; it "
+                       "runs BiCGStab with the same convergence-residue and max-iterations")
     prec = values["preconditioner"].lower()
     if prec not in PRECONDITIONERS:
         raise ConfigError(f"preconditioner {prec!r} is not a TNL preconditioner name")

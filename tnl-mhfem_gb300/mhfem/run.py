@@ -100,7 +100,8 @@ def run(cfg: config.Config, log: Logger, device: int = 0) -> dict:
     else:
         z0 = np.zeros(s.C)
     s.setup(tol=cfg["convergence-residue"], max_iter=min(cfg["max-iterations"], 2 ** 31 - 1),
-            inner_tol=cfg["inner-tolerance"])
+            inner_tol=cfg["inner-tolerance"], linear_solver=cfg["_solver"], gmres_restart=cfg["_gmres_restart"],
+            gmres_variant=cfg["_gmres_variant"])
     if cfg["solver-form"] == "learned":
         s.learned_options(train_steps=cfg["learned-train-steps"])
     s.setInitialCondition(z0)
@@ -114,6 +115,8 @@ def run(cfg: config.Config, log: Logger, device: int = 0) -> dict:
     log.param("Mesh type:", ("rectangles" if dim == 2 else "cuboids") if box else
               ("triangles" if dim == 2 else "tetrahedra"))
     log.param("Sparse matrix:", "ELL (off-diagonal part, unit diagonal)")
+    log.param("Linear solver:", f"GMRES({cfg['_gmres_restart']}, {cfg['_gmres_variant'].upper()})"
+              if cfg["_solver"] == "gmres" else "BiCGStab")
     log.param("Mass lumping:", cfg["mass-lumping"])
     log.param("Advection discretization:", "explicit upwind")
     log.param("Solver form:", cfg["solver-form"])
