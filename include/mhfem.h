@@ -153,10 +153,14 @@ void         mhfem_default_solver_opts(mhfem_solver_opts* opts);
 /* ---- setup -------------------------------------------------------------- */
 
 /* Replaces Solver::setMesh (Solver.hpp:28-80) after MHFEM::init loaded the
- * mesh (control.h:15-47).  cell_verts is [C][dim+1]; local vertex e is
- * opposite local face e (the convention MassMatrix.h:538 relies on).  The
- * library numbers the faces in order of first appearance over the cells
- * and their local faces. */
+ * mesh (control.h:15-47).  Simplices: cell_verts is [C][dim+1]; local
+ * vertex e is opposite local face e (the convention MassMatrix.h:538 relies
+ * on).  Boxes (desc.cell = MHFEM_CELL_BOX): cell_verts is [C][2^dim], the
+ * vertices of TNL's Quadrangle / Hexahedron: axis-aligned, counterclockwise
+ * from the lowest corner, the bottom face before the top one (the order
+ * MassMatrix.h:171-186, 340-362 reads the side lengths from); another order
+ * is refused with MHFEM_ERR_INVALID_ARGUMENT.  The library numbers the faces
+ * in order of first appearance over the cells and their local faces. */
 mhfem_status mhfem_set_mesh(mhfem_t h, int64_t num_vertices, const double* coords,
                             int64_t num_cells, const int32_t* cell_verts);
 
