@@ -69,3 +69,23 @@ def test_mixed_cell_kinds_are_refused(tmp_path):
     _legacy_with_types(f, coords, cells, vtkio.VTK_QUAD)  # 3 vertices declared as quadrilaterals
     with pytest.raises(ValueError):
         vtkio.read_mesh(f)
+
+
+@pytest.mark.parametrize("kind", ["triangles", "tetrahedra"])
+def test_netgen_roundtrip(tmp_path, kind):
+    coords, cells = MESHES[kind]()
+    f = tmp_path / "m.ng"
+    vtkio.write_netgen(f, coords, cells)
+    c2, k2 = vtkio.read_mesh(f)
+    assert np.allclose(c2, coords, rtol=0, atol=1e-15) and np.array_equal(k2, cells)
+
+
+def test_netgen_reads_boundary_elements_and_rejects_bad_indices(tmp_path):
+    f = tmp_path / "t.ng"
+    # two triangles of the unit square, one boundary edge listed after the elements
+    f.write_text("4\n0 0\n1 0\n1 1\n0 1\n2\n1 1 2 3\n1 1 3 4\n1\n1 1 2\n")
+    c, k = vtkio.read_mesh(f)
+    assert c.shape == (4, 2) and np.array_equal(k, [[0, 1, 2], [0, 2, 3]])
+    f.write_text("3\n0 0\n1 0\n1 1\n1\n1 1 2 4\n")
+    with pytest.raises(ValueError):
+        vtkio.read_mesh(f)

@@ -100,8 +100,6 @@ def parse(path, overrides: dict | None = None) -> Config:
             values[key] = default
     if values["mesh-format"] not in MESH_FORMATS:
         raise ConfigError(f"mesh-format must be one of {sorted(MESH_FORMATS)}")
-    if values["mesh-format"] == "ng":
-        raise ConfigError("mesh-format 'ng' (Netgen) is not supported by this library; use vtk or vtu")
     solver = values["linear-solver"].lower()
     if solver not in LINEAR_SOLVERS:
         raise ConfigError(f"linear-solver {solver!r} is not a TNL solver name")

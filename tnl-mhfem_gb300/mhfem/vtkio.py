@@ -8,6 +8,8 @@
   axis-aligned pixel (8) and voxel (11) cells, whose vertices are reordered
   into the quadrilateral / hexahedron order (VTK numbers a pixel's corners
   in lexicographic order, a quadrilateral's counterclockwise).
+* Netgen's neutral format (``.ng``, triangles and tetrahedra), the third
+  mesh format of configSetup.h:16-21; ``write_netgen`` writes it.
 * ``read_cell_data(path, name)``: a cell array from a VTU file, e.g. the
   initial condition ``InitialCondition[Z0]`` (Solver.hpp:296-306).
 * ``write_vtu(path, coords, cells, cell_data, ...)``: the snapshot files
@@ -226,6 +228,46 @@ def _read_vtu(path: Path):
     return pts[:, :dim].copy(), cells.astype(np.int32)
 
 
+# ---- Netgen ---------------------------------------------------------------------
+
+
+def _read_netgen(path: Path):
+    """Netgen's neutral mesh format (the `ng` mesh-format of configSetup.h:16-21):
+    the number of points, one point per line (2 or 3 coordinates), the number
+    of elements, one element per line as a material index followed by its
+    1-based vertex indices (3 for triangles, 4 for tetrahedra), then
+    optionally the boundary elements, which carry no information the solver
+    needs (faces and their boundary flags follow from the cells)."""
+    tokens = path.read_text().split("\n")
+    lines = [ln.split() for ln in tokens if ln.strip()]
+    npts = int(lines[0][0])
+    pts = np.array([[float(v) for v in ln] for ln in lines[1:1 + npts]], dtype=np.float64)
+    if pts.ndim != 2 or pts.shape[1] not in (2, 3):
+        raise ValueError(f"{path}: points must have 2 or 3 coordinates")
+    ncell = int(lines[1 + npts][0])
+    rows = lines[2 + npts:2 + npts + ncell]
+    if len(rows) != ncell:
+        raise ValueError(f"{path}: expected {ncell} elements")
+    cells = np.array([[int(v) for v in ln[1:]] for ln in rows], dtype=np.int64) - 1
+    dim = pts.shape[1]
+    if cells.shape[1] != dim + 1:
+        raise ValueError(f"{path}: {dim}D Netgen meshes hold simplices with {dim + 1} vertices")
+    if cells.min(initial=0) < 0 or cells.max(initial=0) >= npts:
+        raise ValueError(f"{path}: vertex index out of range")
+    return pts, cells.astype(np.int32)
+
+
+def write_netgen(path, coords: np.ndarray, cells: np.ndarray) -> None:
+    """The same neutral format (material 1, no boundary elements)."""
+    coords = np.asarray(coords, np.float64)
+    with open(path, "w") as fh:
+        fh.write(f"{coords.shape[0]}\n")
+        np.savetxt(fh, coords, fmt="%.17g")
+        fh.write(f"{cells.shape[0]}\n")
+        np.savetxt(fh, np.hstack([np.ones((cells.shape[0], 1), np.int64), np.asarray(cells, np.int64) + 1]), fmt="%d")
+        fh.write("0\n")
+
+
 def read_mesh(path, fmt: str = "auto"):
     path = Path(path)
     fmt = path.suffix[1:].lower() if fmt == "auto" else fmt
@@ -233,7 +275,9 @@ def read_mesh(path, fmt: str = "auto"):
         return _read_legacy(path)
     if fmt == "vtu":
         return _read_vtu(path)
-    raise ValueError(f"unsupported mesh format {fmt!r} (vtk, vtu)")
+    if fmt == "ng":
+        return _read_netgen(path)
+    raise ValueError(f"unsupported mesh format {fmt!r} (vtk, vtu, ng)")
 
 
 def read_cell_data(path, name: str) -> np.ndarray:
