@@ -178,7 +178,7 @@ __device__ __forceinline__ void ell_apply(const EllRows<T, WW, RPT>& e, const T*
 //
 // Each phase is a grid-stride loop over rows plus, for the reductions, the
 // scalar update that the last CTA applies.  The five iteration kernels below
-// each run one phase; the persistent kernel runs all five with grid barriers.
+// each run one phase.
 
 // v = A p ; acc = (rh, v)
 template <typename T, int WW, int RPT>
