@@ -60,7 +60,7 @@ def parse_args():
                     help="online training steps of the learned form before its timed steps")
     ap.add_argument("--profile-run", action="store_true",
                     help="only the warm-up and timed steps (for an ncu launch list)")
-    ap.add_argument("--profile-form", choices=["fp64", "mixed", "learned", "box"], default="fp64",
+    ap.add_argument("--profile-form", choices=["fp64", "mixed", "learned", "box", "gmres"], default="fp64",
                     help="form used by --profile-run (learned: --learned-train training steps first)")
     return ap.parse_args()
 
@@ -388,10 +388,15 @@ def profile_other_form(args, dev):
         p = problems.diffusion3d(N=args.grid, form=L.FORM_MIXED)
     elif args.profile_form == "box":
         p = problems.diffusion3d_box(N=2 * args.grid)
+    elif args.profile_form == "gmres":
+        p = problems.diffusion3d(N=args.grid)
     else:
         p = problems.diffusion3d_source(N=args.grid, steps=1000, form=L.FORM_LEARNED)
     p.config.device = dev
     s = problems.make_solver(p, check_every=8)
+    if args.profile_form == "gmres":
+        s.setup(tol=p.tol, max_iter=100000, check_every=8, linear_solver="gmres", gmres_restart=30,
+                gmres_variant="cgs")
     t = 0.0
     if args.profile_form == "learned":
         s.learned_options(train_steps=args.learned_train, train_iters=4, learning_rate=3e-3)
