@@ -118,3 +118,28 @@ def test_driver_end_to_end(tmp_path, box):
         m.step(t, 5e-4, 1e-14)
         t += 5e-4
     assert rel_err(z_gpu, m.Z_iK) < 1e-9
+
+
+def test_example_refuses_host_exec_and_mpi_ranks(tmp_path):
+    from mhfem import example
+
+    (tmp_path / "config.ini").write_text(CONFIG)
+    assert example.main(["--config", str(tmp_path / "config.ini"), "--exec", "host"]) == 1
+    assert example.main(["--config", str(tmp_path / "config.ini"), "--mpi-ranks", "2"]) == 1
+
+
+@pytest.mark.gpu
+def test_example_workflow(tmp_path):
+    """The reference's examples/HeatEquation/run.py flow: init (IC + BC file at
+    the configured paths) and then the solver, from one config.ini."""
+    from mhfem import example
+
+    coords, cells = meshgen.square_triangles(6)
+    vtkio.write_vtu(tmp_path / "mesh.vtu", coords, cells, {})
+    cfg = CONFIG.replace("boundary-conditions-file = boundary.bcs", "boundary-conditions-file = out/boundary.bcs")
+    cfg = cfg.replace("initial-condition = initial.vtu", "initial-condition = out/initial.vtu")
+    (tmp_path / "config.ini").write_text(cfg)
+    assert example.main(["--config", str(tmp_path / "config.ini")]) == 0
+    out = tmp_path / "out"
+    assert (out / "initial.vtu").exists() and (out / "boundary.bcs").exists() and (out / "log.txt").exists()
+    assert sorted(f.name for f in out.glob("data_*.vtu")) == [f"data_{k:05d}.vtu" for k in range(4)]

@@ -176,8 +176,8 @@ def main(argv=None) -> int:
         print("this library runs on the GPU only (--exec cuda); it has no host implementation", file=sys.stderr)
         return 1
     if args.print_static_configuration:
-        print("Real: double, Index: int, cells: triangles or tetrahedra (from the mesh), matrix: ELL, "
-              "advection: explicit upwind, model: heat equation")
+        print("Real: double, Index: int, cells: triangles, tetrahedra, rectangles or cuboids (from the "
+              "mesh), matrix: ELL, advection: explicit upwind, model: heat equation")
         return 0
     try:
         cfg = config.parse(args.config, {"output-directory": args.output_directory})
