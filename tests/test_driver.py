@@ -1,4 +1,6 @@
 """config.ini driver, boundary-condition storage and the init step."""
+import struct
+
 import numpy as np
 import pytest
 
@@ -143,3 +145,35 @@ def test_example_workflow(tmp_path):
     out = tmp_path / "out"
     assert (out / "initial.vtu").exists() and (out / "boundary.bcs").exists() and (out / "log.txt").exists()
     assert sorted(f.name for f in out.glob("data_*.vtu")) == [f"data_{k:05d}.vtu" for k in range(4)]
+
+
+def _tnl_object(magic: bytes, typ: str) -> bytes:
+    t = typ.encode()
+    return magic + struct.pack("<i", len(t)) + t
+
+
+@pytest.mark.parametrize("real", ["double", "float"])
+def test_bc_storage_reads_the_tnl_file_layout(tmp_path, real):
+    """The layout BoundaryConditionsStorage::save writes with TNL's File:
+    object header, dofSize, then three arrays with their own headers."""
+    n = 7
+    rng = np.random.default_rng(2)
+    tags = rng.integers(0, 4, n).astype(np.uint8)
+    vals = rng.standard_normal(n)
+    dvals = rng.standard_normal(n)
+    fdt = "<f8" if real == "double" else "<f4"
+    m = b"TNLMN"
+    raw = _tnl_object(m, f"TNL::MHFEM::BoundaryConditionsStorage< {real} >") + struct.pack("<q", n)
+    raw += _tnl_object(m, "TNL::Containers::Array< std::uint8_t, [any_device], std::int64_t >")
+    raw += struct.pack("<q", n) + tags.tobytes()
+    for arr in (vals, dvals):
+        raw += _tnl_object(m, f"TNL::Containers::Array< {real}, [any_device], std::int64_t >")
+        raw += struct.pack("<q", n) + arr.astype(fdt).tobytes()
+    (tmp_path / "b.tnl").write_bytes(raw)
+    b = bcstorage.BoundaryConditionsStorage.load(tmp_path / "b.tnl")
+    assert b.dofSize == n and np.array_equal(b.tags, tags)
+    assert np.array_equal(b.values, vals.astype(fdt).astype(np.float64))
+    assert np.array_equal(b.dirichletValues, dvals.astype(fdt).astype(np.float64))
+    (tmp_path / "short.tnl").write_bytes(raw[:-3])
+    with pytest.raises(ValueError):
+        bcstorage.BoundaryConditionsStorage.load(tmp_path / "short.tnl")

@@ -10,7 +10,9 @@ line ``MHFEM-BCS 1\\n``, the serialization type
 ``TNL::MHFEM::BoundaryConditionsStorage< double >`` as a little-endian int32
 length plus bytes, dofSize as int64, then tags (uint8), values and
 dirichletValues (float64), each preceded by its int64 element count.  All
-arrays are indexed i*F + E.
+arrays are indexed i*F + E.  ``load`` also reads files in the layout the
+reference writes through TNL's File (``load_tnl``), e.g. the ``boundary.tnl``
+of its examples/HeatEquation/init.py, checked structurally.
 """
 from __future__ import annotations
 
@@ -53,9 +55,11 @@ class BoundaryConditionsStorage:
 
     @classmethod
     def load(cls, path) -> "BoundaryConditionsStorage":
+        """This library's format, or the layout the reference's save() writes
+        through TNL's File (detected by its first bytes)."""
         data = Path(path).read_bytes()
         if not data.startswith(MAGIC):
-            raise ValueError(f"{path}: not a boundary-conditions file of this library")
+            return cls.load_tnl(path, data)
         pos = len(MAGIC)
         (ln,) = struct.unpack_from("<i", data, pos)
         pos += 4
@@ -73,6 +77,63 @@ class BoundaryConditionsStorage:
                 raise ValueError(f"Invalid dofSize in BoundaryConditionsStorage: dofSize = {n}, {name} has {m}")
             setattr(obj, name, np.frombuffer(data, dtype=dt, count=m, offset=pos).copy())
             pos += m * size
+        if obj.tags.size and int(obj.tags.max()) > 3:
+            raise ValueError("unknown boundary condition tag in file")
+        return obj
+
+    @classmethod
+    def load_tnl(cls, path, data: bytes | None = None) -> "BoundaryConditionsStorage":
+        """The object as BoundaryConditionsStorage::save writes it with TNL's
+        File (BoundaryConditionsStorage.h:23-34): saveObjectType (a magic
+        number, then the type string as an int32 length and its bytes),
+        dofSize as int64, then tags, values and dirichletValues, each an
+        Array saved the same way: its object type, its int64 size and the
+        raw elements (std::uint8_t tags, BoundaryConditionsType.h:7-9; Real
+        values, the Real named in the object type).  The magic number is taken
+        from the file's first bytes and the array type strings are not
+        compared text for text: TNL's source is not available to pin them.
+        The checks are structural: sizes equal to dofSize, the stream fully
+        consumed, known tags."""
+        data = Path(path).read_bytes() if data is None else data
+        pos = 0
+
+        def object_type(where: str) -> str:
+            nonlocal pos
+            if data[pos:pos + len(magic)] != magic:
+                raise ValueError(f"{path}: no object header at {where}")
+            pos += len(magic)
+            (ln,) = struct.unpack_from("<i", data, pos)
+            pos += 4
+            if not 0 < ln < 4096 or pos + ln > len(data):
+                raise ValueError(f"{path}: bad object type length at {where}")
+            typ = data[pos:pos + ln].decode("ascii", "replace")
+            pos += ln
+            return typ
+
+        head = data.find(b"TNL::MHFEM::BoundaryConditionsStorage")
+        if head < 9:
+            raise ValueError(f"{path}: neither this library's nor TNL's boundary-conditions format")
+        magic = data[:head - 4]
+        typ = object_type("the start")
+        real = typ[typ.index("<") + 1:typ.rindex(">")].strip() if "<" in typ else "double"
+        rsize = {"double": 8, "float": 4}.get(real)
+        if rsize is None:
+            raise ValueError(f"{path}: unsupported Real type {real!r}")
+        (n,) = struct.unpack_from("<q", data, pos)
+        pos += 8
+        obj = cls(n)
+        for name, dt, size in (("tags", "<u1", 1), ("values", f"<f{rsize}", rsize),
+                               ("dirichletValues", f"<f{rsize}", rsize)):
+            object_type(name)
+            (m,) = struct.unpack_from("<q", data, pos)
+            pos += 8
+            if m != n or pos + m * size > len(data):
+                raise ValueError(f"Invalid dofSize in BoundaryConditionsStorage: dofSize = {n}, {name} has {m}")
+            arr = np.frombuffer(data, dtype=dt, count=m, offset=pos)
+            setattr(obj, name, arr.astype(np.uint8 if size == 1 else np.float64))
+            pos += m * size
+        if pos != len(data):
+            raise ValueError(f"{path}: {len(data) - pos} trailing bytes")
         if obj.tags.size and int(obj.tags.max()) > 3:
             raise ValueError("unknown boundary condition tag in file")
         return obj
