@@ -56,6 +56,9 @@ def parse_args():
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-box", action="store_true", help="skip the cuboid (box cell) leg")
     ap.add_argument("--no-gmres", action="store_true", help="skip the GMRES leg")
+    ap.add_argument("--mixed-error-steps", type=int, default=0,
+                    help="after timing: run the mixed and FP64 forms in lockstep for K steps from the same state "
+                         "and report each step's relative error of the mixed face traces")
     ap.add_argument("--learned-train", type=int, default=200,
                     help="online training steps of the learned form before its timed steps")
     ap.add_argument("--profile-run", action="store_true",
@@ -269,6 +272,43 @@ def gmres_leg(args, dev, world):
     s.close()
     return {"solver": "GMRES(30), classical Gram-Schmidt", "value": world * args.steps / (el / 1e3), "unit": UNIT,
             "ms_per_step": el / args.steps, "iterations_per_step": (it1 - it0) / args.steps}
+
+
+def mixed_lockstep_errors(args, dev, zk, zf, t):
+    """Per-step relative errors of the face traces, outside the timed region:
+    the mixed form and the FP64 form at the workload's tolerance and the FP64
+    form solved to 1e-13 (the exact discrete solution up to rounding), all
+    advanced in lockstep from the same state; each step's traces of the first
+    two against the third, and the mixed form against the FP64 form."""
+    import numpy as np
+
+    from mhfem import _lib as L
+    from mhfem import problems
+
+    sols = {}
+    for name, form in (("mixed", L.FORM_MIXED), ("fp64", L.FORM_FP64), ("exact", L.FORM_FP64)):
+        q = problems.diffusion3d(N=args.grid, form=form)
+        q.config.device = dev
+        if name == "exact":
+            q.tol = 1e-13
+        sol = problems.make_solver(q, check_every=8)
+        sol.setInitialCondition(zk, zf)
+        sols[name] = sol
+    rel = lambda a, b: float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+    out = {"mixed_vs_fp64_1e-13": [], "fp64_vs_fp64_1e-13": [], "mixed_vs_fp64": []}
+    for _ in range(args.mixed_error_steps):
+        for sol in sols.values():
+            sol.step(t, q.dt)
+        a, _ = sols["mixed"].state()
+        b, _ = sols["fp64"].state()
+        c, _ = sols["exact"].state()
+        out["mixed_vs_fp64_1e-13"].append(rel(a, c))
+        out["fp64_vs_fp64_1e-13"].append(rel(b, c))
+        out["mixed_vs_fp64"].append(rel(a, b))
+        t += q.dt
+    for sol in sols.values():
+        sol.close()
+    return out
 
 
 def learned_leg(args, dev, world):
@@ -579,6 +619,8 @@ def main():
                               "mixed": [rel(outs["mixed"][0], zr), rel(outs["mixed"][1], kr)],
                               "fp64_at_same_tol": [rel(outs["fp64"][0], zr), rel(outs["fp64"][1], kr)]},
                           "spmv_fp32_gbs": sp32["bytes"] / (sp32["ms"] * 1e-3) / 1e9}
+        if args.mixed_error_steps > 0:
+            forms["mixed"]["per_step_rel_err_vs_fp64"] = mixed_lockstep_errors(args, dev, zkm, zfm, tm)
         sm.close()
 
     if not args.no_learned:
