@@ -241,7 +241,9 @@ void build_pattern(const HostTopology& T, int n, const uint8_t* tags, HostPatter
                 const int32_t g = T.cell_faces[(int64_t)K1 * nf + f];
                 if (g != (int32_t)E) list[L++] = g;
             }
-        std::sort(list, list + L);
+        // at most 2 nf - 1 = 11 faces: insertion sort
+        for (int x = 1; x < L; ++x)
+            for (int y = x; y > 0 && list[y - 1] > list[y]; --y) std::swap(list[y - 1], list[y]);
         auto pos_of = [&](int32_t g) {
             for (int q = 0; q < L; ++q)
                 if (list[q] == g) return q;
