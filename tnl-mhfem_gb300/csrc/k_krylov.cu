@@ -59,6 +59,7 @@ __global__ void __launch_bounds__(KB) k_init(const int32_t* cols, const T* vals,
         if (bn == 0) bn = 1;
         sc->bnorm = bn;
         sc->rho = s[0];
+        sc->rr = s[0];
         sc->rhnorm = sqrt(s[0]);
         sc->restart = 0;
         sc->half = 0;
@@ -284,10 +285,11 @@ __device__ __forceinline__ void phase_update_s(int64_t rows, const T* r, const T
     for (int64_t q = nv * V + gtid; q < rows; q += gstride) s[q] = fma(-alpha, v[q], r[q]);
 }
 
-// t = A s ; acc = (t, s), (t, t), (s, s)
-template <typename T, int WW, int RPT>
+// t = A s ; acc = (t, s), (t, t) and, on a check iteration, (s, s)
+template <typename T, int WW, int RPT, bool CHECK>
 __device__ __forceinline__ void phase_spmv_dots2(const int32_t* cols, const T* vals, int W, int64_t rows,
-                                                 const T* s, T* t, int64_t gtid, int64_t gstride, T (&acc)[3])
+                                                 const T* s, T* t, int64_t gtid, int64_t gstride,
+                                                 T (&acc)[CHECK ? 3 : 2])
 {
     if constexpr (spmv_pipelined<T>(WW, RPT)) {
         const int64_t ng = rows / RPT;
@@ -307,7 +309,7 @@ __device__ __forceinline__ void phase_spmv_dots2(const int32_t* cols, const T* v
                 yv.v[j] = y[j];
                 acc[0] = fma(y[j], sv.v[j], acc[0]);
                 acc[1] = fma(y[j], y[j], acc[1]);
-                acc[2] = fma(sv.v[j], sv.v[j], acc[2]);
+                if constexpr (CHECK) acc[2] = fma(sv.v[j], sv.v[j], acc[2]);
             }
             stv<T, RPT>(t, q, yv);
             cur = nxt;
@@ -323,18 +325,23 @@ __device__ __forceinline__ void phase_spmv_dots2(const int32_t* cols, const T* v
                 yv.v[j] = y[j];
                 acc[0] = fma(y[j], sv[j], acc[0]);
                 acc[1] = fma(y[j], y[j], acc[1]);
-                acc[2] = fma(sv[j], sv[j], acc[2]);
+                if constexpr (CHECK) acc[2] = fma(sv[j], sv[j], acc[2]);
             }
             stv<T, RPT>(t, q, yv);
         }
 }
 
-// ||s||, the half-step test, omega = (t, s) / (t, t)
-__device__ __forceinline__ void scalars_omega(KrylovScalars* sc, const double (&sum)[3])
+// check iteration: ||s|| and the half-step test; omega = (t, s) / (t, t)
+template <bool CHECK>
+__device__ __forceinline__ void scalars_omega(KrylovScalars* sc, const double (&sum)[CHECK ? 3 : 2])
 {
-    sc->snorm = sqrt(sum[2]) / sc->bnorm;
-    sc->half = (sc->snorm < sc->tol) ? 1 : 0;
-    if (sc->half) return;
+    if constexpr (CHECK) {
+        sc->snorm = sqrt(sum[2]) / sc->bnorm;
+        sc->half = (sc->snorm < sc->tol) ? 1 : 0;
+        if (sc->half) return;
+    }
+    else
+        sc->half = 0;
     sc->ts = sum[0];
     sc->tt = sum[1];
     if (!finite(sum[0]) || !finite(sum[1])) { sc->status = KS_NOTFINITE; sc->done = 1; }
@@ -365,11 +372,11 @@ __device__ __forceinline__ void scalars_half(KrylovScalars* sc)
     sc->done = 1;
 }
 
-// x += alpha p + omega s ; r = s - omega t ; acc = (rh, r), (r, r)
-template <typename T, int V>
+// x += alpha p + omega s ; r = s - omega t ; acc = (rh, r) and, on a check iteration, (r, r)
+template <typename T, int V, bool CHECK>
 __device__ __forceinline__ void phase_update_xr(int64_t rows, T* x, const T* p, const T* s, const T* t, T* r,
                                                 const T* rh, T alpha, T omega, int64_t gtid, int64_t gstride,
-                                                T (&acc)[2])
+                                                T (&acc)[CHECK ? 2 : 1])
 {
     const int64_t nv = rows / V;
     auto apply = [&](int64_t q, VecT<T, V> xx, const VecT<T, V>& pp, const VecT<T, V>& ss, const VecT<T, V>& tt,
@@ -380,7 +387,7 @@ __device__ __forceinline__ void phase_update_xr(int64_t rows, T* x, const T* p, 
             xx.v[j] = fma(omega, ss.v[j], fma(alpha, pp.v[j], xx.v[j]));
             rr.v[j] = fma(-omega, tt.v[j], ss.v[j]);
             acc[0] = fma(hh.v[j], rr.v[j], acc[0]);
-            acc[1] = fma(rr.v[j], rr.v[j], acc[1]);
+            if constexpr (CHECK) acc[1] = fma(rr.v[j], rr.v[j], acc[1]);
         }
         stv<T, V>(x, q, xx);
         stv<T, V>(r, q, rr);
@@ -399,26 +406,36 @@ __device__ __forceinline__ void phase_update_xr(int64_t rows, T* x, const T* p, 
         const T rv = fma(-omega, t[q], sv);
         r[q] = rv;
         acc[0] = fma(rh[q], rv, acc[0]);
-        acc[1] = fma(rv, rv, acc[1]);
+        if constexpr (CHECK) acc[1] = fma(rv, rv, acc[1]);
     }
 }
 
 // iteration count, convergence, restart test, beta
-__device__ __forceinline__ void scalars_beta(KrylovScalars* sc, const double (&sum)[2])
+// The residual norm (the convergence test) is formed on check iterations
+// only, the last of each group the host replays between its checks: the
+// other iterations skip the (r, r) and (s, s) products, two of the about 24
+// FP64 operations per row of an iteration.  Convergence is then detected at
+// the end of such a group, up to check_every - 1 iterations later.  The
+// restart test compares (rh, r) with the last known ||r||; on a restart,
+// update_p forms (r, r) for the new rho.
+template <bool CHECK>
+__device__ __forceinline__ void scalars_beta(KrylovScalars* sc, const double (&sum)[CHECK ? 2 : 1])
 {
     sc->it += 1;
-    sc->rr = sum[1];
-    sc->res = sqrt(sum[1]) / sc->bnorm;
-    if (!finite(sc->res)) { sc->status = KS_NOTFINITE; sc->done = 1; }
-    else if (sc->res < sc->tol) { sc->status = KS_CONVERGED; sc->done = 1; }
-    else if (sc->it >= sc->max_iter) { sc->status = KS_MAXITER; sc->done = 1; }
+    if constexpr (CHECK) {
+        sc->rr = sum[1];
+        sc->res = sqrt(sum[1]) / sc->bnorm;
+        if (!finite(sc->res)) { sc->status = KS_NOTFINITE; sc->done = 1; return; }
+        if (sc->res < sc->tol) { sc->status = KS_CONVERGED; sc->done = 1; return; }
+    }
+    else if (!finite(sum[0])) { sc->status = KS_NOTFINITE; sc->done = 1; return; }
+    if (sc->it >= sc->max_iter) { sc->status = KS_MAXITER; sc->done = 1; }
     else if (sc->omega == 0 || sc->rho == 0) { sc->status = KS_BREAKDOWN; sc->done = 1; }
-    else if (fabs(sum[0]) <= kRestartEps * sqrt(sum[1]) * sc->rhnorm) {
+    else if (fabs(sum[0]) <= kRestartEps * sqrt(sc->rr) * sc->rhnorm) {
         // shadow residual (numerically) orthogonal to r: restart with rh = p = r
+        // (rho = (r, r) and ||rh|| come from update_p's restart pass)
         sc->restart = 1;
         sc->beta = 0;
-        sc->rho = sum[1];
-        sc->rhnorm = sqrt(sum[1]);
     }
     else {
         sc->restart = 0;
@@ -427,10 +444,10 @@ __device__ __forceinline__ void scalars_beta(KrylovScalars* sc, const double (&s
     }
 }
 
-// p = r + beta (p - omega v); on a restart rh = p = r
+// p = r + beta (p - omega v); on a restart rh = p = r and acc = (r, r)
 template <typename T, int V>
 __device__ __forceinline__ void phase_update_p(int64_t rows, T* p, const T* r, const T* v, T* rh, T beta, T omega,
-                                               bool restart, int64_t gtid, int64_t gstride)
+                                               bool restart, int64_t gtid, int64_t gstride, T (&acc)[1])
 {
     const int64_t nv = rows / V;
     if (restart) {
@@ -438,11 +455,14 @@ __device__ __forceinline__ void phase_update_p(int64_t rows, T* p, const T* r, c
             const VecT<T, V> rr = ldv<T, V>(r, q);
             stv<T, V>(p, q, rr);
             stv<T, V>(rh, q, rr);
+#pragma unroll
+            for (int j = 0; j < V; ++j) acc[0] = fma(rr.v[j], rr.v[j], acc[0]);
         }
         for (int64_t q = nv * V + gtid; q < rows; q += gstride) {
             const T rv = r[q];
             p[q] = rv;
             rh[q] = rv;
+            acc[0] = fma(rv, rv, acc[0]);
         }
         return;
     }
@@ -496,27 +516,29 @@ __global__ void __launch_bounds__(KB) k_update_s(int64_t rows, const T* r, const
     phase_update_s<T, V>(rows, r, v, s, (T)sc->alpha, gtid, gstride);
 }
 
-// The half-step decision (||s|| < tol) is taken here, after the SpMV: the
-// same decision as testing ||s|| before it; t is then unused.
-template <typename T, int WW, int RPT>
+// On a check iteration the half-step decision (||s|| < tol) is taken here,
+// after the SpMV: the same decision as testing ||s|| before it; t is then
+// unused.
+template <typename T, int WW, int RPT, bool CHECK>
 __global__ void __launch_bounds__(KB) k_spmv_dots2(const int32_t* cols, const T* vals, int W, int64_t rows,
                                                    const T* s, T* t,
                                                    KrylovScalars* sc, double* partials, uint32_t* counter)
 {
+    constexpr int NS = CHECK ? 3 : 2;
     pdl_wait();
     pdl_release();
     if (*(volatile int32_t*)&sc->done) return;
     MHFEM_GRID_STRIDE;
-    T acc[3] = {0, 0, 0};
-    phase_spmv_dots2<T, WW, RPT>(cols, vals, W, rows, s, t, gtid, gstride, acc);
-    block_reduce_store<T, 3>(acc, partials);
+    T acc[NS] = {};
+    phase_spmv_dots2<T, WW, RPT, CHECK>(cols, vals, W, rows, s, t, gtid, gstride, acc);
+    block_reduce_store<T, NS>(acc, partials);
     if (!ticket_last(counter)) return;
-    double sum[3];
-    final_sums<3>(partials, sum);
-    if (threadIdx.x == 0) scalars_omega(sc, sum);
+    double sum[NS];
+    final_sums<NS>(partials, sum);
+    if (threadIdx.x == 0) scalars_omega<CHECK>(sc, sum);
 }
 
-template <typename T, int V>
+template <typename T, int V, bool CHECK>
 __global__ void __launch_bounds__(KB) k_update_xr(int64_t rows, T* x, const T* p, const T* s, const T* t,
                                                   T* r, const T* rh,
                                                   KrylovScalars* sc, double* partials, uint32_t* counter)
@@ -532,24 +554,38 @@ __global__ void __launch_bounds__(KB) k_update_xr(int64_t rows, T* x, const T* p
         if (threadIdx.x == 0) scalars_half(sc);
         return;
     }
-    T acc[2] = {0, 0};
-    phase_update_xr<T, V>(rows, x, p, s, t, r, rh, alpha, (T)sc->omega, gtid, gstride, acc);
-    block_reduce_store<T, 2>(acc, partials);
+    constexpr int NS = CHECK ? 2 : 1;
+    T acc[NS] = {};
+    phase_update_xr<T, V, CHECK>(rows, x, p, s, t, r, rh, alpha, (T)sc->omega, gtid, gstride, acc);
+    block_reduce_store<T, NS>(acc, partials);
     if (!ticket_last(counter)) return;
-    double sum[2];
-    final_sums<2>(partials, sum);
-    if (threadIdx.x == 0) scalars_beta(sc, sum);
+    double sum[NS];
+    final_sums<NS>(partials, sum);
+    if (threadIdx.x == 0) scalars_beta<CHECK>(sc, sum);
 }
 
 template <typename T, int V>
 __global__ void __launch_bounds__(KB) k_update_p(int64_t rows, T* p, const T* r, const T* v, T* rh,
-                                                 const KrylovScalars* sc)
+                                                 KrylovScalars* sc, double* partials, uint32_t* counter)
 {
     pdl_wait();
     pdl_release();
     if (*(volatile const int32_t*)&sc->done) return;
     MHFEM_GRID_STRIDE;
-    phase_update_p<T, V>(rows, p, r, v, rh, (T)sc->beta, (T)sc->omega, sc->restart != 0, gtid, gstride);
+    const bool restart = sc->restart != 0;  // the same in every block
+    T acc[1] = {0};
+    phase_update_p<T, V>(rows, p, r, v, rh, (T)sc->beta, (T)sc->omega, restart, gtid, gstride, acc);
+    if (!restart) return;
+    // the new shadow residual rh = r: rho = (rh, r) = (r, r)
+    block_reduce_store<T, 1>(acc, partials);
+    if (!ticket_last(counter)) return;
+    double sum[1];
+    final_sums<1>(partials, sum);
+    if (threadIdx.x == 0) {
+        sc->rho = sum[0];
+        sc->rr = sum[0];
+        sc->rhnorm = sqrt(sum[0]);
+    }
 }
 
 // ---- launch shapes ---------------------------------------------------------------
@@ -587,14 +623,23 @@ static void iterate(const EllMatrix& A, const T* vals, T* x, T* r, T* rh, T* p, 
 {
     const int32_t* cols = A.cols;
     for (int it = 0; it < iters; ++it) {
+        const bool check = (it == iters - 1);  // the last iteration before the host's check
         MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dot<T, WW, spmv_rpt(WW, RPT)>, st, cols, vals, A.width,
                                                  A.rows, (const T*)p, (const T*)rh, v, sc, W.partials, W.counters));
         launch_pdl(k_update_s<T, V>, st, A.rows, (const T*)r, (const T*)v, s, (const KrylovScalars*)sc);
-        MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dots2<T, WW, spmv_rpt(WW, RPT)>, st, cols, vals, A.width,
-                                                 A.rows, (const T*)s, t, sc, W.partials, W.counters));
-        launch_pdl(k_update_xr<T, V>, st, A.rows, x, (const T*)p, (const T*)s, (const T*)t, r, (const T*)rh, sc,
-                   W.partials, W.counters);
-        launch_pdl(k_update_p<T, V>, st, A.rows, p, (const T*)r, (const T*)v, rh, (const KrylovScalars*)sc);
+        if (check) {
+            MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dots2<T, WW, spmv_rpt(WW, RPT), true>, st, cols, vals,
+                                                     A.width, A.rows, (const T*)s, t, sc, W.partials, W.counters));
+            launch_pdl(k_update_xr<T, V, true>, st, A.rows, x, (const T*)p, (const T*)s, (const T*)t, r,
+                       (const T*)rh, sc, W.partials, W.counters);
+        }
+        else {
+            MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dots2<T, WW, spmv_rpt(WW, RPT), false>, st, cols, vals,
+                                                     A.width, A.rows, (const T*)s, t, sc, W.partials, W.counters));
+            launch_pdl(k_update_xr<T, V, false>, st, A.rows, x, (const T*)p, (const T*)s, (const T*)t, r,
+                       (const T*)rh, sc, W.partials, W.counters);
+        }
+        launch_pdl(k_update_p<T, V>, st, A.rows, p, (const T*)r, (const T*)v, rh, sc, W.partials, W.counters);
     }
 }
 
@@ -796,6 +841,7 @@ __global__ void __launch_bounds__(KB) k_inner_init(int64_t rows, const double* r
         sc->max_iter = max_iter;
         sc->bnorm = sqrt(s[0]) > 0 ? sqrt(s[0]) : 1.0;
         sc->rho = s[0];
+        sc->rr = s[0];
         sc->rhnorm = sqrt(s[0]);
         sc->restart = 0;
         sc->half = 0;
