@@ -208,7 +208,11 @@ mhfem_status mhfem_set_hook(mhfem_t h, int32_t point, mhfem_hook fn, void* user)
  * advection terms on for every later step (exact zeros leave the results
  * unchanged). */
 mhfem_status mhfem_coeff_device(mhfem_t h, int32_t which, double** data, int64_t* count);
-/* The device array of a scheme or state array (MHFEM_ARRAY_*). */
+/* The device array of a scheme or state array (MHFEM_ARRAY_*).
+ * Pointers from these two calls stay valid until the next mhfem_set_mesh,
+ * mhfem_set_coeff of the same coefficient with another count, or
+ * mhfem_destroy; MHFEM_ARRAY_RHS also moves when the linear system is set
+ * up again (mhfem_setup_linear_system, or new boundary tags). */
 mhfem_status mhfem_array_device(mhfem_t h, int32_t which, double** data, int64_t* count);
 
 /* Time-modulated source (a model hook of updateNonLinearTerms,

@@ -261,7 +261,10 @@ mhfem_status mhfem_set_mesh(mhfem_t h, int64_t V, const double* coords, int64_t 
     if (!msg.empty()) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "%s", msg.c_str());
     const int nf = h->nf, nv = h->nv, n = h->n;
     const int64_t F = h->topo.F;
-    // release everything that depends on the mesh
+    // release everything that depends on the mesh; the handle has no mesh
+    // until the new one is complete (a failed allocation leaves it unusable,
+    // not pointing at freed arrays)
+    h->has_mesh = false;
     invalidate_graphs(h);
     learned_release(h);
     for (void* p : h->allocs) cudaFree(p);
@@ -332,13 +335,13 @@ mhfem_status mhfem_set_mesh(mhfem_t h, int64_t V, const double* coords, int64_t 
     const int ones[] = {MHFEM_COEF_N, MHFEM_COEF_M, MHFEM_COEF_D, MHFEM_COEF_M_UPW, MHFEM_COEF_M_BND};
     const int zeros[] = {MHFEM_COEF_U, MHFEM_COEF_W, MHFEM_COEF_A, MHFEM_COEF_R, MHFEM_COEF_F};
     for (int w : ones)
-        if ((st = set_coef_device(h, w, &one, 1)) != MHFEM_OK) return st;
+        if ((st = set_coef_device(h, w, &one, 1)) != MHFEM_OK) { h->has_mesh = false; return st; }
     for (int w : zeros)
-        if ((st = set_coef_device(h, w, &zero, 1)) != MHFEM_OK) return st;
+        if ((st = set_coef_device(h, w, &zero, 1)) != MHFEM_OK) { h->has_mesh = false; return st; }
     // default boundary conditions: zero Dirichlet everywhere (Solver.hpp:282-293)
     std::vector<uint8_t> t0((size_t)n * F, MHFEM_BC_FIXED_VALUE);
     std::vector<double> v0((size_t)n * F, 0.0);
-    if ((st = mhfem_set_bc(h, t0.data(), v0.data(), v0.data())) != MHFEM_OK) return st;
+    if ((st = mhfem_set_bc(h, t0.data(), v0.data(), v0.data())) != MHFEM_OK) { h->has_mesh = false; return st; }
     h->has_bc = false;  // defaults only
     return MHFEM_OK;
 }
