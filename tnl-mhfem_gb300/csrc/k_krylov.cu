@@ -86,8 +86,8 @@ __device__ __forceinline__ void spmv_rows(const int32_t* __restrict__ cols, cons
         VecT<T, RPT> a[WW];
 #pragma unroll
         for (int k = 0; k < WW; ++k) {
-            c[k] = ldv<int32_t, RPT>(cols + (int64_t)k * rows, q);
-            a[k] = ldv<T, RPT>(vals + (int64_t)k * rows, q);
+            c[k] = ldv_stream<int32_t, RPT>(cols + (int64_t)k * rows, q);
+            a[k] = ldv_stream<T, RPT>(vals + (int64_t)k * rows, q);
         }
         T xg[WW][RPT];
 #pragma unroll
@@ -110,7 +110,7 @@ __device__ __forceinline__ void spmv_rows(const int32_t* __restrict__ cols, cons
         T acc = xs;
         for (int k = 0; k < W; ++k) {
             const int64_t o = (int64_t)k * rows + q;
-            acc = fma(__ldg(vals + o), x[__ldg(cols + o)], acc);
+            acc = fma(__ldcs(vals + o), x[__ldcs(cols + o)], acc);
         }
         y[0] = acc;
         self[0] = xs;
@@ -147,8 +147,8 @@ __device__ __forceinline__ void ell_load(const int32_t* __restrict__ cols, const
 {
 #pragma unroll
     for (int k = 0; k < WW; ++k) {
-        e.c[k] = ldv<int32_t, RPT>(cols + (int64_t)k * rows, q);
-        e.a[k] = ldv<T, RPT>(vals + (int64_t)k * rows, q);
+        e.c[k] = ldv_stream<int32_t, RPT>(cols + (int64_t)k * rows, q);
+        e.a[k] = ldv_stream<T, RPT>(vals + (int64_t)k * rows, q);
     }
 }
 
@@ -693,8 +693,8 @@ __global__ void __launch_bounds__(KB) k_learned_prep(const int32_t* __restrict__
             double v[WW];
 #pragma unroll
             for (int k = 0; k < WW; ++k) {
-                c[k] = __ldg(cols + (int64_t)k * rows + q);
-                v[k] = __ldg(vals + (int64_t)k * rows + q);
+                c[k] = __ldcs(cols + (int64_t)k * rows + q);
+                v[k] = __ldcs(vals + (int64_t)k * rows + q);
             }
 #pragma unroll
             for (int k = 0; k < WW; ++k) {
@@ -705,8 +705,8 @@ __global__ void __launch_bounds__(KB) k_learned_prep(const int32_t* __restrict__
         else {
             for (int k = 0; k < W; ++k) {
                 const int64_t o = (int64_t)k * rows + q;
-                const double v = __ldg(vals + o);
-                const int32_t c = __ldg(cols + o);
+                const double v = __ldcs(vals + o);
+                const int32_t c = __ldcs(cols + o);
                 yz = fma(v, Zn[c], yz);
                 y1 = fma(v, Zn1[c], y1);
             }
