@@ -220,10 +220,16 @@ mhfem_status mhfem_create(const mhfem_desc* desc, mhfem_t* out)
         delete h;
         return MHFEM_ERR_CUDA;
     }
-    for (auto& e : h->ev) cudaEventCreate(&e);
-    cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, desc->device);
-    cudaMallocHost((void**)&h->W.host_sc, sizeof(KrylovScalars) * 2);
-    cudaMallocHost((void**)&h->host_err, sizeof(int32_t));
+    bool ok = true;
+    for (auto& e : h->ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+    ok = ok && cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, desc->device) == cudaSuccess;
+    ok = ok && cudaMallocHost((void**)&h->W.host_sc, sizeof(KrylovScalars) * 2) == cudaSuccess;
+    ok = ok && cudaMallocHost((void**)&h->host_err, sizeof(int32_t)) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        mhfem_destroy(h);  // releases whatever was created
+        return MHFEM_ERR_CUDA;
+    }
     *out = h;
     return MHFEM_OK;
 }
