@@ -102,3 +102,32 @@ def test_diffusion3d_workload_sizes():
     assert int(bnd.sum()) == 49152
     assert int((tags[bnd] == problems.BC_FIXED_VALUE).sum()) == 16384
     assert int((tags[bnd] == problems.BC_FIXED_FLUX).sum()) == 32768
+
+
+def test_solver_checks_array_sizes_before_the_library_call():
+    """The Python mirror refuses arrays of the wrong size itself: the C ABI
+    takes plain pointers and would read past a short buffer."""
+    from mhfem.solver import Solver, StaticConfig
+
+    class NoLibrary:
+        def __getattr__(self, name):
+            raise AssertionError(f"the library was called: {name}")
+
+    s = object.__new__(Solver)  # no handle: every check must fire before a library call
+    s.config = StaticConfig(dim=3, n_eq=2)
+    s.lib = NoLibrary()
+    s.V, s.C, s.F = 8, 10, 25
+    with pytest.raises(ValueError, match="Z_iK"):
+        s.setInitialCondition(np.zeros(10))
+    with pytest.raises(ValueError, match="Z_iF"):
+        s.setInitialCondition(np.zeros(20), np.zeros(25))
+    with pytest.raises(ValueError, match="boundary"):
+        s.set_bc(np.zeros(25, np.uint8), np.zeros(50), np.zeros(50))
+    with pytest.raises(ValueError, match="coords"):
+        s.setMesh(np.zeros((8, 2)), np.zeros((10, 4), np.int32))
+    with pytest.raises(ValueError, match="cells"):
+        s.setMesh(np.zeros((8, 3)), np.zeros((10, 3), np.int32))
+    with pytest.raises(ValueError, match="features"):
+        s.learned_forward(np.zeros((25, 3), np.float32))
+    with pytest.raises(ValueError, match="target"):
+        s.learned_gradients(np.zeros((25, L.LEARNED_FEATURES), np.float32), np.zeros(24))

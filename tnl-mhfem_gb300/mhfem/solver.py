@@ -116,8 +116,10 @@ class Solver:
     def setMesh(self, coords: np.ndarray, cells: np.ndarray) -> None:
         coords = np.ascontiguousarray(coords, dtype=np.float64)
         cells = np.ascontiguousarray(cells, dtype=np.int32)
-        assert coords.ndim == 2 and coords.shape[1] == self.config.dim
-        assert cells.ndim == 2 and cells.shape[1] == self.config.verts_per_cell
+        if coords.ndim != 2 or coords.shape[1] != self.config.dim:
+            raise ValueError(f"coords must have shape (V, {self.config.dim}), got {coords.shape}")
+        if cells.ndim != 2 or cells.shape[1] != self.config.verts_per_cell:
+            raise ValueError(f"cells must have shape (C, {self.config.verts_per_cell}), got {cells.shape}")
         self._ck(self.lib.mhfem_set_mesh(self._h, coords.shape[0], _dptr(coords), cells.shape[0], _i32ptr(cells)))
         V = ct.c_int64(); C = ct.c_int64(); F = ct.c_int64()
         self._ck(self.lib.mhfem_get_sizes(self._h, ct.byref(V), ct.byref(C), ct.byref(F), None, None))
@@ -160,11 +162,16 @@ class Solver:
         self._ck(self.lib.mhfem_set_solver(self._h, ct.byref(o)))
 
     def setInitialCondition(self, Z_iK: np.ndarray, Z_iF: np.ndarray | None = None) -> None:
+        n = self.config.n_eq
         Z_iK = np.ascontiguousarray(Z_iK, dtype=np.float64).ravel()
+        if Z_iK.size != n * self.C:
+            raise ValueError(f"Z_iK must hold n*C = {n * self.C} values, got {Z_iK.size}")
         if Z_iF is None:
             self._ck(self.lib.mhfem_set_initial_condition(self._h, _dptr(Z_iK)))
         else:
             Z_iF = np.ascontiguousarray(Z_iF, dtype=np.float64).ravel()
+            if Z_iF.size != n * self.F:
+                raise ValueError(f"Z_iF must hold n*F = {n * self.F} values, got {Z_iF.size}")
             self._ck(self.lib.mhfem_set_state(self._h, _dptr(Z_iK), _dptr(Z_iF)))
 
     def setupLinearSystem(self) -> None:
@@ -296,17 +303,24 @@ class Solver:
         p = np.ascontiguousarray(params, np.float32)
         self._ck(self.lib.mhfem_learned_set_params(self._h, p.ctypes.data_as(ct.POINTER(ct.c_float)), p.size))
 
-    def learned_forward(self, features: np.ndarray) -> np.ndarray:
+    def _features(self, features: np.ndarray) -> np.ndarray:
         x = np.ascontiguousarray(features, np.float32)
-        assert x.shape == (self.F, L.LEARNED_FEATURES)
+        if x.shape != (self.F, L.LEARNED_FEATURES):
+            raise ValueError(f"features must have shape ({self.F}, {L.LEARNED_FEATURES}), got {x.shape}")
+        return x
+
+    def learned_forward(self, features: np.ndarray) -> np.ndarray:
+        x = self._features(features)
         out = np.empty(self.F, np.float32)
         self._ck(self.lib.mhfem_learned_forward(self._h, x.ctypes.data_as(ct.POINTER(ct.c_float)),
                                                 out.ctypes.data_as(ct.POINTER(ct.c_float))))
         return out
 
     def learned_gradients(self, features: np.ndarray, target: np.ndarray):
-        x = np.ascontiguousarray(features, np.float32)
+        x = self._features(features)
         y = np.ascontiguousarray(target, np.float64)
+        if y.shape != (self.F,):
+            raise ValueError(f"target must have shape ({self.F},), got {y.shape}")
         g = np.empty(self.learned_num_params(), np.float32)
         loss = ct.c_double()
         self._ck(self.lib.mhfem_learned_gradients(self._h, x.ctypes.data_as(ct.POINTER(ct.c_float)), _dptr(y),
