@@ -262,7 +262,8 @@ mhfem_status mhfem_get_array(mhfem_t h, int32_t which, double* out, int64_t coun
 /* The assembled system in CSR (rowptr has rows+1 entries), with the unit
  * diagonal included, columns ascending in each row exactly as the
  * reference's row setters emit them (LinearSystem.h:66-256,
- * BoundaryConditions.hpp:132-222).  Any pointer may be NULL. */
+ * BoundaryConditions.hpp:132-222).  cols and vals hold nnz entries and rhs
+ * rows entries (mhfem_get_sizes).  Any pointer may be NULL. */
 mhfem_status mhfem_get_system(mhfem_t h, int64_t* rowptr, int32_t* cols, double* vals,
                               double* rhs);
 
