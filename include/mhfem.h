@@ -4,8 +4,8 @@
  * The library implements the per-time-step hot path of TNL-MHFEM's CUDA
  * solver (TNL::MHFEM::Solver<Model, BoundaryModel, Matrix>, Solver.h:28-210)
  * on one GPU: local RT0 mass-matrix update, upwinding, local condensation,
- * in-place assembly of the hybridized face-trace system, its BiCGStab solve
- * and the reconstruction of the cell averages.  The reference's plugin API is
+ * in-place assembly of the hybridized face-trace system, its Krylov solve
+ * (BiCGStab or restarted GMRES) and the reconstruction of the cell averages.  The reference's plugin API is
  * compile-time C++ (a Model class derived from BaseModel plus a
  * BoundaryModel); this header is the run-time C equivalent a maintainer binds
  * from C, C++, ctypes or any other FFI.
@@ -92,7 +92,7 @@ typedef struct mhfem_solver_s* mhfem_t;
 #define MHFEM_ARRAY_Z_IK    8  /* cell values Z_iK (i,K)  */
 
 typedef struct {
-    int32_t dim;              /* 2: triangles, 3: tetrahedra (examples/config.h:17-21) */
+    int32_t dim;              /* 2: triangles or rectangles, 3: tetrahedra or cuboids (examples/config.h:13-21) */
     int32_t n_eq;             /* NumberOfEquations, 1 to 3 */
     int32_t mass_lumping;     /* MassLumping::enabled = 1 (MassMatrix.h:16-19) */
     int32_t advection;        /* MHFEM_*_UPWIND / MHFEM_IMPLICIT_TRACE */
