@@ -2,11 +2,15 @@
 from __future__ import annotations
 
 import copy
+from pathlib import Path
 
 import numpy as np
 
 from mhfem import _lib as L
 from mhfem import meshgen, problems
+from mhfem.solver import StaticConfig
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
 
 
 def rel_err(a, b) -> float:
@@ -173,3 +177,21 @@ def three_component_cases():
     q.Z0 = np.zeros(n * C)
     cases["adr2d_n3_implicit_upwind"] = q
     return cases
+
+
+def golden_names():
+    return sorted(f.stem for f in GOLDEN.glob("*.npz"))
+
+
+def golden_case(name: str):
+    """A committed fixture (tests/golden/make_golden.py): the problem its
+    inputs define, solved to 1e-13, and its expected outputs."""
+    d = dict(np.load(GOLDEN / f"{name}.npz"))
+    dim, n, lumping, advection, cell = (int(v) for v in d["config"])
+    cfg = StaticConfig(dim=dim, n_eq=n, mass_lumping=bool(lumping), advection=advection, mobility_upwind=False,
+                       cell=cell)
+    coeffs = {k[5:]: (float(v[0]) if v.size == 1 else v) for k, v in d.items() if k.startswith("coef_")}
+    bc = (d["bc_tags"], d["bc_values"], d["bc_dirichlet"])
+    p = problems.Problem(name, cfg, d["coords"], d["cells"], coeffs, d["Z0"], float(d["dt"]), int(d["steps"]),
+                         1e-13, lambda fv, fc: bc, 0)
+    return p, d

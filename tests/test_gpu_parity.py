@@ -12,7 +12,7 @@ import dataclasses
 import numpy as np
 import pytest
 
-from helpers import rel_err, small_cases
+from helpers import golden_case, golden_names, rel_err, small_cases
 from mhfem import _lib as L
 from mhfem import problems
 from oracle.oracle import OracleModel
@@ -87,6 +87,39 @@ def test_step_parity(name):
 
 def p_faces(s):
     return s.F
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_gpu_matches_golden(name):
+    """The GPU path against the committed fixtures (tests/golden): inputs and
+    expected outputs both read from the file, at the bars above."""
+    p, d = golden_case(name)
+    s = problems.make_solver(p, check_every=4)
+    fv, fc, cf = s.topology()
+    assert np.array_equal(fv, d["face_verts"])
+    assert np.array_equal(fc, d["face_cells"])
+    assert np.array_equal(cf, d["cell_faces"])
+    n, C = p.n, p.C
+    nf = p.config.faces_per_cell
+    t = 0.0
+    for step in range(p.steps):
+        s.preIterate(t, p.dt)
+        s.assembleLinearSystem(t, p.dt)
+        if step == 0:
+            assert rel_err(s.array("b", d["b0"].size), d["b0"]) < TOL_LOCAL
+            assert rel_err(s.array("R_ijKe", n * n * nf * C), d["R_ijKe0"]) < TOL_LOCAL
+            assert rel_err(s.array("R_iK", n * C), d["R_iK0"]) < TOL_LOCAL
+            rowptr, cols, vals, rhs = s.system()
+            assert np.array_equal(rowptr, d["rowptr"]) and np.array_equal(cols, d["cols"])
+            assert rel_err(vals, d["vals0"]) < TOL_LOCAL
+            assert rel_err(rhs, d["rhs0"]) < TOL_LOCAL
+        s.solveLinearSystem()
+        s.postIterate(t, p.dt)
+        zf, zk = s.state()
+        assert rel_err(zf, d["Z_iF"][step]) < TOL_STATE, f"step {step}: Z_iF"
+        assert rel_err(zk, d["Z_iK"][step]) < TOL_STATE, f"step {step}: Z_iK"
+        t += p.dt
+    s.close()
 
 
 def test_heat2d_full_size():

@@ -18,7 +18,7 @@ import numpy as np
 import pytest
 import scipy.sparse.linalg as spla
 
-from helpers import rel_err, small_cases, variant
+from helpers import golden_case, golden_names, rel_err, small_cases, variant
 from mhfem import _lib as L
 from mhfem import meshgen, problems
 from oracle.oracle import OracleModel, build_faces
@@ -228,3 +228,30 @@ def test_row_structure_and_direct_solve(name):
     x = spla.spsolve(A.tocsc(), m.rhs)
     m.solve(1e-14)
     assert rel_err(m.Z_iF, x) < 1e-10
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_oracle_reproduces_golden(name):
+    """The oracle still gives the committed fixtures (tests/golden): topology
+    and CSR pattern bit-exact, the first step's local arrays and system within
+    1e-12, the states after every step within 1e-10 (the solves run to 1e-13;
+    the fixtures were written with one thread, the test uses all)."""
+    p, d = golden_case(name)
+    m = OracleModel.from_problem(p)
+    assert np.array_equal(m.face_verts, d["face_verts"])
+    assert np.array_equal(m.face_cells, d["face_cells"])
+    assert np.array_equal(m.cell_faces, d["cell_faces"])
+    t = 0.0
+    for step in range(p.steps):
+        m.pre_iterate(t, p.dt)
+        m.assemble(t, p.dt)
+        if step == 0:
+            assert np.array_equal(m.rowptr, d["rowptr"]) and np.array_equal(m.cols, d["cols"])
+            for got, key in ((m.b, "b0"), (m.R_ijKe, "R_ijKe0"), (m.R_iK, "R_iK0"), (m.vals, "vals0"),
+                             (m.rhs, "rhs0")):
+                assert rel_err(got, d[key]) < 1e-12, key
+        m.solve(1e-13)
+        m.post_iterate(t, p.dt)
+        assert rel_err(m.Z_iF, d["Z_iF"][step]) < 1e-10, f"step {step}: Z_iF"
+        assert rel_err(m.Z_iK, d["Z_iK"][step]) < 1e-10, f"step {step}: Z_iK"
+        t += p.dt
