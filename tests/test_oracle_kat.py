@@ -255,3 +255,68 @@ def test_oracle_reproduces_golden(name):
         assert rel_err(m.Z_iF, d["Z_iF"][step]) < 1e-10, f"step {step}: Z_iF"
         assert rel_err(m.Z_iK, d["Z_iK"][step]) < 1e-10, f"step {step}: Z_iK"
         t += p.dt
+
+
+@pytest.mark.parametrize("name,lumping", [("heat2d", False), ("heat2d", True), ("diffusion3d", False),
+                                          ("diffusion3d", True), ("diffusion3d_box", False)])
+def test_pure_diffusion_matrix_is_symmetric_before_row_scaling(name, lumping):
+    """For pure diffusion the assembled A is symmetric before the unit-diagonal
+    row scaling, so the stored rows a_EF = A_EF / d_E satisfy
+    a_EF d_E = a_FE d_F for one positive d over every pair of rows that are
+    not Dirichlet rows (a Dirichlet row keeps only its diagonal).  d is
+    propagated along the graph from one row per component and the relation
+    checked on every pair."""
+    small = {"heat2d": dict(N=6), "diffusion3d": dict(N=3), "diffusion3d_box": dict(N=3)}[name]
+    p = variant(problems.WORKLOADS[name](steps=1, **small), mass_lumping=lumping)
+    m = OracleModel.from_problem(p)
+    m.pre_iterate(0.0, p.dt)
+    m.assemble(0.0, p.dt)
+    A = m.csr().tocsr()
+    R = A.shape[0]
+    # n = 1: row index = face index; tags matter on boundary faces only
+    free = (m.face_cells[:, 1] >= 0) | (m.tags != 0)
+    a = {}
+    for r in np.flatnonzero(free):
+        for k in range(A.indptr[r], A.indptr[r + 1]):
+            c = A.indices[k]
+            if c != r and free[c]:
+                a[(r, c)] = A.data[k]
+    assert a, "no coupled free rows"
+    for (r, c), v in a.items():
+        assert (r, c)[::-1] in a, f"entry ({r}, {c}) has no transposed partner"
+        assert v * a[(c, r)] > 0
+    nbr = {}
+    for r, c in a:
+        nbr.setdefault(r, []).append(c)
+    d = np.full(R, np.nan)
+    for root in nbr:
+        if not np.isnan(d[root]):
+            continue
+        d[root] = 1.0
+        stack = [root]
+        while stack:
+            r = stack.pop()
+            for c in nbr[r]:
+                if np.isnan(d[c]):
+                    d[c] = d[r] * a[(r, c)] / a[(c, r)]
+                    stack.append(c)
+    scale = max(abs(v * d[r]) for (r, c), v in a.items())
+    worst = max(abs(v * d[r] - a[(c, r)] * d[c]) for (r, c), v in a.items())
+    assert worst < 1e-12 * scale
+
+
+def test_same_seed_same_mesh_numbering_and_system():
+    """Determinism: the same seeds give an identical mesh, face numbering,
+    CSR pattern and (one thread) bitwise identical values."""
+    def run():
+        p = problems.diffusion3d(N=3, steps=1)
+        m = OracleModel.from_problem(p, threads=1)
+        m.pre_iterate(0.0, p.dt)
+        m.assemble(0.0, p.dt)
+        return p, m
+
+    (p1, m1), (p2, m2) = run(), run()
+    assert np.array_equal(p1.coords, p2.coords) and np.array_equal(p1.cells, p2.cells)
+    assert np.array_equal(np.asarray(p1.coeffs["D"]), np.asarray(p2.coeffs["D"]))
+    for k in ("face_verts", "face_cells", "cell_faces", "rowptr", "cols", "vals", "rhs"):
+        assert np.array_equal(getattr(m1, k), getattr(m2, k)), k
