@@ -131,3 +131,26 @@ def test_solver_checks_array_sizes_before_the_library_call():
         s.learned_forward(np.zeros((25, 3), np.float32))
     with pytest.raises(ValueError, match="target"):
         s.learned_gradients(np.zeros((25, L.LEARNED_FEATURES), np.float32), np.zeros(24))
+
+
+@pytest.mark.parametrize("lang,std", [("c", "-std=c99"), ("c++", "-std=c++17")])
+def test_header_compiles_as_strict_c_and_cpp(tmp_path, lang, std):
+    """include/mhfem.h is a plain C header (what an FFI binds), warning-free
+    as strict C99 and as C++17, and links against the library's symbols."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc" if lang == "c" else "g++")
+    if cc is None:
+        pytest.skip("no host compiler")
+    src = tmp_path / "use_header.c"
+    src.write_text('#include "mhfem.h"\n'
+                   "int main(void) { mhfem_solver_opts o; mhfem_default_solver_opts(&o);\n"
+                   "  return o.max_iter > 0 && o.tol > 0 ? 0 : 1; }\n")
+    flags = ["-Wall", "-Wextra", "-Werror"] + (["-pedantic"] if lang == "c" else [])
+    out = tmp_path / "use_header"
+    r = subprocess.run([cc, std, *flags, "-I", str(REPO / "include"), "-x", lang, str(src), "-x", "none",
+                        str(L.LIB_PATH), f"-Wl,-rpath,{L.LIB_PATH.parent}", "-o", str(out)],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert subprocess.run([str(out)], timeout=60).returncode == 0
