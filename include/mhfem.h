@@ -164,7 +164,9 @@ void         mhfem_default_solver_opts(mhfem_solver_opts* opts);
 mhfem_status mhfem_set_mesh(mhfem_t h, int64_t num_vertices, const double* coords,
                             int64_t num_cells, const int32_t* cell_verts);
 
-/* Sizes: vertices, cells, faces, rows (n*F) and non-zeros of the face system. */
+/* Sizes: vertices, cells, faces, rows (n*F, Solver::getDofs, Solver.hpp:560-569)
+ * and non-zeros of the face system (the row capacities, Solver.hpp:449-484).
+ * Any output pointer may be NULL. */
 mhfem_status mhfem_get_sizes(mhfem_t h, int64_t* V, int64_t* C, int64_t* F,
                              int64_t* rows, int64_t* nnz);
 
