@@ -146,7 +146,11 @@ typedef struct {
 /* Replaces constructing Solver<Model,...> with its compile-time static
  * configuration (examples/config.h:1-61, examples/main.h:17). */
 mhfem_status mhfem_create(const mhfem_desc* desc, mhfem_t* out);
+/* Frees every device array the handle owns (the Solver owns mdd and its
+ * arrays, Solver.h:182-207). */
 mhfem_status mhfem_destroy(mhfem_t h);
+/* Message of the last failure on the handle: the text the reference puts in
+ * its exceptions (e.g. the non-convergence message of Solver.hpp:1259-1264). */
 const char*  mhfem_last_error(mhfem_t h);
 void         mhfem_default_solver_opts(mhfem_solver_opts* opts);
 
@@ -235,7 +239,9 @@ mhfem_status mhfem_set_bc(mhfem_t h, const uint8_t* tags, const double* values,
  * cells (Solver.hpp:319-339) and v_iKe = 0. */
 mhfem_status mhfem_set_initial_condition(mhfem_t h, const double* Z_iK);
 
-/* Sets both state arrays explicitly (restart). Z_iF may be NULL: face average. */
+/* Sets both state arrays explicitly: a restart from saved Z_iK and Z_iF (the
+ * reference restarts from the initial-condition file, Solver.hpp:296-306,
+ * and averages Z_iF from it); Z_iF may be NULL: that face average. */
 mhfem_status mhfem_set_state(mhfem_t h, const double* Z_iK, const double* Z_iF);
 
 /* Replaces Solver::setup's solver selection (Solver.hpp:88-258) and the
@@ -257,8 +263,11 @@ mhfem_status mhfem_step(mhfem_t h, double t, double tau, mhfem_step_stats* stats
 
 /* ---- results ------------------------------------------------------------ */
 
-/* Z_iF (n*F, (E,i)) and Z_iK (n*C, (i,K)); either may be NULL. */
+/* Z_iF (n*F, (E,i)) and Z_iK (n*C, (i,K)); either may be NULL.  What a
+ * model's makeSnapshot reads (HeatEquationModel.h:164-231). */
 mhfem_status mhfem_get_state(mhfem_t h, double* Z_iF, double* Z_iK);
+/* One of the scheme arrays of BaseModel (BaseModel.h:280-286), MHFEM_ARRAY_*;
+ * count must be its size. */
 mhfem_status mhfem_get_array(mhfem_t h, int32_t which, double* out, int64_t count);
 
 /* The assembled system in CSR (rowptr has rows+1 entries), with the unit
