@@ -70,7 +70,7 @@ def golden_problems() -> dict:
     advection variants and boundary tags.  None uses mobility upwinding,
     whose step parity needs the GPU's velocities where the upwind choice is
     at rounding level."""
-    from helpers import box_cases, three_component_cases, variant
+    from helpers import box_cases, dummy_row_cases, three_component_cases, variant
     from mhfem import _lib as L
     from mhfem import problems
 
@@ -90,6 +90,8 @@ def golden_problems() -> dict:
     cases["adr2d_rect_implicit_upwind"] = variant(p, advection=L.IMPLICIT_UPWIND, mass_lumping=False)
     cases["adr2d_n3_implicit_upwind"] = three_component_cases()["adr2d_n3_implicit_upwind"]
     cases["diffusion3d_box_n2"] = box_cases()["diffusion3d_box_n2"]
+    # an all-zero row of Q on isolated cells: the dummy equation of Solver.hpp:829-847
+    cases["diffusion3d_dummy_row"] = dummy_row_cases(N=3)["diffusion3d_dummy_row"]
     return cases
 
 

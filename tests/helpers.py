@@ -75,6 +75,76 @@ def small_cases():
     cases["diffusion3d_n2"] = q
     cases.update(three_component_cases())
     cases.update(box_cases())
+    cases.update(dummy_row_cases())
+    return cases
+
+
+def isolated_interior_cells(cells: np.ndarray, stride: int = 5) -> np.ndarray:
+    """Simplex cells with no boundary face, no two of them sharing a face:
+    every `stride`-th interior cell in index order, skipping the neighbours of
+    cells already taken."""
+    C, nf = cells.shape
+    faces = np.sort(np.stack([np.delete(cells, e, axis=1) for e in range(nf)], axis=1), axis=2)
+    _, inv, counts = np.unique(faces.reshape(C * nf, -1), axis=0, return_inverse=True, return_counts=True)
+    inv = inv.reshape(C, nf)
+    interior = (counts[inv] == 2).all(axis=1)
+    by_face = {}
+    for K in range(C):
+        for e in range(nf):
+            by_face.setdefault(int(inv[K, e]), []).append(K)
+    taken, blocked = [], set()
+    for K in np.flatnonzero(interior)[::stride]:
+        if K in blocked:
+            continue
+        taken.append(int(K))
+        for e in range(nf):
+            blocked.update(by_face[int(inv[K, e])])
+    return np.array(taken, np.int64)
+
+
+def dummy_row_cases(N: int = 4):
+    """Cells whose local matrix Q_K has an all-zero row, so that the reference
+    replaces that row by the dummy equation Q_ii = 1, R_iK += Z_iK
+    (Solver.hpp:829-847): on isolated interior cells one component has D = 0,
+    N = 0 and r = 0 (and u = 0, no implicit advection).  Its face rows there
+    take their entries from the neighbouring cells only.  n = 1 on tetrahedra,
+    and n = 2 on tetrahedra where only the second component vanishes (the
+    first keeps its coupling D_01, so the LU of Q mixes the dummy row into
+    the other one)."""
+    cases = {}
+    p = problems.diffusion3d(N=N, steps=3)
+    C = p.C
+    iso = isolated_interior_cells(p.cells)
+    rng = np.random.default_rng(23)
+    D = np.array(p.coeffs["D"], np.float64, copy=True)
+    D[iso] = 0.0
+    Nc = np.ones(C)
+    Nc[iso] = 0.0
+    w = rng.uniform(-0.01, 0.01, (4, C))
+    q = variant(p, coeffs={"D": D, "N": Nc, "w": w.ravel()})
+    q.Z0 = rng.uniform(0, 1, C)
+    q.extra = {"dummy_cells": iso}
+    cases["diffusion3d_dummy_row"] = q
+
+    p3 = problems.diffusion3d(N=N, steps=3)
+    Nc = np.zeros((2, 2, C)); Nc[0, 0] = 1.0; Nc[1, 1] = 2.0
+    D = np.zeros((2, 2, C)); D[0, 0] = p3.coeffs["D"]; D[1, 1] = 0.5 * p3.coeffs["D"]
+    D[0, 1] = 0.1; D[1, 0] = 0.05
+    r = np.zeros((2, 2, C)); r[0, 0] = 0.3; r[0, 1] = -0.1; r[1, 0] = -0.1; r[1, 1] = 0.2
+    for arr in (Nc, D, r):
+        arr[1, :, iso] = 0.0
+    w = rng.uniform(-0.01, 0.01, (2, 4, C))
+    base_bc = p3.bc_fn
+
+    def bc2(fv, fc):
+        t, v, d = base_bc(fv, fc)
+        return np.concatenate([t, t]), np.concatenate([v, v + 0.1 * (t == 1)]), np.concatenate([d + 0.2, d])
+
+    q = variant(p3, n_eq=2, coeffs={"N": Nc.ravel(), "D": D.ravel(), "r": r.ravel(), "w": w.ravel(), "f": 0.5})
+    q.bc_fn = bc2
+    q.Z0 = rng.uniform(0, 1, 2 * C)
+    q.extra = {"dummy_cells": iso, "dummy_component": 1}
+    cases["diffusion3d_n2_dummy_row"] = q
     return cases
 
 

@@ -320,3 +320,37 @@ def test_same_seed_same_mesh_numbering_and_system():
     assert np.array_equal(np.asarray(p1.coeffs["D"]), np.asarray(p2.coeffs["D"]))
     for k in ("face_verts", "face_cells", "cell_faces", "rowptr", "cols", "vals", "rhs"):
         assert np.array_equal(getattr(m1, k), getattr(m2, k)), k
+
+
+@pytest.mark.parametrize("name", ["diffusion3d_dummy_row", "diffusion3d_n2_dummy_row"])
+def test_dummy_equation_for_singular_q(name):
+    """Cells whose Q_K has an all-zero row i take the reference's dummy
+    equation Q_ii = 1, R_iK += Z_iK (Solver.hpp:829-847).  There D_ij = 0 and
+    N_ij = 0 for that i, so b and hence R_ijKe vanish, and the reconstruction
+    Z_iK = sum R_ijKf Z_jF + R_iK (Solver.hpp:1283-1292) gives, whatever the
+    face traces, Z_iK_new = Z_iK + |K| f_i - sum_e m_iE_upw w_iKe (the R_iK of
+    SecondaryCoefficients.h:87-127 without its N and advection terms).  The
+    other cells still follow the face solve, checked against a direct sparse
+    solve."""
+    p = small_cases()[name]
+    m = OracleModel.from_problem(p)
+    n, C = p.n, p.C
+    iso = p.extra["dummy_cells"]
+    i = p.extra.get("dummy_component", 0)
+    X = p.coords[p.cells]
+    vol = np.abs(np.linalg.det(X[:, 1:] - X[:, :1])) / 6
+    f = np.broadcast_to(np.asarray(p.coeffs.get("f", 0.0), np.float64), (n * C,)).reshape(n, C)
+    w = np.asarray(p.coeffs["w"], np.float64).reshape(n, 4, C)
+    t = 0.0
+    for _ in range(p.steps):
+        z_old = m.Z_iK.reshape(n, C)[i, iso].copy()
+        m.pre_iterate(t, p.dt)
+        m.assemble(t, p.dt)
+        x = spla.spsolve(m.csr().tocsc(), m.rhs)
+        m.solve(1e-14)
+        assert rel_err(m.Z_iF, x) < 1e-10
+        m.post_iterate(t, p.dt)
+        expect = z_old + vol[iso] * f[i, iso] - w[i, :, iso].sum(axis=1)
+        got = m.Z_iK.reshape(n, C)[i, iso]
+        assert np.abs(got - expect).max() <= 1e-13 * max(1.0, np.abs(expect).max())
+        t += p.dt
