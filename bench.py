@@ -15,8 +15,15 @@ Rank 0 prints one JSON line.  `value` is time steps/s of the plain FP64 form
 summed over all replicas (each GPU runs an independent copy of the
 workload: the path is not sharded, "replicas only").  `e2e` is the same
 metric through the public C ABI with host buffers: every step uploads the
-source field from pinned host memory and reads Z_iK back.  The mixed form is
-reported beside it under "forms".  `--impl reference` times the CPU
+source field from pinned host memory and reads Z_iK back.  Beside it:
+  forms.mixed             the mixed form on the same workload and steps;
+  forms.learned_protocol  the learned-form protocol (200 training + 800 used
+                          steps of the time-varying source) for four forms;
+  other_configs           the 128^2 heat equation (100 steps), the 512^2
+                          two-component ADR (200 steps) and the mixed form on
+                          the 128^3 cube (20 steps);
+every one with the relative error of each step's face traces against the
+FP64 form solved to 1e-13 in lockstep.  `--impl reference` times the CPU
 restatement of the reference algorithm (the reference itself cannot be
 built: its TNL dependency is absent) on all host cores.
 """
@@ -49,23 +56,43 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--grid", type=int, default=64, help="cubes per axis (64 = the benchmark workload)")
-    ap.add_argument("--cpu-steps", type=int, default=3, help="time steps of the CPU baseline sample")
+    ap.add_argument("--cpu-steps", type=int, default=3, help="timed time steps of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-form protocol leg")
     ap.add_argument("--no-box", action="store_true", help="skip the cuboid (box cell) leg")
     ap.add_argument("--no-gmres", action="store_true", help="skip the GMRES leg")
-    ap.add_argument("--mixed-error-steps", type=int, default=0,
-                    help="after timing: run the mixed and FP64 forms in lockstep for K steps from the same state "
-                         "and report each step's relative error of the mixed face traces")
-    ap.add_argument("--learned-train", type=int, default=200,
-                    help="online training steps of the learned form before its timed steps")
+    ap.add_argument("--configs", default="heat2d,adr2d,mixed128",
+                    help="comma-separated other workloads to run: heat2d (128^2 heat equation, 100 steps), "
+                         "adr2d (512^2 two-component ADR, 200 steps), mixed128 (mixed form on the 128^3 cube, "
+                         "20 steps); 'none' skips them")
+    ap.add_argument("--learned-train", type=int, default=200, help="online training steps of the learned protocol")
+    ap.add_argument("--learned-used", type=int, default=800, help="steps after training in the learned protocol")
+    ap.add_argument("--learned-iters", type=int, default=2, help="Adam iterations per training step")
+    ap.add_argument("--learned-order", type=int, default=3,
+                    help="polynomial extrapolation order of the base the network corrects (0-3)")
     ap.add_argument("--profile-run", action="store_true",
                     help="only the warm-up and timed steps (for an ncu launch list)")
     ap.add_argument("--profile-form", choices=["fp64", "mixed", "learned", "box", "gmres"], default="fp64",
                     help="form used by --profile-run (learned: --learned-train training steps first)")
     return ap.parse_args()
+
+
+def allowed_cpus() -> int:
+    """Host threads this process may run on (its CPU affinity)."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def workload_config(grid, C, F, rows, tol, dt, n=1, nf=4):
+    """The `config` object of both arms: the same keys and values for the same workload."""
+    W = (2 * nf - 1) * n - 1
+    return {"workload": f"diffusion3d_{grid}", "cells": C, "faces": F, "rows": rows, "tol": tol, "dt": dt,
+            "l2": f"working set larger than L2 (ELL values+columns {rows * W * 12 / 1e6:.0f} MB, cell records "
+                  f"{8 * (n * nf + 1) * n * nf * C / 1e6:.0f} MB)"}
 
 
 def dist_env():
@@ -163,7 +190,7 @@ def run_reference_arm(args, rank, world):
     from oracle.oracle import OracleModel, load
 
     lib = load()
-    threads = os.cpu_count() or 1
+    threads = allowed_cpus()
     lib.orc_set_threads(threads)
     p = problems.diffusion3d(N=args.grid)
     m = OracleModel.from_problem(p)
@@ -179,12 +206,14 @@ def run_reference_arm(args, rank, world):
         t += p.dt
     el = time.perf_counter() - t0
     value = args.steps / el
-    sample = f"{args.steps} time steps of the {args.grid}^3 tetrahedral workload after {args.warmup} warm-up steps"
+    sample = (f"{args.steps} time steps of the {args.grid}^3 tetrahedral workload after {args.warmup} warm-up steps "
+              f"(CPU restatement of the reference algorithm, C + OpenMP, -O3 as the reference's release build, FP64)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": f"diffusion3d_{args.grid}", "cells": m.C, "faces": m.F,
-                                            "form": "fp64 (CPU restatement, OpenMP)", "tol": p.tol, "dt": p.dt},
+            "data": f"synthetic: seeded jittered {args.grid}^3 cube grid split into 6 tetrahedra, D = exp(Gaussian field)",
+            "form": "fp64 (CPU restatement, OpenMP)",
+            "config": workload_config(args.grid, m.C, m.F, m.F * p.n, p.tol, p.dt),
             "face_dof_per_s": value * m.F * p.n, "iterations_per_step": statistics.mean(iters),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -201,6 +230,34 @@ def kernel_table(s, L, hbm_peak):
         out[name] = {"ms": r["ms"], "gbs": gbs, "hbm_frac": gbs / hbm_peak,
                      "fp64_tflops": r["flops"] / (r["ms"] * 1e-3) / 1e12}
     return out
+
+
+# The five kernels of one FP64 BiCGStab iteration (one launch each; every
+# check_every-th iteration the second SpMV and the x / r update also form the
+# norms): name, kernel id, kernel symbol.
+ITERATION_KERNELS = [
+    ("spmv_dot", "KERNEL_SPMV_FP64", "k_spmv_dot<double,6,1> (v = A p, (rh, v))"),
+    ("update_s", "KERNEL_UPDATE_S_FP64", "k_update_s<double,2> (s = r - alpha v)"),
+    ("spmv_dots2", "KERNEL_SPMV2_FP64", "k_spmv_dots2<double,6,1,0> (t = A s, (t, s), (t, t))"),
+    ("update_xr", "KERNEL_UPDATE_XR_FP64", "k_update_xr<double,2,0> (x, r updates, (rh, r))"),
+    ("update_p", "KERNEL_UPDATE_P_FP64", "k_update_p<double,2> (p = r + beta (p - omega v))"),
+]
+
+
+def iteration_table(s, L, hbm_peak, reps=50):
+    """CUDA-event time, algorithmic bytes and share of the iteration of each
+    FP64 BiCGStab kernel, timed alone (back-to-back launches on the
+    library's stream); the roofline names the one with the largest share."""
+    out = {}
+    for name, kid, sym in ITERATION_KERNELS:
+        r = s.time_kernel(getattr(L, kid), reps=reps)
+        gbs = r["bytes"] / (r["ms"] * 1e-3) / 1e9
+        out[name] = {"kernel": sym, "ms": r["ms"], "bytes": r["bytes"], "gbs": gbs, "hbm_frac": gbs / hbm_peak,
+                     "fp64_tflops": r["flops"] / (r["ms"] * 1e-3) / 1e12}
+    total = sum(v["ms"] for v in out.values())
+    for v in out.values():
+        v["share_of_iteration"] = v["ms"] / total
+    return out, total
 
 
 def box_leg(args, dev, world):
@@ -274,146 +331,285 @@ def gmres_leg(args, dev, world):
             "ms_per_step": el / args.steps, "iterations_per_step": (it1 - it0) / args.steps}
 
 
-def mixed_lockstep_errors(args, dev, zk, zf, t):
-    """Per-step relative errors of the face traces, outside the timed region:
-    the mixed form and the FP64 form at the workload's tolerance and the FP64
-    form solved to 1e-13 (the exact discrete solution up to rounding), all
-    advanced in lockstep from the same state; each step's traces of the first
-    two against the third, and the mixed form against the FP64 form."""
+class Arm:
+    """One solver of a lockstep run: every step is timed with CUDA events on
+    the library's stream (synchronized after the step, so other solvers' work
+    between the steps is not counted), and its face traces are compared on
+    the device with the reference solver's after every step."""
+
+    def __init__(self, name, sol, dev):
+        import torch
+
+        self.name, self.sol, self.dev = name, sol, dev
+        self.ext = torch.cuda.ExternalStream(sol.stream(), device=dev)
+        self.e0 = torch.cuda.Event(enable_timing=True)
+        self.e1 = torch.cuda.Event(enable_timing=True)
+        self.ms, self.stats, self.err_f, self.err_k = [], [], [], []
+        self.zf = torch.as_tensor(sol.array_device("Z_iF"), device=f"cuda:{dev}")
+        self.zk = torch.as_tensor(sol.array_device("Z_iK"), device=f"cuda:{dev}")
+
+    def step(self, t, dt):
+        self.e0.record(self.ext)
+        st = self.sol.step(t, dt)
+        self.e1.record(self.ext)
+        self.e1.synchronize()
+        self.ms.append(self.e0.elapsed_time(self.e1))
+        self.stats.append(st)
+        return st
+
+    def close(self):
+        self.sol.close()
+
+
+def _rel_dev(a, b) -> float:
+    """max |a - b| / max |b| on the device (FP64)."""
+    return float((a - b).abs().max() / b.abs().max().clamp_min(1e-300))
+
+
+def lockstep(arms, exact, dt, steps, t0=0.0):
+    """Advances every arm and the reference solver `exact` (FP64 solved to
+    1e-13, the exact discrete solution up to rounding) from the same state in
+    lockstep; after each step every arm's face traces and cell values are
+    compared with the reference's."""
+    t = t0
+    for _ in range(steps):
+        for a in arms:
+            a.step(t, dt)
+        if exact is not None:
+            exact.step(t, dt)
+            for a in arms:
+                a.err_f.append(_rel_dev(a.zf, exact.zf))
+                a.err_k.append(_rel_dev(a.zk, exact.zk))
+        t += dt
+    return t
+
+
+def arm_summary(a, world=1, lo=0, hi=None, err_bound=1e-8, full_errors=True):
+    """Steps/s, iterations and errors of an arm over steps [lo, hi)."""
     import numpy as np
 
-    from mhfem import _lib as L
-    from mhfem import problems
-
-    sols = {}
-    for name, form in (("mixed", L.FORM_MIXED), ("fp64", L.FORM_FP64), ("exact", L.FORM_FP64)):
-        q = problems.diffusion3d(N=args.grid, form=form)
-        q.config.device = dev
-        if name == "exact":
-            q.tol = 1e-13
-        sol = problems.make_solver(q, check_every=8)
-        sol.setInitialCondition(zk, zf)
-        sols[name] = sol
-    rel = lambda a, b: float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
-    out = {"mixed_vs_fp64_1e-13": [], "fp64_vs_fp64_1e-13": [], "mixed_vs_fp64": []}
-    for _ in range(args.mixed_error_steps):
-        for sol in sols.values():
-            sol.step(t, q.dt)
-        a, _ = sols["mixed"].state()
-        b, _ = sols["fp64"].state()
-        c, _ = sols["exact"].state()
-        out["mixed_vs_fp64_1e-13"].append(rel(a, c))
-        out["fp64_vs_fp64_1e-13"].append(rel(b, c))
-        out["mixed_vs_fp64"].append(rel(a, b))
-        t += q.dt
-    for sol in sols.values():
-        sol.close()
+    hi = len(a.ms) if hi is None else hi
+    ms = float(np.sum(a.ms[lo:hi]))
+    n = hi - lo
+    its = [st["iterations"] for st in a.stats[lo:hi]]
+    out = {"value": world * n / (ms / 1e3), "ms_per_step": ms / n, "steps": n,
+           "iterations_per_step": float(np.mean(its))}
+    sw = [st["sweeps"] for st in a.stats[lo:hi]]
+    if max(sw) > 1:
+        out["sweeps_per_step"] = float(np.mean(sw))
+    if a.err_f:
+        ef, ek = a.err_f[lo:hi], a.err_k[lo:hi]
+        out["rel_err_vs_fp64_1e-13_max"] = {"face_traces": max(ef), "cell_values": max(ek)}
+        out["steps_over_1e-8"] = int(sum(1 for e in ef if e > err_bound))
+        if full_errors:
+            out["rel_err_vs_fp64_1e-13_per_step"] = [float(f"{e:.3e}") for e in ef]
+        else:
+            out["rel_err_vs_fp64_1e-13_every_10th_step"] = [float(f"{e:.3e}") for e in ef[::10]]
     return out
 
 
-def learned_leg(args, dev, world):
-    """Learned warm start on the time-varying source workload
-    f = 1 + 0.5 sin(2 pi t / T) psi(x), T = 1000 dt: online training on the
-    first `learned_train` steps, then the same warm-up + timed steps for the
-    learned form and for the plain FP64 form started from the identical state."""
+def _solver(p, dev, check_every=8, tol=None):
+    from mhfem import problems
+
+    p.config.device = dev
+    if tol is not None:
+        p.tol = tol
+    return problems.make_solver(p, check_every=check_every)
+
+
+def mixed_leg(args, dev, world, el_fp64_ms):
+    """The mixed form on the headline workload: the same warm-up and timed
+    steps as the FP64 form, in lockstep with the FP64 form solved to 1e-13
+    (per-step errors of every step, warm-up included), and the FP32 SpMV."""
+    from mhfem import _lib as L
+    from mhfem import problems
+
+    pm = problems.diffusion3d(N=args.grid, form=L.FORM_MIXED)
+    mixed = Arm("mixed", _solver(pm, dev), dev)
+    exact = Arm("exact", _solver(problems.diffusion3d(N=args.grid), dev, tol=1e-13), dev)
+    lockstep([mixed], exact, pm.dt, args.warmup + args.steps)
+    out = arm_summary(mixed, world, lo=args.warmup)
+    out["speedup_vs_fp64"] = (out["value"] / world) / (args.steps / (el_fp64_ms / 1e3))
+    errs = arm_summary(mixed, world)
+    out["rel_err_vs_fp64_1e-13_per_step"] = errs["rel_err_vs_fp64_1e-13_per_step"]
+    out["rel_err_vs_fp64_1e-13_max"] = errs["rel_err_vs_fp64_1e-13_max"]
+    out["steps_over_1e-8"] = errs["steps_over_1e-8"]
+    out["error_steps"] = "every step from the initial state, warm-up steps included"
+    sp32 = mixed.sol.time_kernel(L.KERNEL_SPMV_FP32, reps=50)
+    out["spmv_fp32_gbs"] = sp32["bytes"] / (sp32["ms"] * 1e-3) / 1e9
+    mixed.close()
+    exact.close()
+    return out
+
+
+def heat2d_leg(args, dev, world):
+    """BASELINE config 1: the plain FP64 heat equation on the 128^2 triangle
+    mesh (49,408 faces), 100 steps of dt = 1e-4 from the Gaussian bump, tol
+    1e-12; every step timed, in lockstep with the FP64 form at 1e-13; the CPU
+    oracle over the same 100 steps beside it."""
+    from mhfem import problems
+
+    p = problems.heat2d(N=128)
+    a = Arm("fp64", _solver(p, dev), dev)
+    exact = Arm("exact", _solver(problems.heat2d(N=128), dev, tol=1e-13), dev)
+    lockstep([a], exact, p.dt, p.steps)
+    out = {"workload": "heat2d_128 (BASELINE config 1)", "cells": a.sol.C, "faces": a.sol.F, "tol": p.tol,
+           "dt": p.dt, "steps_from_initial_condition": p.steps, "fp64": arm_summary(a, world, full_errors=False)}
+    out["fp64"]["face_dof_per_s"] = out["fp64"]["value"] * a.sol.F
+    a.close()
+    exact.close()
+    if not args.no_cpu_baseline and world == 1:
+        out["cpu_baseline"] = cpu_baseline(problems.heat2d(N=128), p.steps, warmup=0,
+                                           what=f"all {p.steps} time steps of the 128^2 heat-equation workload")
+    return out
+
+
+def adr2d_leg(args, dev, world):
+    """BASELINE config 3: coupled two-component advection-diffusion-reaction on
+    the 512^2 triangle mesh (n = 2, 1,574,912 rows), 200 steps of dt = 5e-4,
+    tol 1e-10; every step timed, in lockstep with the FP64 form at 1e-13."""
+    from mhfem import problems
+
+    p = problems.adr2d(N=512)
+    a = Arm("fp64", _solver(p, dev), dev)
+    exact = Arm("exact", _solver(problems.adr2d(N=512), dev, tol=1e-13), dev)
+    lockstep([a], exact, p.dt, p.steps)
+    out = {"workload": "adr2d_512 (BASELINE config 3)", "cells": a.sol.C, "faces": a.sol.F, "rows": 2 * a.sol.F,
+           "tol": p.tol, "dt": p.dt, "steps_from_initial_condition": p.steps,
+           "fp64": arm_summary(a, world, full_errors=False)}
+    out["fp64"]["face_dof_per_s"] = out["fp64"]["value"] * 2 * a.sol.F
+    a.close()
+    exact.close()
+    if not args.no_cpu_baseline and world == 1:
+        out["cpu_baseline"] = cpu_baseline(problems.adr2d(N=512), args.cpu_steps, warmup=1,
+                                           what=f"{args.cpu_steps} time steps of the 512^2 ADR workload after 1 "
+                                                "warm-up step")
+    return out
+
+
+def mixed128_leg(args, dev, world):
+    """BASELINE config 4: the mixed form on the 128^3 cube (12,582,912
+    tetrahedra, 25,264,128 faces), 20 steps from the initial state, with the
+    plain FP64 form on the same steps, both in lockstep with the FP64 form
+    solved to 1e-13; the assembly kernel timed at this size."""
+    from mhfem import _lib as L
+    from mhfem import problems
+
+    hbm_peak, _ = measured_peaks()
+    steps = 20
+    fp = Arm("fp64", _solver(problems.diffusion3d(N=128), dev), dev)
+    mx = Arm("mixed", _solver(problems.diffusion3d(N=128, form=L.FORM_MIXED), dev), dev)
+    exact = Arm("exact", _solver(problems.diffusion3d(N=128), dev, tol=1e-13), dev)
+    p = problems.diffusion3d(N=2)
+    lockstep([fp, mx], exact, p.dt, steps)
+    out = {"workload": "diffusion3d_128 (BASELINE config 4)", "cells": fp.sol.C, "faces": fp.sol.F, "tol": p.tol,
+           "dt": p.dt, "inner_tol": 1e-4, "steps_from_initial_condition": steps,
+           "fp64": arm_summary(fp, world), "mixed": arm_summary(mx, world)}
+    out["mixed"]["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["iterations_per_step_fp64"] = [st["iterations"] for st in fp.stats]
+    out["inner_iterations_per_step_mixed"] = [st["iterations"] for st in mx.stats]
+    out["sweeps_per_step_mixed"] = [st["sweeps"] for st in mx.stats]
+    kern = {}
+    for name, sol in (("assemble_fp64", fp.sol), ("assemble_mixed", mx.sol)):
+        r = sol.time_kernel(L.KERNEL_ASSEMBLE, reps=10)
+        gbs = r["bytes"] / (r["ms"] * 1e-3) / 1e9
+        kern[name] = {"ms": r["ms"], "gbs": gbs, "hbm_frac": gbs / hbm_peak}
+    r = fp.sol.time_kernel(L.KERNEL_SPMV_FP64, reps=20)
+    kern["spmv_fp64"] = {"ms": r["ms"], "gbs": r["bytes"] / (r["ms"] * 1e-3) / 1e9}
+    kern["spmv_fp64"]["hbm_frac"] = kern["spmv_fp64"]["gbs"] / hbm_peak
+    out["kernels"] = kern
+    for a in (fp, mx, exact):
+        a.close()
+    return out
+
+
+def learned_protocol_leg(args, dev, world):
+    """BASELINE config 5, the whole protocol: the time-varying source
+    f = 1 + 0.5 sin(2 pi t / T) psi(x) on the 64^3 workload (T = the
+    protocol's span), the network trained online on the first
+    `learned_train` steps and used for the next `learned_used`.  Four forms
+    run it from the initial state, each timed over every step (training
+    included): plain FP64, mixed, learned (FP64 BiCGStab from the gated
+    guess: the protocol's form) and learned with the mixed-precision solve;
+    all in lockstep with the FP64 form solved to 1e-13 for per-step errors."""
     import numpy as np
-    import torch
 
     from mhfem import _lib as L
     from mhfem import problems
 
-    total = 1000
-    pl = problems.diffusion3d_source(N=args.grid, steps=total, form=L.FORM_LEARNED)
-    pl.config.device = dev
-    sl = problems.make_solver(pl, check_every=8)
-    sl.learned_options(train_steps=args.learned_train, train_iters=4, learning_rate=3e-3)
-    t = 0.0
-    t0 = time.perf_counter()
-    train_iters = []
-    for _ in range(args.learned_train):
-        train_iters.append(sl.step(t, pl.dt)["iterations"])
-        t += pl.dt
-    torch.cuda.synchronize()
-    train_s = time.perf_counter() - t0
-    zf, zk = sl.state()
-
-    def from_state(form):
-        q = problems.diffusion3d_source(N=args.grid, steps=total, form=form)
-        q.config.device = dev
-        sq = problems.make_solver(q, check_every=8)
-        sq.setInitialCondition(zk, zf)
-        return sq
-
-    sf = from_state(L.FORM_FP64)
-    # the trained network in a second learned solver whose solve from the
-    # guess is the mixed-precision refinement; the plain mixed form beside it
-    slm = from_state(L.FORM_LEARNED)
-    slm.learned_options(train_steps=0, mixed_solve=True)
-    slm.set_learned_params(sl.learned_params())
-    smx = from_state(L.FORM_MIXED)
-    arms = (("learned", sl), ("fp64", sf), ("learned_mixed", slm), ("mixed", smx))
-    for _ in range(args.warmup):
-        for _, sol in arms:
-            sol.step(t, pl.dt)
-        t += pl.dt
-    res = {}
-    for name, sol in arms:
-        ext = torch.cuda.ExternalStream(sol.stream(), device=dev)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        tt = t
-        its, used, rg, rw, sw = [], 0, [], [], []
-        torch.cuda.synchronize()
-        e0.record(ext)
-        for _ in range(args.steps):
-            st = sol.step(tt, pl.dt)
-            its.append(st["iterations"])
-            sw.append(st["sweeps"])
-            used += st["guess_used"]
-            if st["guess_residual"] > 0:
-                rg.append(st["guess_residual"])
-                rw.append(st["warm_residual"])
-            tt += pl.dt
-        e1.record(ext)
-        e1.synchronize()
-        res[name] = {"ms": e0.elapsed_time(e1) / args.steps, "iters": float(np.mean(its)), "used": used,
-                     "sweeps": float(np.mean(sw)), "state": sol.state()[0],
-                     "its": [int(v) for v in its],
-                     "guess_res": float(np.exp(np.mean(np.log(rg)))) if rg else None,
-                     "warm_res": float(np.exp(np.mean(np.log(rw)))) if rw else None}
-    zp = res["fp64"]["state"]
-    rel = lambda a: float(np.abs(a - zp).max() / max(np.abs(zp).max(), 1e-300))
-    err = rel(res["learned"]["state"])
-    status = sl.learned_status()
-    for _, sol in arms:
-        sol.close()
-    lm, mx = res["learned_mixed"], res["mixed"]
-    return {"value": world * 1e3 / res["learned"]["ms"], "ms_per_step": res["learned"]["ms"],
-            "workload": f"diffusion3d_source_{args.grid} (f = 1 + 0.5 sin(2 pi t/T) psi, T = 1000 dt)",
-            "fp64_same_steps": {"value": world * 1e3 / res["fp64"]["ms"], "ms_per_step": res["fp64"]["ms"],
-                                "iterations_per_step": res["fp64"]["iters"]},
-            "speedup_vs_fp64": res["fp64"]["ms"] / res["learned"]["ms"],
-            "iterations_per_step": res["learned"]["iters"],
-            # the guess weakens with the distance from the training window
-            "iterations_first_last_5": [res["learned"]["its"][:5], res["learned"]["its"][-5:]],
-            "fp64_iterations_first_last_5": [res["fp64"]["its"][:5], res["fp64"]["its"][-5:]],
-            "guess_accepted_steps": res["learned"]["used"], "timed_steps": args.steps,
-            "guess_rel_residual_geomean": res["learned"]["guess_res"],
-            "warm_start_rel_residual_geomean": res["learned"]["warm_res"],
-            "train_steps": args.learned_train, "train_seconds": train_s,
-            "train_phase_iterations_per_step": float(np.mean(train_iters)) if train_iters else None,
-            "final_training_loss": status["last_loss"],
-            "rel_err_face_traces_vs_fp64": err,
-            # the same network, its guess followed by the mixed-precision refinement
-            "with_mixed_solve": {
-                "value": world * 1e3 / lm["ms"], "ms_per_step": lm["ms"],
-                "speedup_vs_fp64": res["fp64"]["ms"] / lm["ms"],
-                "inner_fp32_iterations_per_step": lm["iters"], "sweeps_per_step": lm["sweeps"],
-                "guess_accepted_steps": lm["used"], "rel_err_face_traces_vs_fp64": rel(lm["state"]),
-                "mixed_form_same_steps": {"value": world * 1e3 / mx["ms"], "ms_per_step": mx["ms"],
-                                          "speedup_vs_fp64": res["fp64"]["ms"] / mx["ms"],
-                                          "inner_fp32_iterations_per_step": mx["iters"],
-                                          "sweeps_per_step": mx["sweeps"]}}}
+    total = args.learned_train + args.learned_used
+    mk = lambda form: problems.diffusion3d_source(N=args.grid, steps=total, form=form)
+    fp = Arm("fp64", _solver(mk(L.FORM_FP64), dev), dev)
+    mx = Arm("mixed", _solver(mk(L.FORM_MIXED), dev), dev)
+    ln = Arm("learned", _solver(mk(L.FORM_LEARNED), dev), dev)
+    lm = Arm("learned_mixed", _solver(mk(L.FORM_LEARNED), dev), dev)
+    # ablations: the same form with the network never consulted (the gate
+    # chooses between the warm start and the extrapolated base only), and the
+    # network on the linear base 2 Zn - Zn1 (the previous two traces), with
+    # and without the network
+    bo = Arm("extrapolation_only", _solver(mk(L.FORM_LEARNED), dev), dev)
+    l1 = Arm("learned_linear_base", _solver(mk(L.FORM_LEARNED), dev), dev)
+    b1 = Arm("extrapolation_only_linear", _solver(mk(L.FORM_LEARNED), dev), dev)
+    for a, mixed_solve, order in ((ln, False, args.learned_order), (lm, True, args.learned_order), (l1, False, 1)):
+        a.sol.learned_options(train_steps=args.learned_train, train_iters=args.learned_iters, learning_rate=3e-3,
+                              use_during_training=True, mixed_solve=mixed_solve, extrapolation_order=order)
+    bo.sol.learned_options(train_steps=0, extrapolation_order=args.learned_order)
+    b1.sol.learned_options(train_steps=0, extrapolation_order=1)
+    # the FP64 solution to 1e-13 in lockstep (started from the extrapolated
+    # base when that is closer: the initial guess changes its iteration
+    # count, not its solution)
+    exact = Arm("exact", _solver(mk(L.FORM_LEARNED), dev, tol=1e-13), dev)
+    exact.sol.learned_options(train_steps=0, extrapolation_order=3)
+    p = mk(L.FORM_FP64)
+    arms = [fp, mx, ln, lm, bo, l1, b1]
+    lockstep(arms, exact, p.dt, total)
+    nt = args.learned_train
+    out = {"workload": f"diffusion3d_source_{args.grid} (BASELINE config 5: f = 1 + 0.5 sin(2 pi t/T) psi, "
+                       f"T = {total} dt)",
+           "train_steps": nt, "used_steps": args.learned_used, "adam_iterations_per_training_step": args.learned_iters,
+           "extrapolation_order": args.learned_order,
+           "timing": "every step of the protocol from the initial state, training included"}
+    for a in arms:
+        d = {"protocol": arm_summary(a, world, full_errors=False),
+             "training_phase": arm_summary(a, world, 0, nt, full_errors=False),
+             "used_phase": arm_summary(a, world, nt, total, full_errors=False)}
+        for ph in ("training_phase", "used_phase"):
+            for k in list(d[ph]):
+                if k.startswith("rel_err") or k == "steps_over_1e-8":
+                    del d[ph][k]
+        if a in (ln, lm, bo, l1, b1):
+            used = [st for st in a.stats[nt:]]
+            d["used_phase"]["guess_accepted_steps"] = int(sum(st["guess_used"] for st in used))
+            for ph, lo, hi in (("training_phase", 0, nt), ("used_phase", nt, total)):
+                src = [st["guess_source"] for st in a.stats[lo:hi]]
+                d[ph]["initial_guess_steps"] = {"warm_start": src.count(0), "network": src.count(1),
+                                                "extrapolated_base": src.count(2)}
+            rb = [st["base_residual"] for st in used if st["base_residual"] > 0]
+            if rb:
+                d["used_phase"]["base_rel_residual_geomean"] = float(np.exp(np.mean(np.log(rb))))
+            rg = [st["guess_residual"] for st in used if st["guess_residual"] > 0]
+            rw = [st["warm_residual"] for st in used if st["warm_residual"] > 0]
+            if rg:
+                d["used_phase"]["guess_rel_residual_geomean"] = float(np.exp(np.mean(np.log(rg))))
+                d["used_phase"]["warm_start_rel_residual_geomean"] = float(np.exp(np.mean(np.log(rw))))
+            d["used_phase"]["iterations_per_100_steps"] = [
+                float(np.mean([st["iterations"] for st in a.stats[k:k + 100]])) for k in range(nt, total, 100)]
+            if a not in (bo, b1):
+                d["final_training_loss"] = a.sol.learned_status()["last_loss"]
+        out[a.name] = d
+    out["network_gain_over_extrapolation_only"] = {
+        base: {ph: out[net][ph]["value"] / out[ext][ph]["value"] for ph in ("protocol", "used_phase")}
+        for base, net, ext in (("cubic_base", "learned", "extrapolation_only"),
+                               ("linear_base", "learned_linear_base", "extrapolation_only_linear"))}
+    base = out["fp64"]
+    for a in arms[1:]:
+        out[a.name]["speedup_vs_fp64"] = {
+            ph: out[a.name][ph]["value"] / base[ph]["value"] for ph in ("protocol", "training_phase", "used_phase")}
+    out["learned_mixed"]["speedup_vs_mixed"] = {
+        ph: out["learned_mixed"][ph]["value"] / out["mixed"][ph]["value"] for ph in ("protocol", "used_phase")}
+    for a in arms + [exact]:
+        a.close()
+    return out
 
 
 def profile_other_form(args, dev):
@@ -459,22 +655,29 @@ def profile_other_form(args, dev):
     s.close()
 
 
-def cpu_baseline(p, steps):
+def cpu_baseline(p, steps, warmup=1, what=None):
+    """The CPU oracle (the restatement of the reference's algorithm, C +
+    OpenMP on the threads this process may use) over `steps` time steps after
+    `warmup` untimed ones: a bounded sample of the workload."""
     from oracle.oracle import OracleModel, load
 
     lib = load()
-    threads = os.cpu_count() or 1
+    threads = allowed_cpus()
     lib.orc_set_threads(threads)
     m = OracleModel.from_problem(p)
     t = 0.0
+    for _ in range(warmup):
+        m.step(t, p.dt, p.tol)
+        t += p.dt
     t0 = time.perf_counter()
     for _ in range(steps):
         m.step(t, p.dt, p.tol)
         t += p.dt
     el = time.perf_counter() - t0
+    what = what or f"{steps} time steps of the same workload after {warmup} warm-up step(s)"
     return {"value": steps / el, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"the first {steps} time steps of the same {p.grid_N}^3 workload (CPU restatement of the "
-                      "reference algorithm, OpenMP, FP64, same tolerance)"}
+            "sample": f"{what} (CPU restatement of the reference algorithm, C + OpenMP, -O3 as the reference's "
+                      "release build, FP64, same tolerance)"}
 
 
 def main():
@@ -535,7 +738,6 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
-    zf64, zk64 = s.state()
     iters = (it1 - it0) / args.steps
     if args.profile_run:
         if rank == 0:
@@ -546,90 +748,29 @@ def main():
     value = replicas_value(args.steps, world, el_ms)
     bytes_step = step_bytes(n, nf, S, C, F, V, W, iters)
 
-    # dominant kernel: the FP64 SpMV fused with its dot product
+    # the iteration kernels, each timed alone; the roofline names the one with the largest share
     hbm_peak, peak_kind = measured_peaks()
-    spmv = s.time_kernel(L.KERNEL_SPMV_FP64, reps=50)
-    achieved = spmv["bytes"] / (spmv["ms"] * 1e-3) / 1e9
+    iteration, iter_kernel_ms = iteration_table(s, L, hbm_peak)
+    top = max(iteration, key=lambda k: iteration[k]["share_of_iteration"])
     kernels = kernel_table(s, L, hbm_peak)
-    kernels["spmv_fp64"] = {"ms": spmv["ms"], "gbs": achieved, "hbm_frac": achieved / hbm_peak,
-                            "fp64_tflops": spmv["flops"] / (spmv["ms"] * 1e-3) / 1e12}
-    traffic = None
-    tfile = REPO / "profiles" / "spmv_fp64_diffusion3d.txt"
-    if tfile.exists() and args.grid == 64:  # the ncu capture is of the 64^3 launch
-        for line in tfile.read_text().splitlines():
-            if line.startswith("dram_bytes_per_launch_full_size:"):
-                try:
-                    traffic = float(line.split(":", 1)[1].split()[0])
-                except ValueError:
-                    traffic = None
+    traffic, traffic_src = ncu_traffic(top, args.grid)
     gpu_launches = kl1 - kl0
 
     forms = {}
     if not args.no_mixed:
-        pm = problems.diffusion3d(N=args.grid, form=L.FORM_MIXED)
-        pm.config.device = dev
-        sm = problems.make_solver(pm, check_every=8)
-        extm = torch.cuda.ExternalStream(sm.stream(), device=dev)
-        tm = 0.0
-        for _ in range(args.warmup):
-            sm.step(tm, pm.dt)
-            tm += pm.dt
-        itm0, _, _ = sm.totals()
-        a0 = torch.cuda.Event(enable_timing=True)
-        a1 = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        a0.record(extm)
-        sweeps = []
-        for _ in range(args.steps):
-            sweeps.append(sm.step(tm, pm.dt)["sweeps"])
-            tm += pm.dt
-        a1.record(extm)
-        a1.synchronize()
-        mel = a0.elapsed_time(a1)
-        itm1, _, _ = sm.totals()
-        zfm, zkm = sm.state()
-        err_f = float(np.abs(zfm - zf64).max() / max(np.abs(zf64).max(), 1e-300))
-        err_k = float(np.abs(zkm - zk64).max() / max(np.abs(zk64).max(), 1e-300))
-        sp32 = sm.time_kernel(L.KERNEL_SPMV_FP32, reps=50)
-        # Single-step accuracy from one common state: the mixed and the FP64
-        # form at the same tolerance, each against the FP64 form solved to
-        # 1e-13.  After many steps the two forms' traces differ by the
-        # tolerance's own error (the "vs_fp64" figures above); this isolates
-        # the precision of the mixed solve from that.
-        pr = problems.diffusion3d(N=args.grid)
-        pr.config.device = dev
-        sr = problems.make_solver(pr, check_every=8)
-        outs = {}
-        for name, tol in (("ref", 1e-13), ("fp64", pr.tol)):
-            sr.setInitialCondition(zkm, zfm)
-            sr.setup(tol=tol, max_iter=20000, check_every=8)
-            sr.step(tm, pr.dt)
-            outs[name] = sr.state()
-        sr.close()
-        sm.step(tm, pm.dt)
-        outs["mixed"] = sm.state()
-        zr, kr = outs["ref"]
-        rel = lambda a, b: float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
-        forms["mixed"] = {"value": world * args.steps / (mel / 1e3), "ms_per_step": mel / args.steps,
-                          "speedup_vs_fp64": (args.steps / mel) / (args.steps / el_ms),
-                          "inner_iterations_per_step": (itm1 - itm0) / args.steps,
-                          "sweeps_per_step": statistics.mean(sweeps),
-                          "rel_err_face_traces_vs_fp64": err_f, "rel_err_cell_values_vs_fp64": err_k,
-                          "one_step_rel_err_vs_fp64_at_1e-13": {
-                              "mixed": [rel(outs["mixed"][0], zr), rel(outs["mixed"][1], kr)],
-                              "fp64_at_same_tol": [rel(outs["fp64"][0], zr), rel(outs["fp64"][1], kr)]},
-                          "spmv_fp32_gbs": sp32["bytes"] / (sp32["ms"] * 1e-3) / 1e9}
-        if args.mixed_error_steps > 0:
-            forms["mixed"]["per_step_rel_err_vs_fp64"] = mixed_lockstep_errors(args, dev, zkm, zfm, tm)
-        sm.close()
-
-    if not args.no_learned:
-        forms["learned"] = learned_leg(args, dev, world)
+        forms["mixed"] = mixed_leg(args, dev, world, el_ms)
     if not args.no_gmres:
         forms["fp64_gmres"] = gmres_leg(args, dev, world)
     other_cells = None
     if not args.no_box:
         other_cells = {"cuboids": box_leg(args, dev, world)}
+    configs = {}
+    wanted = [c for c in args.configs.split(",") if c and c != "none"]
+    for name, leg in (("heat2d", heat2d_leg), ("adr2d", adr2d_leg), ("mixed128", mixed128_leg)):
+        if name in wanted:
+            configs[name] = leg(args, dev, world)
+    if not args.no_learned:
+        forms["learned_protocol"] = learned_protocol_leg(args, dev, world)
 
     e2e = None
     if not args.no_e2e:
@@ -662,36 +803,59 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(problems.diffusion3d(N=args.grid), args.cpu_steps)
+        cpu = cpu_baseline(problems.diffusion3d(N=args.grid), args.cpu_steps, warmup=1,
+                           what=f"{args.cpu_steps} time steps of the same {args.grid}^3 workload after 1 warm-up step")
 
     s.close()
     if rank != 0:
         return
+    tk = iteration[top]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64",
         "data": f"synthetic: seeded jittered {args.grid}^3 cube grid split into 6 tetrahedra, D = exp(Gaussian field)",
-        "config": {"workload": f"diffusion3d_{args.grid}", "cells": C, "faces": F, "rows": rows,
-                   "tol": p.tol, "dt": p.dt,
-                   "form": "fp64", "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2": f"working set larger than L2 (ELL values+columns {rows * W * 12 / 1e6:.0f} MB, cell records "
-                         f"{8 * (n * nf + 1) * n * nf * C / 1e6:.0f} MB)"},
+        "form": "fp64", "parallelism": "replicas" if world > 1 else "single GPU",
+        "config": workload_config(args.grid, C, F, rows, p.tol, p.dt, n, nf),
         "face_dof_per_s": value * F * n, "iterations_per_step": iters,
         "hbm_gbs_step": bytes_step / (ms_step * 1e-3) / 1e9,
         "hbm_frac_step": bytes_step / (ms_step * 1e-3) / 1e9 / hbm_peak,
-        "roofline": {"bound": "hbm", "kernel": "k_spmv_dot<double> (BiCGStab SpMV + dot)", "achieved": achieved,
-                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak, "traffic": traffic,
-                     "peak_kind": peak_kind, "bytes_per_launch": spmv["bytes"], "ms_per_launch": spmv["ms"]},
+        "roofline": {"bound": "hbm", "kernel": tk["kernel"], "achieved": tk["gbs"], "peak": hbm_peak, "unit": "GB/s",
+                     "frac": tk["hbm_frac"], "traffic": traffic, "traffic_source": traffic_src,
+                     "peak_kind": peak_kind, "bytes_per_launch": tk["bytes"], "ms_per_launch": tk["ms"],
+                     "share_of_iteration": tk["share_of_iteration"],
+                     "selection": "largest share of the FP64 BiCGStab iteration's kernel time (each kernel timed "
+                                  "alone with CUDA events on the library's stream)"},
+        "iteration_kernels": iteration,
+        "iteration_kernel_ms": iter_kernel_ms,
+        "iteration_ms_in_step": ms_step / max(iters, 1),
         "kernels": kernels,
         "forms": forms,
         "other_cells": other_cells,
+        "other_configs": configs,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": gpu_launches,
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)
+
+
+def ncu_traffic(kernel_name, grid):
+    """DRAM bytes per launch of a kernel from the committed ncu summary of the
+    iteration kernels (`traffic <name> <bytes> <commit>` lines; captured on
+    the 64^3 workload), with the file and commit it came from."""
+    f = REPO / "profiles" / "iteration_kernels_fp64_diffusion3d64.txt"
+    if grid != 64 or not f.exists():
+        return None, None
+    for line in f.read_text().splitlines():
+        parts = line.split()
+        if len(parts) >= 4 and parts[0] == "traffic" and parts[1] == kernel_name:
+            try:
+                return float(parts[2]), f"profiles/{f.name}, ncu capture of commit {parts[3]}"
+            except ValueError:
+                return None, None
+    return None, None
 
 
 if __name__ == "__main__":

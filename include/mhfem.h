@@ -139,6 +139,9 @@ typedef struct {
     double  ms_pre, ms_assemble, ms_solve, ms_post;   /* device time per phase */
     double  ms_guess;         /* learned form: device time of the guess (features, network, gate
                                  residuals), included in ms_solve; 0 for the other forms */
+    double  base_residual;    /* learned form: relative residual of the extrapolated base (-1: none) */
+    int32_t guess_source;     /* learned form: the initial guess the solve started from:
+                                 0 the warm start, 1 the network's guess, 2 the extrapolated base */
 } mhfem_step_stats;
 
 /* ---- lifecycle ---------------------------------------------------------- */
@@ -198,14 +201,31 @@ mhfem_status mhfem_set_coeff(mhfem_t h, int32_t which, const double* data, int64
  * on the calling thread at a fixed point of the step with the handle's CUDA
  * stream, and updates the coefficient arrays on the device in place
  * (mhfem_coeff_device), reading the state (mhfem_array_device), with work
- * ordered on that stream.  The cell kernel fuses the mass-matrix update with
- * everything after it, so a vector coefficient whose projection depends on
- * b sees the previous step's b.  Writes through these pointers bypass the
- * host copies that mhfem_set_coeff keeps: the learned form's static
- * features keep the values last passed to mhfem_set_coeff. */
+ * ordered on that stream.
+ *  - MHFEM_HOOK_PRE_ITERATE is updateNonLinearTerms: the scalar
+ *    coefficients (N, m, D, r, f) of this step, from the current state.
+ *  - MHFEM_HOOK_VECTOR_COEFFICIENTS is updateVectorCoefficients: it runs
+ *    after this step's b update (MHFEM_ARRAY_B holds the new b) and before
+ *    upwinding, so the RT0 projections of u, w and a may read b, as in the
+ *    reference.  With it registered the step launches the b update as a
+ *    kernel of its own before the hook and the fused cell kernel after it;
+ *    without it the cell kernel forms b and everything after it in one
+ *    pass.  The cell kernel forms b again from D, so D changes belong in
+ *    the PRE_ITERATE hook.
+ *  - getBoundaryMobility (Solver.hpp:696) is the array MHFEM_COEF_M_BND
+ *    (i*F+E), read on the inflow boundary faces by the mobility upwinding of
+ *    the same step; a model with a time- or state-dependent boundary mobility
+ *    rewrites it from either hook above (both run after the velocities v_iKe
+ *    of the previous step's reconstruction and before the inflow test).
+ *  - MHFEM_HOOK_POST_ITERATE runs after the reconstruction (BaseModel's
+ *    postIterate).
+ * Writes through these pointers bypass the host copies that mhfem_set_coeff
+ * keeps: the learned form's static features keep the values last passed to
+ * mhfem_set_coeff. */
 typedef void (*mhfem_hook)(void* user, double t, double tau, void* stream);
-#define MHFEM_HOOK_PRE_ITERATE  0  /* start of mhfem_pre_iterate, before upwinding and the cell kernel */
-#define MHFEM_HOOK_POST_ITERATE 1  /* end of mhfem_post_iterate, after the reconstruction */
+#define MHFEM_HOOK_PRE_ITERATE          0  /* start of mhfem_pre_iterate, before the b update */
+#define MHFEM_HOOK_POST_ITERATE         1  /* end of mhfem_post_iterate, after the reconstruction */
+#define MHFEM_HOOK_VECTOR_COEFFICIENTS  2  /* after the b update, before upwinding (Solver.hpp:641-652) */
 /* fn == NULL removes the hook. */
 mhfem_status mhfem_set_hook(mhfem_t h, int32_t point, mhfem_hook fn, void* user);
 /* The device array of a coefficient as currently stored (count 1: uniform,
@@ -278,6 +298,13 @@ mhfem_status mhfem_get_array(mhfem_t h, int32_t which, double* out, int64_t coun
 mhfem_status mhfem_get_system(mhfem_t h, int64_t* rowptr, int32_t* cols, double* vals,
                               double* rhs);
 
+/* The FP32 copy of the matrix values that the mixed form (and the learned
+ * form's mixed solve) assembles beside the FP64 one: nnz entries in the CSR
+ * order of mhfem_get_system, the unit diagonal as 1.0f; each value is the
+ * FP64 value rounded to nearest (ties to even).  No counterpart in the
+ * reference, whose matrix is FP64 only. */
+mhfem_status mhfem_get_system32(mhfem_t h, float* vals32);
+
 /* Cumulative counters as in Solver::writeEpilog (Solver.hpp:1326-1391),
  * plus the number of kernels this library launched on the handle. */
 mhfem_status mhfem_get_totals(mhfem_t h, int64_t* iterations, int64_t* time_steps,
@@ -295,11 +322,17 @@ mhfem_status mhfem_get_stream(mhfem_t h, void** stream);
 #define MHFEM_KERNEL_SPMV_FP64    2   /* BiCGStab SpMV fused with a dot product, FP64 */
 #define MHFEM_KERNEL_SPMV_FP32    3   /* the same in FP32 (mixed form) */
 #define MHFEM_KERNEL_RECONSTRUCT  4   /* Z_iK (and v_iKe) reconstruction */
+#define MHFEM_KERNEL_SPMV2_FP64       5   /* BiCGStab second SpMV fused with (t, s), (t, t), FP64 */
+#define MHFEM_KERNEL_UPDATE_S_FP64    6   /* BiCGStab s = r - alpha v, FP64 */
+#define MHFEM_KERNEL_UPDATE_XR_FP64   7   /* BiCGStab x += alpha p + omega s, r = s - omega t, (rh, r), FP64 */
+#define MHFEM_KERNEL_UPDATE_P_FP64    8   /* BiCGStab p = r + beta (p - omega v), FP64 */
 
 /* Times `reps` back-to-back launches of one kernel on the current system
  * with CUDA events on the handle's stream (after a step has run) and returns
  * the mean duration, the algorithmic bytes one launch must move (each array
- * counted once at its size) and its FP64 (or FP32) operation count. */
+ * counted once at its size) and its FP64 (or FP32) operation count.  The
+ * Krylov kernels run on the solver's Krylov work vectors (overwritten; the
+ * next solve initializes them again); the state Z_iF, Z_iK is left as it is. */
 mhfem_status mhfem_time_kernel(mhfem_t h, int32_t kernel, int32_t reps, double* ms_per_launch,
                                double* bytes_per_launch, double* flops_per_launch);
 
@@ -308,11 +341,13 @@ mhfem_status mhfem_time_kernel(mhfem_t h, int32_t kernel, int32_t reps, double* 
  * adjacency graph (3 layers, hidden width 64, BF16 weights, FP32
  * accumulation on the tensor cores) predicts the initial guess of each
  * solve (FP64 BiCGStab, or with `mixed_solve` the mixed-precision
- * refinement).  The guess is used only when its relative residual is below
- * the previous-step warm start's; the solve always runs to the same FP64
- * tolerance.  The network is trained online on the first `train_steps`
- * steps, or takes parameters from mhfem_learned_set_params.  Only n_eq = 1
- * and simplex cells are supported. */
+ * refinement) as a correction to the polynomial extrapolation in time of the
+ * last traces (order `extrapolation_order`, as far as the history reaches).
+ * Of the previous-step warm start, the extrapolated base and the network's
+ * guess, the one with the lowest relative residual starts the solve; the
+ * solve always runs to the same FP64 tolerance.  The network is trained
+ * online on the first `train_steps` steps, or takes parameters from
+ * mhfem_learned_set_params.  Only n_eq = 1 and simplex cells are supported. */
 typedef struct {
     int32_t train_steps;          /* online training steps (default 200)            */
     int32_t train_iters;          /* Adam iterations per training step (default 2)  */
@@ -327,6 +362,9 @@ typedef struct {
                                      BiCGStab, FP64 residuals, the same FP64
                                      tolerance) instead of FP64 BiCGStab; the handle
                                      then also keeps the FP32 copy of the matrix      */
+    int32_t extrapolation_order;  /* 0 to 3: the base the network corrects, the polynomial
+                                     extrapolation of the last order + 1 traces in time
+                                     (0: the warm start itself; 1: 2 Zn - Zn1; 3: cubic) */
 } mhfem_learned_opts;
 
 #define MHFEM_LEARNED_FEATURES 16
@@ -354,18 +392,30 @@ mhfem_status mhfem_learned_status(mhfem_t h, int32_t* trained_steps, double* las
  * (ELL of the off-diagonal part, [width][rows], padding column = own row).
  * cols, vals, rhs and x are DEVICE pointers; x holds the initial guess and
  * receives the solution; stream is a cudaStream_t (NULL: default stream).
+ * Every column index must lie in [0, rows): one pass checks them before the
+ * solve and a system with any other index is refused with
+ * MHFEM_ERR_INVALID_ARGUMENT (nothing else runs).
  * All work vectors live in one static device array of fixed size (about
- * 12.8 MB, held by every GPU that loads the library until the process
- * exits), so systems with more than MHFEM_NOALLOC_MAX_ROWS rows are rejected
- * with MHFEM_ERR_INVALID_ARGUMENT.  The first call on a device looks the
- * array's address up (cudaGetSymbolAddress) and should come before any
- * stream capture.  Every call shares the array: calls that overlap on the
- * GPU (other streams, other threads) race and must be serialized by the
- * caller.  Returns MHFEM_OK, MHFEM_ERR_NOT_CONVERGED, MHFEM_ERR_BREAKDOWN or
- * MHFEM_ERR_NOT_FINITE like mhfem_solve. */
+ * 12.8 MB), so systems with more than MHFEM_NOALLOC_MAX_ROWS rows are
+ * rejected with MHFEM_ERR_INVALID_ARGUMENT.  Under CUDA's default lazy module
+ * loading that array is committed on a device at the FIRST call there (which
+ * looks its address up with cudaGetSymbolAddress and may synchronize the
+ * device), not when the library is loaded, and it stays until the process
+ * exits: a pool-allocator user makes one warm-up call during its own
+ * initialization, before any stream capture.  Every call shares the array:
+ * calls that overlap on the GPU (other streams, other threads) race and must
+ * be serialized by the caller.
+ * The call blocks until the solve ends: at most max_iter iterations, and at
+ * most timeout_s seconds of wall-clock time when timeout_s > 0 (checked every
+ * 8 iterations, after the queued work has drained; then MHFEM_ERR_TIMEOUT).
+ * Returns MHFEM_OK, MHFEM_ERR_NOT_CONVERGED, MHFEM_ERR_BREAKDOWN or
+ * MHFEM_ERR_NOT_FINITE like mhfem_solve.  *residual is the relative residual
+ * ||b - Ax|| / ||b|| of the last iteration that formed it (every 8th
+ * iteration and the converged one): on MHFEM_ERR_NOT_CONVERGED and
+ * MHFEM_ERR_TIMEOUT it can be up to 7 iterations older than x. */
 #define MHFEM_NOALLOC_MAX_ROWS 262144
 mhfem_status mhfem_bicgstab_noalloc(const int32_t* cols, const double* vals, int32_t width, int64_t rows,
-                                    const double* rhs, double* x, double tol, int32_t max_iter,
+                                    const double* rhs, double* x, double tol, int32_t max_iter, double timeout_s,
                                     int32_t* iterations, double* residual, void* stream);
 
 #ifdef __cplusplus

@@ -159,6 +159,10 @@ class OracleModel:
         self.f_base = np.ascontiguousarray(np.atleast_1d(np.asarray(coeffs.get("f", 0.0), np.float64)).ravel())
         self.psi = coeffs.get("psi")
         self.source = None
+        # a model's updateVectorCoefficients: called as vector_hook(model, t, tau)
+        # after the b update and before upwinding (Solver.hpp:641-652); it may
+        # change coeff_arrays in place (w, a, u, m_bnd)
+        self.vector_hook = None
         # pattern
         rows = n * F
         rowlen = np.empty(rows, np.int32)
@@ -198,6 +202,8 @@ class OracleModel:
         self._update_source(t)
         P = ct.byref(self.P)
         self.lib.orc_update_b(P)
+        if self.vector_hook is not None:
+            self.vector_hook(self, t, tau)
         self.lib.orc_upwind(P, t, tau)
         self.lib.orc_update_R(P, tau)
         self.lib.orc_update_Q(P, tau)

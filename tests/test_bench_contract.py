@@ -2,6 +2,7 @@
 OpenMP on the host's cores) on a small grid prints the keys the contract
 asks for."""
 import json
+import os
 import subprocess
 import sys
 from pathlib import Path
@@ -22,6 +23,8 @@ def test_reference_arm_json_line():
     assert d["impl"] == "reference" and d["value"] > 0 and d["steps"] == 2 and d["warmup"] == 1
     assert d["higher_is_better"] is True and d["dtype"] == "f64"
     assert d["config"]["workload"] == "diffusion3d_8"
-    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    # the same config keys as the GPU arm's line (bench.workload_config), the threads this process may use
+    assert set(d["config"]) == {"workload", "cells", "faces", "rows", "tol", "dt", "l2"}
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] == len(os.sched_getaffinity(0))
     assert "8^3" in d["cpu_baseline"]["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}

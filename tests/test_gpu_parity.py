@@ -240,6 +240,22 @@ def test_mixed_128_cube():
     sf.close()
 
 
+def test_mixed_fp32_matrix_is_the_rounded_fp64_matrix():
+    """The mixed form's FP32 copy of the assembled values (converted on the
+    integer pipes) equals the FP64 values rounded to nearest even, bit for
+    bit, over the 32^3 tetrahedral system (1.3M values) and the two-component
+    triangle system."""
+    for p in (problems.diffusion3d(N=32, steps=1, form=L.FORM_MIXED), problems.adr2d(N=32, steps=1, form=L.FORM_MIXED)):
+        s = problems.make_solver(p)
+        s.preIterate(0.0, p.dt)
+        s.assembleLinearSystem(0.0, p.dt)
+        _, _, vals, _ = s.system()
+        v32 = s.system32()
+        assert v32.dtype == np.float32 and v32.size == vals.size
+        assert np.array_equal(v32.view(np.uint32), vals.astype(np.float32).view(np.uint32)), p.name
+        s.close()
+
+
 def test_mixed_precision_matches_fp64_oracle():
     """FP32 inner BiCGStab + FP64 refinement to 1e-10: error vs the FP64 oracle."""
     p = problems.diffusion3d(N=12, steps=3, form=L.FORM_MIXED)
@@ -339,19 +355,20 @@ def test_gmres_step_parity(name, variant):
 
 def test_gmres_heat2d_full_size():
     """The 128^2 heat-equation workload with the reference example's solver
-    keys (GMRES, CGS, restart 30) at tol 1e-12, 3 steps against the oracle."""
+    keys (GMRES, CGS, restart 30), 3 steps against the oracle at the 1e-10
+    bar; both solves run to 1e-13 like every other parity test."""
     p = problems.heat2d(N=128, steps=3)
     s, m = _pair(p, check_every=8)
-    s.setup(tol=1e-12, max_iter=20000, check_every=8, linear_solver="gmres", gmres_restart=30, gmres_variant="cgs")
+    s.setup(tol=1e-13, max_iter=20000, check_every=8, linear_solver="gmres", gmres_restart=30, gmres_variant="cgs")
     t = 0.0
     for _ in range(p.steps):
         st = s.step(t, p.dt)
         m.step(t, p.dt, 1e-13)
-        assert st["residual"] < 1e-12
+        assert st["residual"] < 1e-13
         t += p.dt
     zf, zk = s.state()
-    assert rel_err(zf, m.Z_iF) < 1e-9
-    assert rel_err(zk, m.Z_iK) < 1e-9
+    assert rel_err(zf, m.Z_iF) < TOL_STATE
+    assert rel_err(zk, m.Z_iK) < TOL_STATE
     s.close()
 
 

@@ -154,3 +154,22 @@ def test_header_compiles_as_strict_c_and_cpp(tmp_path, lang, std):
                        capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr
     assert subprocess.run([str(out)], timeout=60).returncode == 0
+
+
+def test_integer_pipe_conversions_match_ieee_casts(tmp_path):
+    """csrc/fp_convert.h (the FP64 -> FP32 round-to-nearest-even and exact
+    FP32 -> FP64 conversions the mixed form runs on the integer pipes) gives
+    bit for bit what the compiler's IEEE casts give, over millions of inputs
+    including every tie at every binary32 exponent and the range edges."""
+    import shutil
+    import subprocess
+
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not available")
+    out = tmp_path / "fp_convert_check"
+    r = subprocess.run([cxx, "-std=c++17", "-O2", "-I", str(REPO / "tnl-mhfem_gb300" / "csrc"),
+                        str(REPO / "tests" / "fp_convert_check.cpp"), "-o", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout[-2000:]

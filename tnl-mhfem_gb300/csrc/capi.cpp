@@ -450,6 +450,7 @@ mhfem_status mhfem_set_state(mhfem_t h, const double* Z_iK, const double* Z_iF)
     }
     if (h->v_iKe) CK(cudaMemsetAsync(h->v_iKe, 0, sizeof(double) * h->n * h->nf * h->topo.C, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    learned_reset_history(h);  // the learned form's extrapolation restarts from this state
     h->has_state = true;
     return MHFEM_OK;
 }
@@ -765,6 +766,16 @@ mhfem_status mhfem_pre_iterate(mhfem_t h, double t, double tau)
     if ((st = run_hook(h, MHFEM_HOOK_PRE_ITERATE, t, tau)) != MHFEM_OK) return st;
     DevProblem P = make_problem(h);
     cudaEventRecord(h->ev[0], h->stream);
+    if (h->hooks[MHFEM_HOOK_VECTOR_COEFFICIENTS].fn) {
+        // Solver.hpp:627-652: this step's b first, then the model's
+        // updateVectorCoefficients (its RT0 projections of u, w, a read b),
+        // then upwinding and the rest of the cell work.  Without the hook the
+        // fused cell kernel forms b and everything after it in one pass.
+        h->launches += launch_update_b(P, h->stream);
+        CK(cudaGetLastError());
+        if ((st = run_hook(h, MHFEM_HOOK_VECTOR_COEFFICIENTS, t, tau)) != MHFEM_OK) return st;
+        P = make_problem(h);  // the hook may have asked for a or u (explicit advection terms on)
+    }
     h->launches += launch_upwind(P, h->stream);
     h->launches += launch_cell_local(P, tau, h->stream);
     cudaEventRecord(h->ev[1], h->stream);
@@ -807,6 +818,8 @@ mhfem_status mhfem_solve(mhfem_t h, mhfem_step_stats* stats)
         stats->guess_residual = -1;
         stats->warm_residual = -1;
         stats->ms_guess = 0;
+        stats->base_residual = -1;
+        stats->guess_source = 0;
     }
     if (h->desc.form == MHFEM_FORM_MIXED) st = run_mixed(h, &iters, &sweeps, &res);
     else if (h->desc.form == MHFEM_FORM_LEARNED) st = learned_solve(h, &iters, &sweeps, &res, stats);
@@ -836,7 +849,7 @@ mhfem_status mhfem_post_iterate(mhfem_t h, double t, double tau)
 mhfem_status mhfem_set_hook(mhfem_t h, int32_t point, mhfem_hook fn, void* user)
 {
     if (!h) return MHFEM_ERR_INVALID_ARGUMENT;
-    if (point != MHFEM_HOOK_PRE_ITERATE && point != MHFEM_HOOK_POST_ITERATE)
+    if (point != MHFEM_HOOK_PRE_ITERATE && point != MHFEM_HOOK_POST_ITERATE && point != MHFEM_HOOK_VECTOR_COEFFICIENTS)
         return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "unknown hook point %d", point);
     h->hooks[point].fn = fn;
     h->hooks[point].user = user;
@@ -947,6 +960,34 @@ mhfem_status mhfem_get_system(mhfem_t h, int64_t* rowptr, int32_t* cols, double*
     return MHFEM_OK;
 }
 
+mhfem_status mhfem_get_system32(mhfem_t h, float* vals32)
+{
+    mhfem_status st = require_ready(h);
+    if (st) return st;
+    if (!vals32) return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "null output");
+    if ((st = ensure_pattern(h)) != MHFEM_OK) return st;
+    if (!h->fp32_copy || !h->A.vals32)
+        return fail(h, MHFEM_ERR_STATE, "no FP32 copy of the matrix (mixed form or the learned form's mixed solve)");
+    cudaSetDevice(h->desc.device);
+    const int64_t rows = h->pat.rows;
+    const int W = h->pat.W;
+    std::vector<float> ev((size_t)W * rows);
+    CK(cudaMemcpyAsync(ev.data(), h->A.vals32, sizeof(float) * W * rows, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    int64_t pos = 0;
+    for (int64_t r = 0; r < rows; ++r) {
+        const int len = h->pat.row_len[r];
+        int k = 0;
+        bool diag_done = false;
+        for (int q = 0; q < len; ++q) {
+            const bool take_diag = !diag_done && (k >= len - 1 || h->pat.ell_cols[(size_t)k * rows + r] > r);
+            if (take_diag) { vals32[pos++] = 1.0f; diag_done = true; }
+            else vals32[pos++] = ev[(size_t)(k++) * rows + r];
+        }
+    }
+    return MHFEM_OK;
+}
+
 mhfem_status mhfem_get_totals(mhfem_t h, int64_t* iterations, int64_t* time_steps, int64_t* kernel_launches)
 {
     if (!h) return MHFEM_ERR_INVALID_ARGUMENT;
@@ -989,6 +1030,12 @@ mhfem_status mhfem_time_kernel(mhfem_t h, int32_t kernel, int32_t reps, double* 
             FL = R * (W + 3);
             break;
         case MHFEM_KERNEL_SPMV_FP64: B = R * (12 * W + 24); FL = 2 * R * (W + 1); break;
+        // the other FP64 BiCGStab iteration kernels: ELL words, s, t (second SpMV);
+        // r, v, s (s update); x, p, s, t, rh read and x, r written; p, r, v, p
+        case MHFEM_KERNEL_SPMV2_FP64: B = R * (12 * W + 16); FL = 2 * R * (W + 2); break;
+        case MHFEM_KERNEL_UPDATE_S_FP64: B = R * 24; FL = 2 * R; break;
+        case MHFEM_KERNEL_UPDATE_XR_FP64: B = R * 56; FL = 8 * R; break;
+        case MHFEM_KERNEL_UPDATE_P_FP64: B = R * 32; FL = 4 * R; break;
         case MHFEM_KERNEL_SPMV_FP32:
             if (!h->fp32_copy) return fail(h, MHFEM_ERR_STATE, "FP32 SpMV needs the FP32 matrix (mixed form or mixed learned solve)");
             B = R * (8 * W + 12); FL = 2 * R * (W + 1); break;
@@ -998,11 +1045,27 @@ mhfem_status mhfem_time_kernel(mhfem_t h, int32_t kernel, int32_t reps, double* 
             break;
         default: return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "unknown kernel %d", kernel);
     }
-    if (kernel == MHFEM_KERNEL_SPMV_FP64 || kernel == MHFEM_KERNEL_SPMV_FP32) {
-        // make the Krylov kernels run (clear "done"); the state is re-initialized by the next solve
+    const int fp64_iter = kernel == MHFEM_KERNEL_SPMV_FP64 ? 0 : kernel == MHFEM_KERNEL_SPMV2_FP64 ? 1
+                        : kernel == MHFEM_KERNEL_UPDATE_S_FP64 ? 2 : kernel == MHFEM_KERNEL_UPDATE_XR_FP64 ? 3
+                        : kernel == MHFEM_KERNEL_UPDATE_P_FP64 ? 4 : -1;
+    if (fp64_iter >= 0 || kernel == MHFEM_KERNEL_SPMV_FP32) {
+        // Make the Krylov kernels run: scalars that keep every launch going
+        // (not done, no half step, no restart, finite non-zero alpha, omega,
+        // beta, no iteration cap).  The FP64 vectors start as copies of the
+        // current face traces, so the reductions see finite non-zero values.
+        // The Krylov vectors are scratch between solves (the next solve
+        // initializes them); Z_iF is only read.
         KrylovScalars z{};
         z.rho = 1.0;
-        CK(cudaMemcpyAsync(kernel == MHFEM_KERNEL_SPMV_FP64 ? h->W.sc : h->W.sc32, &z, sizeof(z),
+        z.alpha = z.omega = z.beta = 0.5;
+        z.bnorm = z.rr = z.rhnorm = 1.0;
+        z.max_iter = 0x7fffffff;
+        if (fp64_iter >= 0) {
+            const size_t bytes = sizeof(double) * (size_t)R;
+            for (double* v : {h->W.r, h->W.rh, h->W.p, h->W.v, h->W.s, h->W.t})
+                CK(cudaMemcpyAsync(v, h->Z_iF, bytes, cudaMemcpyDeviceToDevice, h->stream));
+        }
+        CK(cudaMemcpyAsync(kernel == MHFEM_KERNEL_SPMV_FP32 ? h->W.sc32 : h->W.sc, &z, sizeof(z),
                            cudaMemcpyHostToDevice, h->stream));
     }
     auto launch = [&]() {
@@ -1010,7 +1073,9 @@ mhfem_status mhfem_time_kernel(mhfem_t h, int32_t kernel, int32_t reps, double* 
             case MHFEM_KERNEL_CELL_LOCAL: launch_cell_local(P, h->cur_tau > 0 ? h->cur_tau : 1.0, h->stream); break;
             case MHFEM_KERNEL_ASSEMBLE:
                 launch_assemble(P, h->amap, h->A, h->rhs, h->fp32_copy, h->stream); break;
-            case MHFEM_KERNEL_SPMV_FP64: krylov_spmv_dot_once(h->A, h->W, false, h->stream); break;
+            case MHFEM_KERNEL_SPMV_FP64: case MHFEM_KERNEL_SPMV2_FP64: case MHFEM_KERNEL_UPDATE_S_FP64:
+            case MHFEM_KERNEL_UPDATE_XR_FP64: case MHFEM_KERNEL_UPDATE_P_FP64:
+                krylov_fp64_kernel_once(h->A, h->W, fp64_iter, h->stream); break;
             case MHFEM_KERNEL_SPMV_FP32: krylov_spmv_dot_once(h->A, h->W, true, h->stream); break;
             case MHFEM_KERNEL_RECONSTRUCT: launch_reconstruct(P, h->stream); break;
         }

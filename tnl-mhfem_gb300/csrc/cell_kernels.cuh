@@ -313,20 +313,15 @@ __device__ __forceinline__ void lu_inverse(double (&A)[NF][NF], double scale, do
 
 enum { MODE_NO_ADV = 0, MODE_ADV = 1, MODE_CELL_DIRICHLET = 2, MODE_SKIP = 3 };
 
-template <int CT, int NE>
-__global__ void __launch_bounds__(128) k_cell_local(const DevProblem P, const double rtau, const double src_scale)
+// The inverse of the RT0 mass matrix of cell K without D (Binv), its row
+// sums (b_ijKe without D), the cell measure and, for boxes, the value of
+// each face orientation (MassMatrix::update, MassMatrix.h:511-1050 and
+// 152-508).
+template <int CT>
+__device__ __forceinline__ void cell_mass_inverse(const DevProblem& P, int64_t K, double& meas, double (&sv)[3],
+                                                  double (&Binv)[ct_nf(CT)][ct_nf(CT)], double (&Brow)[ct_nf(CT)])
 {
     constexpr int NF = ct_nf(CT);
-    constexpr int S = ct_S(CT);
-    const int64_t K = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (K >= P.C) return;
-    const int64_t C = P.C;
-
-    // inverse of the RT0 mass matrix (without D) and its row sums (b_ijKe without D)
-    double meas;
-    double Binv[NF][NF];
-    double Brow[NF];
-    double sv[3];  // box cells: the value of each face orientation
     if constexpr (ct_box(CT)) {
         box_inverse<CT>(P, K, meas, sv, Binv, Brow);
     }
@@ -348,15 +343,27 @@ __global__ void __launch_bounds__(128) k_cell_local(const DevProblem P, const do
         }
         (void)sv;
     }
+}
 
-    double Dij[NE][NE];
+template <int NE>
+__device__ __forceinline__ void load_D(const DevProblem& P, int64_t K, double (&Dij)[NE][NE])
+{
 #pragma unroll
     for (int i = 0; i < NE; ++i)
 #pragma unroll
-        for (int j = 0; j < NE; ++j) Dij[i][j] = cget(P.D, ((int64_t)i * NE + j) * C + K);
+        for (int j = 0; j < NE; ++j) Dij[i][j] = cget(P.D, ((int64_t)i * NE + j) * P.C + K);
+}
 
-    // b_ijK_storage (i,j,s,K): simplices the packed upper triangle column by
-    // column, then the row sums; boxes one value per face orientation
+// b_ijK_storage (i,j,s,K): simplices the packed upper triangle column by
+// column, then the row sums; boxes one value per face orientation
+template <int CT, int NE>
+__device__ __forceinline__ void store_b(const DevProblem& P, int64_t K, const double (&sv)[3],
+                                        const double (&Binv)[ct_nf(CT)][ct_nf(CT)], const double (&Brow)[ct_nf(CT)],
+                                        const double (&Dij)[NE][NE])
+{
+    constexpr int NF = ct_nf(CT);
+    constexpr int S = ct_S(CT);
+    const int64_t C = P.C;
 #pragma unroll
     for (int i = 0; i < NE; ++i)
 #pragma unroll
@@ -376,6 +383,41 @@ __global__ void __launch_bounds__(128) k_cell_local(const DevProblem P, const do
                 for (int e = 0; e < NF; ++e) bp[(int64_t)(S - NF + e) * C] = Brow[e] * Dij[i][j];
             }
         }
+}
+
+// The b update alone (MassMatrix::update over all cells, Solver.hpp:627-639):
+// the first launch of a step whose model updates its vector coefficients
+// from this step's b (updateVectorCoefficients, Solver.hpp:641-652) before
+// the rest of the cell work.
+template <int CT, int NE>
+__global__ void __launch_bounds__(128) k_update_b(const DevProblem P)
+{
+    constexpr int NF = ct_nf(CT);
+    const int64_t K = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (K >= P.C) return;
+    double meas, sv[3], Binv[NF][NF], Brow[NF], Dij[NE][NE];
+    cell_mass_inverse<CT>(P, K, meas, sv, Binv, Brow);
+    load_D<NE>(P, K, Dij);
+    store_b<CT, NE>(P, K, sv, Binv, Brow, Dij);
+}
+
+template <int CT, int NE>
+__global__ void __launch_bounds__(128) k_cell_local(const DevProblem P, const double rtau, const double src_scale)
+{
+    constexpr int NF = ct_nf(CT);
+    const int64_t K = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (K >= P.C) return;
+    const int64_t C = P.C;
+
+    // inverse of the RT0 mass matrix (without D) and its row sums (b_ijKe without D)
+    double meas;
+    double Binv[NF][NF];
+    double Brow[NF];
+    double sv[3];  // box cells: the value of each face orientation
+    cell_mass_inverse<CT>(P, K, meas, sv, Binv, Brow);
+    double Dij[NE][NE];
+    load_D<NE>(P, K, Dij);
+    store_b<CT, NE>(P, K, sv, Binv, Brow, Dij);
 
     int32_t faces[NF];
 #pragma unroll
@@ -715,6 +757,7 @@ static inline unsigned blocks_for(int64_t n, int bs) { return (unsigned)((n + bs
 
 // box launchers (k_local_box.cu)
 int launch_cell_local_box(const DevProblem& P, double rtau, double src_scale, cudaStream_t s);
+int launch_update_b_box(const DevProblem& P, cudaStream_t s);
 int launch_upwind_cuboid(const DevProblem& P, cudaStream_t s);
 int launch_reconstruct_box(const DevProblem& P, cudaStream_t s);
 

@@ -78,7 +78,7 @@ struct mhfem_solver_s {
     struct Hook {
         mhfem_hook fn = nullptr;
         void* user = nullptr;
-    } hooks[2];              // MHFEM_HOOK_PRE_ITERATE, MHFEM_HOOK_POST_ITERATE
+    } hooks[3];              // MHFEM_HOOK_PRE_ITERATE, MHFEM_HOOK_POST_ITERATE, MHFEM_HOOK_VECTOR_COEFFICIENTS
     bool guess_timed = false;
     std::vector<void*> allocs;
 
@@ -141,5 +141,7 @@ mhfem_status learned_solve(mhfem_t h, int* iters, int* sweeps, double* res, mhfe
 void learned_release(mhfem_t h);
 // Marks the network state stale (the pattern changed); the parameters are kept.
 void learned_invalidate(mhfem_t h);
+// Forgets the trace history (the state was set from outside: a restart).
+void learned_reset_history(mhfem_t h);
 
 }  // namespace mhfem

@@ -18,13 +18,14 @@
 // k_cell_local wrote; each record is read by exactly one row.
 #include <type_traits>
 
+#include "fp_convert.h"
 #include "mhfem_internal.h"
 
 namespace mhfem {
 
-// W32: also write the FP32 copy of the values (mixed form).  A template flag,
-// not a run-time test, so that the FP64-only variant carries no conversions
-// (which issue on the scarce FP64 pipe even when predicated off).
+// W32: also write the FP32 copy of the values (mixed form), rounded to
+// nearest on the integer pipes (fp_convert.h): the hardware conversion issues
+// on the FP64 pipe, which the row scaling already keeps busy.
 template <int NF>
 using QmapWord = std::conditional_t<(NF > 4), uint64_t, uint32_t>;
 
@@ -50,7 +51,7 @@ __global__ void __launch_bounds__(256) k_assemble(const DevProblem P, const Qmap
         const int idx = q * NE + j;
         const int k = idx - (idx > dslot ? 1 : 0);
         vals[(int64_t)k * rows + row] = v;
-        if constexpr (W32) vals32[(int64_t)k * rows + row] = (float)v;
+        if constexpr (W32) vals32[(int64_t)k * rows + row] = f64_to_f32_rn(v);  // integer pipes, not FP64
     };
     // A record is read by one row only, but the 32-byte sectors it spans are
     // shared with the neighbouring records of the same cell, which other rows

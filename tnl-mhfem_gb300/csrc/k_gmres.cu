@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(KB) k_gm_update_x(int64_t rows, const double* 
 void gmres_init(const EllMatrix& A, const double* b, const double* x, GmresWork& G, KrylovWork& W, bool first,
                 cudaStream_t s)
 {
-    MHFEM_WIDTH_DISPATCH(A.width, (k_gm_init<WW><<<occ_grid(k_gm_init<WW>), KB, 0, s>>>(
+    MHFEM_WIDTH_DISPATCH(A.width, (k_gm_init<WW><<<row_grid(k_gm_init<WW>, A.rows), KB, 0, s>>>(
                                       A.cols, A.vals, A.width, A.rows, b, x, G.U, G.st, first ? 1 : 0, W.partials,
                                       W.counters)));
 }
@@ -284,22 +284,22 @@ void gmres_init(const EllMatrix& A, const double* b, const double* x, GmresWork&
 void gmres_iterate(const EllMatrix& A, GmresWork& G, KrylovWork& W, int iters, bool reorth, cudaStream_t s)
 {
     for (int it = 0; it < iters; ++it) {
-        MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_gm_arnoldi<WW, true>, s, (const int32_t*)A.cols,
+        MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_gm_arnoldi<WW, true>, s, A.rows, (const int32_t*)A.cols,
                                                  (const double*)A.vals, A.width, A.rows, G.U, G.st, G.partials,
                                                  W.counters));
         if (reorth) {
-            launch_pdl(k_gm_orth<false>, s, A.rows, G.U, G.st, W.partials, W.counters);
-            launch_pdl(k_gm_arnoldi<0, false>, s, (const int32_t*)A.cols, (const double*)A.vals, A.width, A.rows,
+            launch_pdl(k_gm_orth<false>, s, A.rows, A.rows, G.U, G.st, W.partials, W.counters);
+            launch_pdl(k_gm_arnoldi<0, false>, s, A.rows, (const int32_t*)A.cols, (const double*)A.vals, A.width, A.rows,
                        G.U, G.st, G.partials, W.counters);
         }
-        launch_pdl(k_gm_orth<true>, s, A.rows, G.U, G.st, W.partials, W.counters);
+        launch_pdl(k_gm_orth<true>, s, A.rows, A.rows, G.U, G.st, W.partials, W.counters);
     }
 }
 
 void gmres_update(double* x, GmresWork& G, int64_t rows, cudaStream_t s)
 {
     k_gm_solve<<<1, 32, 0, s>>>(G.st);
-    k_gm_update_x<<<occ_grid(k_gm_update_x), KB, 0, s>>>(rows, G.U, x, G.st);
+    k_gm_update_x<<<row_grid(k_gm_update_x, rows), KB, 0, s>>>(rows, G.U, x, G.st);
 }
 
 }  // namespace mhfem

@@ -19,22 +19,20 @@
 //  - FP32 kernels accumulate per-thread sums in FP32 and block sums in FP64:
 //    GB300 issues FP64 at 1/57 of the FP32 rate.
 #include <initializer_list>
+#include <type_traits>
 
+#include "fp_convert.h"
 #include "krylov_common.cuh"
 
 namespace mhfem {
 
-static int g_grid = 0;
-
+// Partial-sum slots of the reductions: 8 CTAs of KB threads per SM of the
+// current device (full occupancy; no iteration kernel launches more).
 int krylov_grid()
 {
-    if (g_grid == 0) {
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        g_grid = (sms > 0 ? sms : 152) * 8;  // 8 x 256 threads = full occupancy
-    }
-    return g_grid;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return 8 * sm_count(dev);
 }
 
 // r = b - A x ; rh = r ; p = r ; partials: r.r, b.b
@@ -180,15 +178,40 @@ __device__ __forceinline__ void ell_apply(const EllRows<T, WW, RPT>& e, const T*
 // Each phase is a grid-stride loop over rows plus, for the reductions, the
 // scalar update that the last CTA applies.  The five iteration kernels below
 // each run one phase.
+//
+// Loads before the dependency wait.  Every iteration kernel is launched
+// with programmatic stream serialization and waits (griddepcontrol.wait)
+// for the kernel before it, whose last CTA computes the scalar this kernel
+// needs.  Its CTAs become resident while that kernel drains.  The FP64
+// SpMVs load the ELL words of their first row (constant during a solve)
+// before waiting, which overlaps one memory round trip with the previous
+// kernel's tail (measured on the 64^3 workload: 56.0 -> 54.7 and 62.7 ->
+// 60.2 us per launch).  The same early loads of the vectors written two or
+// more kernels back slowed the three vector updates (10.0 -> 10.9, 37.0 ->
+// 38.8, 15.1 -> 16.4 us), so those wait first.  Each phase takes `gate`,
+// which waits, releases the next kernel and returns false when the solve is
+// done; a phase calls it exactly once, before it touches the previous
+// kernel's outputs or the scalars.
 
-// v = A p ; acc = (rh, v)
-template <typename T, int WW, int RPT>
-__device__ __forceinline__ void phase_spmv_dot(const int32_t* cols, const T* vals, int W, int64_t rows,
+// v = A p ; acc = (rh, v).  The FP64 plain loop loads the ELL words of its
+// first row before gate(); the pipelined FP32 loop starts after it.
+template <typename T, int WW, int RPT, typename Gate>
+__device__ __forceinline__ bool phase_spmv_dot(const int32_t* cols, const T* vals, int W, int64_t rows,
                                                const T* p, const T* rh, T* v, int64_t gtid, int64_t gstride,
-                                               T (&acc)[1])
+                                               T (&acc)[1], Gate&& gate)
 {
+    const int64_t ng = rows / RPT;
+    auto finish = [&](int64_t q, const T (&y)[RPT]) {
+        VecT<T, RPT> yv;
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) yv.v[j] = y[j];
+        stv<T, RPT>(v, q, yv);
+        const VecT<T, RPT> h = ldv<T, RPT>(rh, q);
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) acc[0] = fma(h.v[j], y[j], acc[0]);
+    };
     if constexpr (spmv_pipelined<T>(WW, RPT)) {
-        const int64_t ng = rows / RPT;
+        if (!gate()) return false;
         int64_t q = gtid;
         EllRows<T, WW, RPT> cur;
         if (q < ng) ell_load<T, WW, RPT>(cols, vals, rows, q, cur);
@@ -198,28 +221,34 @@ __device__ __forceinline__ void phase_spmv_dot(const int32_t* cols, const T* val
             if (qn < ng) ell_load<T, WW, RPT>(cols, vals, rows, qn, nxt);
             T y[RPT];
             ell_apply<T, WW, RPT>(cur, p, ldv<T, RPT>(p, q), y);
-            VecT<T, RPT> yv;
-#pragma unroll
-            for (int j = 0; j < RPT; ++j) yv.v[j] = y[j];
-            stv<T, RPT>(v, q, yv);
-            const VecT<T, RPT> h = ldv<T, RPT>(rh, q);
-#pragma unroll
-            for (int j = 0; j < RPT; ++j) acc[0] = fma(h.v[j], y[j], acc[0]);
+            finish(q, y);
             cur = nxt;
         }
     }
-    else
-        for (int64_t q = gtid; q < rows / RPT; q += gstride) {
+    else if constexpr (WW > 0 && RPT == 1) {
+        EllRows<T, WW, 1> first;
+        if (gtid < ng) ell_load<T, WW, 1>(cols, vals, rows, gtid, first);
+        if (!gate()) return false;
+        if (gtid < ng) {
+            T y[1];
+            ell_apply<T, WW, 1>(first, p, ldv<T, 1>(p, gtid), y);
+            finish(gtid, y);
+        }
+        for (int64_t q = gtid + gstride; q < ng; q += gstride) {
+            T y[1], self[1];
+            spmv_rows<T, WW, 1>(cols, vals, W, rows, q, p, y, self);
+            finish(q, y);
+        }
+    }
+    else {
+        if (!gate()) return false;
+        for (int64_t q = gtid; q < ng; q += gstride) {
             T y[RPT], self[RPT];
             spmv_rows<T, WW, RPT>(cols, vals, W, rows, q, p, y, self);
-            VecT<T, RPT> yv;
-#pragma unroll
-            for (int j = 0; j < RPT; ++j) yv.v[j] = y[j];
-            stv<T, RPT>(v, q, yv);
-            const VecT<T, RPT> h = ldv<T, RPT>(rh, q);
-#pragma unroll
-            for (int j = 0; j < RPT; ++j) acc[0] = fma(h.v[j], y[j], acc[0]);
+            finish(q, y);
         }
+    }
+    return true;
 }
 
 // Streams the groups of V rows of a grid-stride loop through fn(q, in) with
@@ -285,14 +314,27 @@ __device__ __forceinline__ void phase_update_s(int64_t rows, const T* r, const T
     for (int64_t q = nv * V + gtid; q < rows; q += gstride) s[q] = fma(-alpha, v[q], r[q]);
 }
 
-// t = A s ; acc = (t, s), (t, t) and, on a check iteration, (s, s)
-template <typename T, int WW, int RPT, bool CHECK>
-__device__ __forceinline__ void phase_spmv_dots2(const int32_t* cols, const T* vals, int W, int64_t rows,
+// t = A s ; acc = (t, s), (t, t) and, on a check iteration, (s, s).  The
+// FP64 plain loop loads the ELL words of its first row before gate().
+template <typename T, int WW, int RPT, bool CHECK, typename Gate>
+__device__ __forceinline__ bool phase_spmv_dots2(const int32_t* cols, const T* vals, int W, int64_t rows,
                                                  const T* s, T* t, int64_t gtid, int64_t gstride,
-                                                 T (&acc)[CHECK ? 3 : 2])
+                                                 T (&acc)[CHECK ? 3 : 2], Gate&& gate)
 {
+    const int64_t ng = rows / RPT;
+    auto finish = [&](int64_t q, const T (&y)[RPT], const T (&sv)[RPT]) {
+        VecT<T, RPT> yv;
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) {
+            yv.v[j] = y[j];
+            acc[0] = fma(y[j], sv[j], acc[0]);
+            acc[1] = fma(y[j], y[j], acc[1]);
+            if constexpr (CHECK) acc[2] = fma(sv[j], sv[j], acc[2]);
+        }
+        stv<T, RPT>(t, q, yv);
+    };
     if constexpr (spmv_pipelined<T>(WW, RPT)) {
-        const int64_t ng = rows / RPT;
+        if (!gate()) return false;
         int64_t q = gtid;
         EllRows<T, WW, RPT> cur;
         if (q < ng) ell_load<T, WW, RPT>(cols, vals, rows, q, cur);
@@ -300,35 +342,40 @@ __device__ __forceinline__ void phase_spmv_dots2(const int32_t* cols, const T* v
             EllRows<T, WW, RPT> nxt;
             const int64_t qn = q + gstride;
             if (qn < ng) ell_load<T, WW, RPT>(cols, vals, rows, qn, nxt);
-            const VecT<T, RPT> sv = ldv<T, RPT>(s, q);
-            T y[RPT];
-            ell_apply<T, WW, RPT>(cur, s, sv, y);
-            VecT<T, RPT> yv;
+            const VecT<T, RPT> svv = ldv<T, RPT>(s, q);
+            T y[RPT], sv[RPT];
+            ell_apply<T, WW, RPT>(cur, s, svv, y);
 #pragma unroll
-            for (int j = 0; j < RPT; ++j) {
-                yv.v[j] = y[j];
-                acc[0] = fma(y[j], sv.v[j], acc[0]);
-                acc[1] = fma(y[j], y[j], acc[1]);
-                if constexpr (CHECK) acc[2] = fma(sv.v[j], sv.v[j], acc[2]);
-            }
-            stv<T, RPT>(t, q, yv);
+            for (int j = 0; j < RPT; ++j) sv[j] = svv.v[j];
+            finish(q, y, sv);
             cur = nxt;
         }
     }
-    else
-        for (int64_t q = gtid; q < rows / RPT; q += gstride) {
+    else if constexpr (WW > 0 && RPT == 1) {
+        EllRows<T, WW, 1> first;
+        if (gtid < ng) ell_load<T, WW, 1>(cols, vals, rows, gtid, first);
+        if (!gate()) return false;
+        if (gtid < ng) {
+            const VecT<T, 1> svv = ldv<T, 1>(s, gtid);
+            T y[1], sv[1] = {svv.v[0]};
+            ell_apply<T, WW, 1>(first, s, svv, y);
+            finish(gtid, y, sv);
+        }
+        for (int64_t q = gtid + gstride; q < ng; q += gstride) {
+            T y[1], sv[1];
+            spmv_rows<T, WW, 1>(cols, vals, W, rows, q, s, y, sv);
+            finish(q, y, sv);
+        }
+    }
+    else {
+        if (!gate()) return false;
+        for (int64_t q = gtid; q < ng; q += gstride) {
             T y[RPT], sv[RPT];
             spmv_rows<T, WW, RPT>(cols, vals, W, rows, q, s, y, sv);
-            VecT<T, RPT> yv;
-#pragma unroll
-            for (int j = 0; j < RPT; ++j) {
-                yv.v[j] = y[j];
-                acc[0] = fma(y[j], sv[j], acc[0]);
-                acc[1] = fma(y[j], y[j], acc[1]);
-                if constexpr (CHECK) acc[2] = fma(sv[j], sv[j], acc[2]);
-            }
-            stv<T, RPT>(t, q, yv);
+            finish(q, y, sv);
         }
+    }
+    return true;
 }
 
 // check iteration: ||s|| and the half-step test; omega = (t, s) / (t, t)
@@ -488,17 +535,18 @@ __device__ __forceinline__ void phase_update_p(int64_t rows, T* p, const T* r, c
 
 // ---- one kernel per phase ----------------------------------------------------------
 
+// Waits for the preceding kernel, lets the next one launch, and tells whether
+// the solve is still running (the "done" flag that preceding kernel may set).
+#define MHFEM_GATE(sc) [&]() { pdl_wait(); pdl_release(); return *(volatile const int32_t*)&(sc)->done == 0; }
+
 template <typename T, int WW, int RPT>
 __global__ void __launch_bounds__(KB) k_spmv_dot(const int32_t* cols, const T* vals, int W, int64_t rows,
                                                  const T* p, const T* rh, T* v,
                                                  KrylovScalars* sc, double* partials, uint32_t* counter)
 {
-    pdl_wait();
-    pdl_release();
-    if (*(volatile int32_t*)&sc->done) return;
     MHFEM_GRID_STRIDE;
     T acc[1] = {0};
-    phase_spmv_dot<T, WW, RPT>(cols, vals, W, rows, p, rh, v, gtid, gstride, acc);
+    if (!phase_spmv_dot<T, WW, RPT>(cols, vals, W, rows, p, rh, v, gtid, gstride, acc, MHFEM_GATE(sc))) return;
     block_reduce_store<T, 1>(acc, partials);
     if (!ticket_last(counter)) return;
     double s[1];
@@ -525,12 +573,9 @@ __global__ void __launch_bounds__(KB) k_spmv_dots2(const int32_t* cols, const T*
                                                    KrylovScalars* sc, double* partials, uint32_t* counter)
 {
     constexpr int NS = CHECK ? 3 : 2;
-    pdl_wait();
-    pdl_release();
-    if (*(volatile int32_t*)&sc->done) return;
     MHFEM_GRID_STRIDE;
     T acc[NS] = {};
-    phase_spmv_dots2<T, WW, RPT, CHECK>(cols, vals, W, rows, s, t, gtid, gstride, acc);
+    if (!phase_spmv_dots2<T, WW, RPT, CHECK>(cols, vals, W, rows, s, t, gtid, gstride, acc, MHFEM_GATE(sc))) return;
     block_reduce_store<T, NS>(acc, partials);
     if (!ticket_last(counter)) return;
     double sum[NS];
@@ -624,22 +669,22 @@ static void iterate(const EllMatrix& A, const T* vals, T* x, T* r, T* rh, T* p, 
     const int32_t* cols = A.cols;
     for (int it = 0; it < iters; ++it) {
         const bool check = (it == iters - 1);  // the last iteration before the host's check
-        MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dot<T, WW, spmv_rpt(WW, RPT)>, st, cols, vals, A.width,
+        MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dot<T, WW, spmv_rpt(WW, RPT)>, st, A.rows, cols, vals, A.width,
                                                  A.rows, (const T*)p, (const T*)rh, v, sc, W.partials, W.counters));
-        launch_pdl(k_update_s<T, V>, st, A.rows, (const T*)r, (const T*)v, s, (const KrylovScalars*)sc);
+        launch_pdl(k_update_s<T, V>, st, A.rows, A.rows, (const T*)r, (const T*)v, s, (const KrylovScalars*)sc);
         if (check) {
-            MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dots2<T, WW, spmv_rpt(WW, RPT), true>, st, cols, vals,
+            MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dots2<T, WW, spmv_rpt(WW, RPT), true>, st, A.rows, cols, vals,
                                                      A.width, A.rows, (const T*)s, t, sc, W.partials, W.counters));
-            launch_pdl(k_update_xr<T, V, true>, st, A.rows, x, (const T*)p, (const T*)s, (const T*)t, r,
+            launch_pdl(k_update_xr<T, V, true>, st, A.rows, A.rows, x, (const T*)p, (const T*)s, (const T*)t, r,
                        (const T*)rh, sc, W.partials, W.counters);
         }
         else {
-            MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dots2<T, WW, spmv_rpt(WW, RPT), false>, st, cols, vals,
+            MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dots2<T, WW, spmv_rpt(WW, RPT), false>, st, A.rows, cols, vals,
                                                      A.width, A.rows, (const T*)s, t, sc, W.partials, W.counters));
-            launch_pdl(k_update_xr<T, V, false>, st, A.rows, x, (const T*)p, (const T*)s, (const T*)t, r,
+            launch_pdl(k_update_xr<T, V, false>, st, A.rows, A.rows, x, (const T*)p, (const T*)s, (const T*)t, r,
                        (const T*)rh, sc, W.partials, W.counters);
         }
-        launch_pdl(k_update_p<T, V>, st, A.rows, p, (const T*)r, (const T*)v, rh, sc, W.partials, W.counters);
+        launch_pdl(k_update_p<T, V>, st, A.rows, A.rows, p, (const T*)r, (const T*)v, rh, sc, W.partials, W.counters);
     }
 }
 
@@ -652,7 +697,7 @@ void krylov_init_fp64(const EllMatrix& A, const double* b, double* x, KrylovWork
     h.tol = tol;
     h.max_iter = max_iter;
     cudaMemcpyAsync(W.sc, &h, sizeof(h), cudaMemcpyHostToDevice, s);
-    MHFEM_WIDTH_DISPATCH(A.width, (k_init<double, WW><<<occ_grid(k_init<double, WW>), KB, 0, s>>>(A.cols, A.vals, A.width, A.rows, b, x,
+    MHFEM_WIDTH_DISPATCH(A.width, (k_init<double, WW><<<row_grid(k_init<double, WW>, A.rows), KB, 0, s>>>(A.cols, A.vals, A.width, A.rows, b, x,
                                               W.r, W.rh, W.p, W.sc, W.partials, W.counters)));
 }
 
@@ -668,26 +713,31 @@ void krylov_iterate_fp64(const EllMatrix& A, double* x, KrylovWork& W, int iters
 
 // ---- learned form: one pass for the guess inputs --------------------------------
 
-// base = 2 Zn - Zn1 (the extrapolated guess), r_base = b - A base, and the
-// norms the guess needs, in one pass over the matrix: A Zn and A Zn1 are
-// formed row by row (A base = 2 A Zn - A Zn1), so the ELL arrays are read
-// once.  Sums: r_base^2, (b - A Zn)^2, b^2 over all rows; Zn^2,
-// (Zn - Zn1)^2 and the count over the free rows.  The last block writes
-// out[0] = rms(Zn) and out[1] = rms(Zn - Zn1) over the free rows,
-// out[2] = ||r_base||, out[3] = ||b - A Zn|| / ||b|| (the warm start's
-// relative residual) and out[4] = ||b||.
+// r_base = b - A base for the extrapolated base (formed beforehand), and the
+// norms the guess needs, in one pass over the matrix: A Zn and A base are
+// formed row by row, so the ELL arrays are read once.  Sums: r_base^2,
+// (b - A Zn)^2, b^2 over all rows; Zn^2, (Zn - Zn1)^2 and the count over the
+// free rows.  The last block writes out[0] = rms(Zn) and out[1] = rms(Zn -
+// Zn1) over the free rows, out[2] = ||r_base||, out[3] = ||b - A Zn|| / ||b||
+// (the warm start's relative residual), out[4] = ||b||, out[9] = ||r_base|| /
+// ||b||, out[10] = the network's output scale for this step (the last
+// measured base error out[8] once there is one, else out[1]), and the rms
+// over the free rows of the second and third time differences of the
+// traces (out[11], out[12]; 0 until the history reaches them).
 template <int WW>
 __global__ void __launch_bounds__(KB) k_learned_prep(const int32_t* __restrict__ cols,
                                                      const double* __restrict__ vals, int W, int64_t rows,
                                                      const double* __restrict__ b, const double* __restrict__ Zn,
-                                                     const double* __restrict__ Zn1, const uint8_t* __restrict__ fixed,
-                                                     double* __restrict__ base, double* __restrict__ rbase,
+                                                     const double* __restrict__ Zn1, const double* __restrict__ Zn2,
+                                                     const double* __restrict__ Zn3, int hist,
+                                                     const double* __restrict__ base,
+                                                     const uint8_t* __restrict__ fixed, double* __restrict__ rbase,
                                                      double* out, double* partials, uint32_t* counter)
 {
-    double acc[6] = {0, 0, 0, 0, 0, 0};
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB) {
-        const double z = Zn[q], z1 = Zn1[q], bq = b[q];
-        double yz = z, y1 = z1;
+        const double z = Zn[q], bq = b[q];
+        double yz = z, yb = base[q];
         if constexpr (WW > 0) {
             int32_t c[WW];
             double v[WW];
@@ -699,7 +749,7 @@ __global__ void __launch_bounds__(KB) k_learned_prep(const int32_t* __restrict__
 #pragma unroll
             for (int k = 0; k < WW; ++k) {
                 yz = fma(v[k], Zn[c[k]], yz);
-                y1 = fma(v[k], Zn1[c[k]], y1);
+                yb = fma(v[k], base[c[k]], yb);
             }
         }
         else {
@@ -708,26 +758,35 @@ __global__ void __launch_bounds__(KB) k_learned_prep(const int32_t* __restrict__
                 const double v = __ldcs(vals + o);
                 const int32_t c = __ldcs(cols + o);
                 yz = fma(v, Zn[c], yz);
-                y1 = fma(v, Zn1[c], y1);
+                yb = fma(v, base[c], yb);
             }
         }
-        base[q] = fma(2.0, z, -z1);
-        const double rb = bq - fma(2.0, yz, -y1), rw = bq - yz;
+        const double rb = bq - yb, rw = bq - yz;
         rbase[q] = rb;
         acc[0] = fma(rb, rb, acc[0]);
         acc[1] = fma(rw, rw, acc[1]);
         acc[2] = fma(bq, bq, acc[2]);
         if (!fixed[q]) {
+            const double z1 = Zn1[q];
             const double d = z - z1;
             acc[3] = fma(z, z, acc[3]);
             acc[4] = fma(d, d, acc[4]);
             acc[5] += 1.0;
+            if (hist >= 2) {
+                const double z2 = Zn2[q];
+                const double d2 = fma(-2.0, z1, z + z2);
+                acc[6] = fma(d2, d2, acc[6]);
+                if (hist >= 3) {
+                    const double d3 = (z - Zn3[q]) + 3.0 * (z2 - z1);
+                    acc[7] = fma(d3, d3, acc[7]);
+                }
+            }
         }
     }
-    block_reduce_store<double, 6>(acc, partials);
+    block_reduce_store<double, 8>(acc, partials);
     if (!ticket_last(counter)) return;
-    double s[6];
-    final_sums<6>(partials, s);
+    double s[8];
+    final_sums<8>(partials, s);
     if (threadIdx.x == 0) {
         const double n = s[5] > 0 ? s[5] : 1.0;
         const double bn = s[2] > 0 ? sqrt(s[2]) : 1.0;
@@ -736,16 +795,20 @@ __global__ void __launch_bounds__(KB) k_learned_prep(const int32_t* __restrict__
         out[2] = sqrt(s[0]);
         out[3] = sqrt(s[1]) / bn;
         out[4] = bn;
+        out[9] = sqrt(s[0]) / bn;
+        out[10] = out[8] > 0 ? out[8] : out[1];
+        out[11] = sqrt(s[6] / n);
+        out[12] = sqrt(s[7] / n);
     }
 }
 
-void learned_prep_fp64(const EllMatrix& A, const double* b, const double* Zn, const double* Zn1,
-                       const uint8_t* fixed, double* base, double* rbase, double* out, KrylovWork& W,
-                       cudaStream_t s)
+void learned_prep_fp64(const EllMatrix& A, const double* b, const double* Zn, const double* Zn1, const double* Zn2,
+                       const double* Zn3, int hist, const double* base, const uint8_t* fixed, double* rbase,
+                       double* out, KrylovWork& W, cudaStream_t s)
 {
-    MHFEM_WIDTH_DISPATCH(A.width, (k_learned_prep<WW><<<occ_grid(k_learned_prep<WW>), KB, 0, s>>>(
-                                      A.cols, A.vals, A.width, A.rows, b, Zn, Zn1, fixed, base, rbase, out,
-                                      W.partials, W.counters)));
+    MHFEM_WIDTH_DISPATCH(A.width, (k_learned_prep<WW><<<row_grid(k_learned_prep<WW>, A.rows), KB, 0, s>>>(
+                                      A.cols, A.vals, A.width, A.rows, b, Zn, Zn1, Zn2, Zn3, hist, base, fixed,
+                                      rbase, out, W.partials, W.counters)));
 }
 
 // ---- residual of a candidate (learned gate) ------------------------------------
@@ -775,7 +838,7 @@ __global__ void __launch_bounds__(KB) k_residual_norm(const int32_t* cols, const
 
 void residual_norm_fp64(const EllMatrix& A, const double* b, const double* x, KrylovWork& W, cudaStream_t s)
 {
-    MHFEM_WIDTH_DISPATCH(A.width, (k_residual_norm<WW><<<occ_grid(k_residual_norm<WW>), KB, 0, s>>>(A.cols, A.vals, A.width, A.rows, b, x,
+    MHFEM_WIDTH_DISPATCH(A.width, (k_residual_norm<WW><<<row_grid(k_residual_norm<WW>, A.rows), KB, 0, s>>>(A.cols, A.vals, A.width, A.rows, b, x,
                                                 W.sc, W.partials, W.counters)));
 }
 
@@ -823,7 +886,7 @@ __global__ void __launch_bounds__(KB) k_inner_init(int64_t rows, const double* r
     const double scale = (outer->snorm > 0) ? 1.0 / outer->snorm : 0.0;
     float acc[1] = {0.f};
     for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB) {
-        const float v = (float)(r[q] * scale);
+        const float v = f64_to_f32_rn(r[q] * scale);
         r32[q] = v; rh32[q] = v; p32[q] = v; x32[q] = 0.f;
         acc[0] = fmaf(v, v, acc[0]);
     }
@@ -859,20 +922,20 @@ __global__ void __launch_bounds__(KB) k_apply_correction(int64_t rows, double* x
 {
     const double scale = outer->snorm;
     for (int64_t q = (int64_t)blockIdx.x * KB + threadIdx.x; q < rows; q += (int64_t)gridDim.x * KB)
-        x[q] = fma(scale, (double)x32[q], x[q]);
+        x[q] = fma(scale, f32_to_f64(x32[q]), x[q]);
 }
 
 void mixed_outer_residual(const EllMatrix& A, const double* b, const double* x, KrylovWork& W,
                           double tol, int max_sweeps, cudaStream_t s)
 {
     (void)tol; (void)max_sweeps;
-    MHFEM_WIDTH_DISPATCH(A.width, (k_outer_residual<WW><<<occ_grid(k_outer_residual<WW>), KB, 0, s>>>(A.cols, A.vals, A.width, A.rows, b,
+    MHFEM_WIDTH_DISPATCH(A.width, (k_outer_residual<WW><<<row_grid(k_outer_residual<WW>, A.rows), KB, 0, s>>>(A.cols, A.vals, A.width, A.rows, b,
                                                  x, W.r, W.sc, W.partials, W.counters)));
 }
 
 void mixed_inner_init(KrylovWork& W, double inner_tol, int adaptive, int max_iter, cudaStream_t s)
 {
-    k_inner_init<<<occ_grid(k_inner_init), KB, 0, s>>>(W.rows, W.r, W.r32, W.rh32, W.p32, W.x32, W.sc, W.sc32, inner_tol,
+    k_inner_init<<<row_grid(k_inner_init, W.rows), KB, 0, s>>>(W.rows, W.r, W.r32, W.rh32, W.p32, W.x32, W.sc, W.sc32, inner_tol,
                                        adaptive, max_iter, W.partials, W.counters);
 }
 
@@ -891,24 +954,63 @@ void krylov_spmv_dot_once(const EllMatrix& A, KrylovWork& W, bool fp32, cudaStre
 {
     if (fp32) {
         if (spmv4_ok(A, {W.p32, W.rh32, W.v32}))
-            MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dot<float, WW, spmv_rpt(WW, 4)>, s,
+            MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dot<float, WW, spmv_rpt(WW, 4)>, s, A.rows,
                                                      (const int32_t*)A.cols, (const float*)A.vals32, A.width, A.rows,
                                                      (const float*)W.p32, (const float*)W.rh32, W.v32, W.sc32,
                                                      W.partials, W.counters));
         else
-            MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dot<float, WW, 1>, s, (const int32_t*)A.cols,
+            MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dot<float, WW, 1>, s, A.rows, (const int32_t*)A.cols,
                                                      (const float*)A.vals32, A.width, A.rows, (const float*)W.p32,
                                                      (const float*)W.rh32, W.v32, W.sc32, W.partials, W.counters));
     }
     else
-        MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dot<double, WW, 1>, s, (const int32_t*)A.cols,
+        MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dot<double, WW, 1>, s, A.rows, (const int32_t*)A.cols,
                                                  (const double*)A.vals, A.width, A.rows, (const double*)W.p,
                                                  (const double*)W.rh, W.v, W.sc, W.partials, W.counters));
 }
 
+// One launch of one FP64 iteration kernel on the current Krylov vectors
+// (timing): 0 the SpMV + (rh, v), 1 the second SpMV + (t, s), (t, t), 2 the
+// s update, 3 the x / r update (with W.v standing in for x, so the solution
+// is left alone), 4 the p update.
+void krylov_fp64_kernel_once(const EllMatrix& A, KrylovWork& W, int which, cudaStream_t s)
+{
+    const int32_t* cols = A.cols;
+    const bool v2 = vec_ok<double>({W.r, W.rh, W.p, W.v, W.s, W.t});
+    auto run = [&](auto vtag) {
+        constexpr int V = decltype(vtag)::value;
+        switch (which) {
+            case 0:
+                MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dot<double, WW, 1>, s, A.rows, cols, (const double*)A.vals,
+                                                         A.width, A.rows, (const double*)W.p, (const double*)W.rh,
+                                                         W.v, W.sc, W.partials, W.counters));
+                break;
+            case 1:
+                MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dots2<double, WW, 1, false>, s, A.rows, cols,
+                                                         (const double*)A.vals, A.width, A.rows, (const double*)W.s,
+                                                         W.t, W.sc, W.partials, W.counters));
+                break;
+            case 2:
+                launch_pdl(k_update_s<double, V>, s, A.rows, A.rows, (const double*)W.r, (const double*)W.v, W.s,
+                           (const KrylovScalars*)W.sc);
+                break;
+            case 3:
+                launch_pdl(k_update_xr<double, V, false>, s, A.rows, A.rows, W.v, (const double*)W.p, (const double*)W.s,
+                           (const double*)W.t, W.r, (const double*)W.rh, W.sc, W.partials, W.counters);
+                break;
+            default:
+                launch_pdl(k_update_p<double, V>, s, A.rows, A.rows, W.p, (const double*)W.r, (const double*)W.v, W.rh, W.sc,
+                           W.partials, W.counters);
+                break;
+        }
+    };
+    if (v2) run(std::integral_constant<int, 2>{});
+    else run(std::integral_constant<int, 1>{});
+}
+
 void mixed_apply_correction(double* x, KrylovWork& W, cudaStream_t s)
 {
-    k_apply_correction<<<occ_grid(k_apply_correction), KB, 0, s>>>(W.rows, x, W.x32, W.sc);
+    k_apply_correction<<<row_grid(k_apply_correction, W.rows), KB, 0, s>>>(W.rows, x, W.x32, W.sc);
 }
 
 }  // namespace mhfem

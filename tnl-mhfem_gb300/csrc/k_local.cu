@@ -15,6 +15,16 @@ int launch_cell_local(const DevProblem& P, double tau, cudaStream_t s)
     return 1;
 }
 
+int launch_update_b(const DevProblem& P, cudaStream_t s)
+{
+    if (P.C == 0) return 0;
+    if (P.cell) return launch_update_b_box(P, s);
+    const unsigned grid = blocks_for(P.C, 128);
+    if (P.nf == 3) MHFEM_NE_DISPATCH(CT_TRI, P.n, (k_update_b<CT, NE><<<grid, 128, 0, s>>>(P)));
+    else MHFEM_NE_DISPATCH(CT_TET, P.n, (k_update_b<CT, NE><<<grid, 128, 0, s>>>(P)));
+    return 1;
+}
+
 // k_upwind depends on the number of faces per cell only: rectangles share
 // the tetrahedron instances (4 faces), cuboids have their own.
 int launch_upwind(const DevProblem& P, cudaStream_t s)

@@ -12,6 +12,14 @@ int launch_cell_local_box(const DevProblem& P, double rtau, double src_scale, cu
     return 1;
 }
 
+int launch_update_b_box(const DevProblem& P, cudaStream_t s)
+{
+    const unsigned grid = blocks_for(P.C, 128);
+    if (P.dim == 2) MHFEM_NE_DISPATCH(CT_RECT, P.n, (k_update_b<CT, NE><<<grid, 128, 0, s>>>(P)));
+    else MHFEM_NE_DISPATCH(CT_CUBOID, P.n, (k_update_b<CT, NE><<<grid, 128, 0, s>>>(P)));
+    return 1;
+}
+
 int launch_upwind_cuboid(const DevProblem& P, cudaStream_t s)
 {
     MHFEM_NE_DISPATCH(CT_CUBOID, P.n, (k_upwind<NF, NE><<<blocks_for(P.F, 256), 256, 0, s>>>(P)));

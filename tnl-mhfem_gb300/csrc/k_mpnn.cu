@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(NT, TRAIN ? 2 : 3) k_mpnn_layer(const MpnnView
             if (tid < TB && row0 + tid < F) {
                 const int64_t row = row0 + tid;
                 const float out = sdec[0][tid] + sdec[1][tid] + sdec[2][tid] + sdec[3][tid] + V.bd[0];
-                V.dec_guess[row] = V.fixed[row] ? V.dec_rhs[row] : V.dec_base[row] + V.dec_scal[1] * (double)out;
+                V.dec_guess[row] = V.fixed[row] ? V.dec_rhs[row] : V.dec_base[row] + V.dec_scal[10] * (double)out;
             }
         }
         else {

@@ -1,7 +1,7 @@
 // Inputs and outputs of the learned warm-start network: the 16 BF16 input
-// features of every face, the training target and the gate that accepts or
-// rejects the guess (the per-step scales, the extrapolated base and its
-// residual come from learned_prep_fp64).
+// features of every face, the extrapolated base, the training target and
+// the gate that picks the solve's initial guess (the per-step scales and
+// the residuals come from learned_prep_fp64).
 //
 // Features of face E (x0[E][c]):
 //   0  Zn / sz                 current trace (the previous step's solution)
@@ -12,12 +12,24 @@
 //   5-7 |n_x|, |n_y|, |n_z|   unit normal, sign-free (static)
 //   8  face measure / mean face measure (static)
 //   9  boundary flag, 10 Dirichlet flag, 11 constant 1 (static)
-//   12 r / rms(r), r = b - A (2 Zn - Zn1) the residual of the extrapolated guess
-//   13-15 zero
-// The network predicts (Z_new - (2 Zn - Zn1)) / sd.
+//   12 r / rms(r), r = b - A base the residual of the extrapolated base
+//   13 (Zn - 2 Zn1 + Zn2) / s2, 14 (Zn - 3 Zn1 + 3 Zn2 - Zn3) / s3: the second
+//      and third time differences (zero until the history reaches them)
+//   15 zero
+// The base is the polynomial extrapolation of the last traces in time (order
+// 1 to 3: 2 Zn - Zn1, 3 Zn - 3 Zn1 + Zn2, 4 Zn - 6 Zn1 + 4 Zn2 - Zn3), and the
+// network predicts (Z_new - base) / c, with c the root mean square of the
+// previous step's base error (Z_new - base over the free rows).
+//
+// Device scalars (scal[]): 0 rms(Zn), 1 sd = rms(Zn - Zn1), 2 ||b - A base||,
+// 3 ||b - A Zn|| / ||b||, 4 ||b||, 5 the network guess's relative residual,
+// 6 the gate's choice (0 warm start, 1 network guess, 2 base), 8 the last
+// measured base error c, 9 ||b - A base|| / ||b||, 10 the scale used this
+// step (c, or sd until c is known), 11 and 12 the rms of the second and third
+// time differences.
 #include <cuda_bf16.h>
 
-#include "mhfem_internal.h"
+#include "krylov_common.cuh"
 #include "mpnn.h"
 
 namespace mhfem {
@@ -27,12 +39,14 @@ namespace {
 // The scales come from the device (learned_prep_fp64's output), once per block.
 __global__ void __launch_bounds__(256) k_features(int64_t F, MpnnInputs in, __nv_bfloat16* x0)
 {
-    __shared__ double rsz, rsd;
+    __shared__ double rsz, rsd, rs2, rs3;
     __shared__ float rscale;
     if (threadIdx.x == 0) {
-        const double sz = in.scal[0], sd = in.scal[1], rn = in.scal[2];
+        const double sz = in.scal[0], sd = in.scal[1], rn = in.scal[2], s2 = in.scal[11], s3 = in.scal[12];
         rsz = sz > 0 ? 1.0 / sz : 0.0;
         rsd = sd > 0 ? 1.0 / sd : 0.0;
+        rs2 = (in.hist >= 2 && s2 > 0) ? 1.0 / s2 : 0.0;
+        rs3 = (in.hist >= 3 && s3 > 0) ? 1.0 / s3 : 0.0;
         rscale = rn > 0 ? (float)(sqrt((double)F) / rn) : 0.f;
     }
     __syncthreads();
@@ -47,6 +61,11 @@ __global__ void __launch_bounds__(256) k_features(int64_t F, MpnnInputs in, __nv
     v[2] = (float)(in.rhs[E] * rsz);
     v[4] = (float)((in.f_base[E] + in.src_scale * in.f_psi[E]) * in.f_norm);
     v[12] = (float)in.rbase[E] * rscale;
+    if (in.hist >= 2) {
+        const double z1 = in.Zn1[E], z2 = in.Zn2[E];
+        v[13] = (float)(fma(-2.0, z1, z + z2) * rs2);
+        if (in.hist >= 3) v[14] = (float)(((z - in.Zn3[E]) + 3.0 * (z2 - z1)) * rs3);
+    }
     uint32_t w[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
@@ -58,27 +77,67 @@ __global__ void __launch_bounds__(256) k_features(int64_t F, MpnnInputs in, __nv
     dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
 }
 
-__global__ void k_target(int64_t F, const double* Znew, const double* base, const double* scal, double* y)
+// base = polynomial extrapolation of the last traces; the Dirichlet rows take
+// their prescribed value (their row of the system is the identity)
+__global__ void __launch_bounds__(256) k_extrapolate(int64_t F, int order, const double* Z0, const double* Z1,
+                                                     const double* Z2, const double* Z3, const uint8_t* fixed,
+                                                     const double* rhs, double* base)
 {
-    const double sd = scal[1];
-    const double rsd = sd > 0 ? 1.0 / sd : 0.0;
     const int64_t E = (int64_t)blockIdx.x * 256 + threadIdx.x;
-    if (E < F) y[E] = (Znew[E] - base[E]) * rsd;
+    if (E >= F) return;
+    double v;
+    if (fixed[E]) v = rhs[E];
+    else if (order >= 3) v = fma(4.0, Z0[E], fma(-6.0, Z1[E], fma(4.0, Z2[E], -Z3[E])));
+    else if (order == 2) v = fma(3.0, Z0[E] - Z1[E], Z2[E]);
+    else if (order == 1) v = fma(2.0, Z0[E], -Z1[E]);
+    else v = Z0[E];
+    base[E] = v;
+}
+
+// y = (Znew - base) / scal[10] (training target, when y != nullptr) and the
+// base's error c = rms(Znew - base) over the free rows into scal[8] for the
+// next step: per-block partial sums, summed in a fixed order by the last block.
+__global__ void __launch_bounds__(KB) k_target(int64_t F, const double* Znew, const double* base, const uint8_t* fixed,
+                                               double* scal, double* y, double* partials, uint32_t* counter)
+{
+    const double c = scal[10];
+    const double rc = c > 0 ? 1.0 / c : 0.0;
+    double acc[2] = {0, 0};
+    for (int64_t E = (int64_t)blockIdx.x * KB + threadIdx.x; E < F; E += (int64_t)gridDim.x * KB) {
+        const double d = Znew[E] - base[E];
+        if (y) y[E] = d * rc;
+        if (!fixed[E]) {
+            acc[0] = fma(d, d, acc[0]);
+            acc[1] += 1.0;
+        }
+    }
+    block_reduce_store<double, 2>(acc, partials);
+    if (!ticket_last(counter)) return;
+    double sum[2];
+    final_sums<2>(partials, sum);
+    if (threadIdx.x == 0 && sum[1] > 0) scal[8] = sqrt(sum[0] / sum[1]);
 }
 
 // The learned gate, decided on the device so that no host round trip sits
-// between the guess and the solve.
-__global__ void __launch_bounds__(256) k_gate(int64_t F, const double* guess, double* Z, const double* rguess,
-                                              double* scal)
+// between the guess and the solve: of the warm start (scal[3]), the
+// extrapolated base (scal[9]) and the network's guess (*rguess, when it ran)
+// the one with the lowest relative FP64 residual becomes the initial guess.
+__global__ void __launch_bounds__(256) k_gate(int64_t F, const double* guess, const double* base, double* Z,
+                                              const double* rguess, double* scal)
 {
-    const double rg = *rguess, rw = scal[3];
-    const bool use = isfinite(rg) && rg < rw;
+    const double rw = scal[3], rb = scal[9];
+    const double rg = guess ? *rguess : INFINITY;
+    int choice = 0;
+    double best = rw;
+    if (isfinite(rb) && rb < best) { choice = 2; best = rb; }
+    if (isfinite(rg) && rg < best) { choice = 1; best = rg; }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        scal[5] = rg;
-        scal[6] = use ? 1.0 : 0.0;
+        scal[5] = guess ? rg : -1.0;
+        scal[6] = (double)choice;
     }
-    if (!use) return;
-    for (int64_t q = (int64_t)blockIdx.x * 256 + threadIdx.x; q < F; q += (int64_t)gridDim.x * 256) Z[q] = guess[q];
+    if (choice == 0) return;
+    const double* src = choice == 1 ? guess : base;
+    for (int64_t q = (int64_t)blockIdx.x * 256 + threadIdx.x; q < F; q += (int64_t)gridDim.x * 256) Z[q] = src[q];
 }
 
 __global__ void k_from_host(int64_t n, const float* xf, __nv_bfloat16* x0)
@@ -106,19 +165,27 @@ void mpnn_features(int64_t F, const MpnnInputs& in, __nv_bfloat16* x0, cudaStrea
     k_features<<<nb(F), 256, 0, s>>>(F, in, x0);
 }
 
-void mpnn_target(int64_t F, const double* Znew, const double* base, const double* scal, double* y, cudaStream_t s)
+void mpnn_extrapolate(int64_t F, int order, const double* Z0, const double* Z1, const double* Z2, const double* Z3,
+                      const uint8_t* fixed, const double* rhs, double* base, cudaStream_t s)
 {
-    k_target<<<nb(F), 256, 0, s>>>(F, Znew, base, scal, y);
+    k_extrapolate<<<nb(F), 256, 0, s>>>(F, order, Z0, Z1, Z2, Z3, fixed, rhs, base);
 }
 
-void mpnn_gate(int64_t F, const double* guess, double* Z, const double* rguess, double* scal, cudaStream_t s)
+void mpnn_target(int64_t F, const double* Znew, const double* base, const uint8_t* fixed, double* scal, double* y,
+                 double* partials, uint32_t* counter, cudaStream_t s)
+{
+    k_target<<<row_grid(k_target, F), KB, 0, s>>>(F, Znew, base, fixed, scal, y, partials, counter);
+}
+
+void mpnn_gate(int64_t F, const double* guess, const double* base, double* Z, const double* rguess, double* scal,
+               cudaStream_t s)
 {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int64_t cap = (int64_t)(sms > 0 ? sms : 152) * 8;
     const int64_t g = (int64_t)nb(F) < cap ? (int64_t)nb(F) : cap;
-    k_gate<<<(unsigned)(g > 0 ? g : 1), 256, 0, s>>>(F, guess, Z, rguess, scal);
+    k_gate<<<(unsigned)(g > 0 ? g : 1), 256, 0, s>>>(F, guess, base, Z, rguess, scal);
 }
 
 void mpnn_features_from_host(int64_t F, const float* xf, __nv_bfloat16* x0, cudaStream_t s)

@@ -13,41 +13,71 @@ namespace mhfem {
 
 constexpr int KB = 256;
 
-// Grid of a grid-stride kernel: as many CTAs of KB threads as can be resident
-// at once on every SM (fixed per kernel and device, so reductions stay
-// deterministic).
+// SM count of a device (cached per device ordinal).
+static int sm_count(int dev)
+{
+    static std::mutex mu;
+    static std::unordered_map<int, int> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(dev);
+    if (it != cache.end()) return it->second;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 152;
+    cache[dev] = sms;
+    return sms;
+}
+
+// Grid of a grid-stride kernel on the current device: as many CTAs of KB
+// threads as can be resident at once on every SM, at most 8 per SM (fixed per
+// kernel and device, so reductions stay deterministic).
 template <typename Kern>
 static int occ_grid(Kern kernel)
 {
     static std::mutex mu;
-    static std::unordered_map<const void*, int> cache;
-    static int sms = 0;
+    static std::unordered_map<unsigned long long, int> cache;  // key: device ordinal, kernel address
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int sms = sm_count(dev);
     std::lock_guard<std::mutex> lock(mu);
-    if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 152;
-    }
-    auto it = cache.find((const void*)kernel);
+    const unsigned long long key = ((unsigned long long)(unsigned)dev << 48) ^ (unsigned long long)(uintptr_t)kernel;
+    auto it = cache.find(key);
     if (it != cache.end()) return it->second;
     int nb = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, KB, 0);
     const int g = sms * (nb > 0 ? (nb < 8 ? nb : 8) : 1);
-    cache[(const void*)kernel] = g;
+    cache[key] = g;
     return g;
 }
 
-// Launches an iteration kernel (one wave, occ_grid CTAs) with programmatic
-// stream serialization, so that its CTAs are scheduled while the preceding
-// kernel of the iteration drains (the kernel itself waits for that kernel's
-// results with griddepcontrol.wait).  Captured into a CUDA graph this becomes
-// a programmatic dependency edge.
+// Grid of a grid-stride kernel over `rows` rows: the resident wave
+// (occ_grid), or fewer CTAs for a small system, so that every thread has at
+// least kMinRowsPerThread rows.  A small system's kernels are bound by
+// latency, and each reduction's last CTA then sums fewer partials (the
+// 128^2 heat-equation system, 49,408 rows: 48 CTAs instead of 1,216).  The
+// grid is fixed per kernel, device and row count, so reductions stay
+// deterministic.
+constexpr int kMinRowsPerThread = 4;
+
+template <typename Kern>
+static int row_grid(Kern kernel, int64_t rows)
+{
+    const int64_t per_cta = (int64_t)KB * kMinRowsPerThread;
+    const int64_t need = (rows + per_cta - 1) / per_cta;
+    const int64_t g = occ_grid(kernel);
+    return (int)(need < 1 ? 1 : (need < g ? need : g));
+}
+
+// Launches an iteration kernel (at most one wave: row_grid CTAs) with
+// programmatic stream serialization, so that its CTAs are scheduled while the
+// preceding kernel of the iteration drains (the kernel itself waits for that
+// kernel's results with griddepcontrol.wait).  Captured into a CUDA graph
+// this becomes a programmatic dependency edge.
 template <typename... KArgs, typename... Args>
-static void launch_pdl(void (*kernel)(KArgs...), cudaStream_t s, Args&&... args)
+static void launch_pdl(void (*kernel)(KArgs...), cudaStream_t s, int64_t grid_rows, Args&&... args)
 {
     cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3((unsigned)occ_grid(kernel));
+    cfg.gridDim = dim3((unsigned)row_grid(kernel, grid_rows));
     cfg.blockDim = dim3(KB);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = s;

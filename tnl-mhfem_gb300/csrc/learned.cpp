@@ -2,13 +2,17 @@
 // (k_mpnn.cu) around the unchanged FP64 BiCGStab solve.
 //
 // Per time step (after the assembly):
-//   1. Zn = the previous step's traces (the default warm start);
-//   2. once the network is trained: guess = 2 Zn - Zn1 + sd * net(features);
-//      the guess replaces the warm start only if its relative residual
-//      ||b - A x|| / ||b|| is smaller than the warm start's;
-//   3. the FP64 BiCGStab runs to the same tolerance as the plain form, so the
-//      network can only change the iteration count;
-//   4. during the first `train_steps` steps the network is trained online
+//   1. Zn = the previous step's traces (the default warm start); the last
+//      four traces are kept;
+//   2. base = the polynomial extrapolation in time of the last traces (order
+//      1 to 3, as far as the history reaches);
+//   3. once the network is trained: guess = base + c * net(features), c the
+//      size of the base's error in the previous step;
+//   4. of the warm start, the base and the guess, the one with the lowest
+//      relative residual ||b - A x|| / ||b|| starts the solve;
+//   5. the FP64 BiCGStab runs to the same tolerance as the plain form, so the
+//      initial guess can only change the iteration count;
+//   6. during the first `train_steps` steps the network is trained online
 //      (Adam) on the solution the method just produced.
 #include <cmath>
 #include <cstring>
@@ -45,9 +49,9 @@ struct LearnedState {
     double* dec_partials = nullptr;
     float* dw_partials = nullptr;
     double* loss = nullptr;
-    double* scal = nullptr;  // [8] device: learned_prep_fp64's out[0..4], r_guess, used
-    double* Zn = nullptr;
-    double* Zn1 = nullptr;
+    double* scal = nullptr;  // [16] device scalars, laid out in k_mpnn_io.cu
+    double* Zs[4] = {};      // the last traces, a ring: Zs[cur] is this step's Zn
+    int cur = 0;
     double* base = nullptr;
     double* guess = nullptr;
     double* target = nullptr;
@@ -66,6 +70,7 @@ struct LearnedState {
     float lr = 1e-3f;
     double lr_final = 1.0;  // fraction of lr at the last training step (cosine decay)
     int use_during_training = 0;
+    int order = 3;        // extrapolation order of the base
     uint64_t seed = 1234;
     double last_loss = -1;
     std::vector<void*> allocs;
@@ -186,6 +191,11 @@ double coef_at(mhfem_t h, int which, int64_t idx, double dflt)
 void learned_invalidate(mhfem_t h)
 {
     if (h->learned) h->learned->ready = false;
+}
+
+void learned_reset_history(mhfem_t h)
+{
+    if (h->learned) h->learned->hist = 0;
 }
 
 void learned_release(mhfem_t h)
@@ -321,17 +331,17 @@ static mhfem_status learned_prepare(mhfem_t h)
     LCK(lalloc(L, &L->dec_partials, (size_t)mpnn_grid_size(F) * (H + 2)));
     LCK(lalloc(L, &L->dw_partials, (size_t)mpnn_partials_floats(F)));
     LCK(lalloc(L, &L->loss, 1));
-    LCK(lalloc(L, &L->scal, 8));
-    LCK(cudaMemset(L->scal, 0, sizeof(double) * 8));
-    LCK(lalloc(L, &L->Zn, F));
-    LCK(lalloc(L, &L->Zn1, F));
+    LCK(lalloc(L, &L->scal, 16));
+    LCK(cudaMemset(L->scal, 0, sizeof(double) * 16));
+    for (auto& z : L->Zs) LCK(lalloc(L, &z, F));
+    L->cur = 0;
     LCK(lalloc(L, &L->base, F));
     LCK(lalloc(L, &L->guess, F));
     LCK(lalloc(L, &L->target, F));
     LCK(lalloc(L, &L->out, F));
     LCK(lalloc(L, &L->err, 1));
     LCK(cudaMemset(L->err, 0, sizeof(int32_t)));
-    if (!L->host) LCK(cudaMallocHost((void**)&L->host, sizeof(double) * 8));
+    if (!L->host) LCK(cudaMallocHost((void**)&L->host, sizeof(double) * 16));
     std::vector<float> p0;
     if (had_params && !keep.empty()) p0 = keep;
     else init_params_host(p0, L->seed);
@@ -384,13 +394,18 @@ mhfem_status learned_solve(mhfem_t h, int* iters, int* sweeps, double* res, mhfe
     LearnedState* L = h->learned;
     const int64_t F = L->F;
     cudaStream_t s = h->stream;
-    LCK(cudaMemcpyAsync(L->Zn, h->Z_iF, sizeof(double) * F, cudaMemcpyDeviceToDevice, s));
+    double* Zn = L->Zs[L->cur];
+    const double* Zprev[3] = {L->Zs[(L->cur + 3) & 3], L->Zs[(L->cur + 2) & 3], L->Zs[(L->cur + 1) & 3]};
+    LCK(cudaMemcpyAsync(Zn, h->Z_iF, sizeof(double) * F, cudaMemcpyDeviceToDevice, s));
     const bool have_hist = L->hist >= 1;
     const bool training = L->trained_steps < L->train_steps;
     const bool infer = have_hist && (!training || L->use_during_training) && (L->trained_steps > 0 || L->params_loaded);
     MpnnInputs in{};
-    in.Zn = L->Zn;
-    in.Zn1 = L->Zn1;
+    in.Zn = Zn;
+    in.Zn1 = Zprev[0];
+    in.Zn2 = Zprev[1];
+    in.Zn3 = Zprev[2];
+    in.hist = std::min(L->hist, 3);
     in.rhs = h->rhs;
     in.stat = L->stat;
     in.f_base = L->f_base;
@@ -399,27 +414,33 @@ mhfem_status learned_solve(mhfem_t h, int* iters, int* sweeps, double* res, mhfe
     in.f_norm = L->f_norm;
     in.rbase = h->W.r;  // the Krylov r vector is idle until the solve
     in.scal = L->scal;
-    if (infer) {
+    if (have_hist) {
         cudaEventRecord(h->ev[5], s);
         h->guess_timed = true;
     }
-    // Inference runs without a host round trip: the scales stay on the
-    // device and the gate decides there.  Training reads the scales (the
-    // target divides by sd), outside the timed use phase.
+    // The base, its residual and the gate run without a host round trip:
+    // the scales stay on the device and the gate decides there.  Training
+    // reads the scales (the features divide by them), outside the timed use
+    // phase.
     bool have_features = false;
     if (have_hist) {
-        learned_prep_fp64(h->A, h->rhs, L->Zn, L->Zn1, L->fixed, L->base, h->W.r, L->scal, h->W, s);
-        h->launches += 1;
-        if (training) {
-            LCK(cudaMemcpyAsync(L->host, L->scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
-            LCK(cudaStreamSynchronize(s));
-            have_features = L->host[0] > 0 && L->host[1] > 0;
-        }
-        else
-            have_features = true;  // zero scales make the features zero; the gate rejects a useless guess
-        if (have_features) {
-            mpnn_features(F, in, L->x0, s);
-            h->launches += 1;
+        const int order = std::min(L->order, L->hist);
+        mpnn_extrapolate(F, order, Zn, Zprev[0], Zprev[1], Zprev[2], L->fixed, h->rhs, L->base, s);
+        learned_prep_fp64(h->A, h->rhs, Zn, Zprev[0], Zprev[1], Zprev[2], std::min(L->hist, 3), L->base, L->fixed,
+                          h->W.r, L->scal, h->W, s);
+        h->launches += 2;
+        if (training || infer) {
+            if (training) {
+                LCK(cudaMemcpyAsync(L->host, L->scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+                LCK(cudaStreamSynchronize(s));
+                have_features = L->host[0] > 0 && L->host[1] > 0;
+            }
+            else
+                have_features = true;  // zero scales make the features zero; the gate rejects a useless guess
+            if (have_features) {
+                mpnn_features(F, in, L->x0, s);
+                h->launches += 1;
+            }
         }
     }
     const bool guessed = infer && have_features;
@@ -431,36 +452,45 @@ mhfem_status learned_solve(mhfem_t h, int* iters, int* sweeps, double* res, mhfe
         V.dec_guess = L->guess;
         mpnn_infer_guess(V, s);
         residual_norm_fp64(h->A, h->rhs, L->guess, h->W, s);
-        mpnn_gate(F, L->guess, h->Z_iF, &h->W.sc->res, L->scal, s);
-        h->launches += (kMpnnLayers + 1) + 2;
+        h->launches += (kMpnnLayers + 1) + 1;
+    }
+    if (have_hist) {
+        mpnn_gate(F, guessed ? L->guess : nullptr, L->base, h->Z_iF, &h->W.sc->res, L->scal, s);
+        h->launches += 1;
     }
     if (h->guess_timed) cudaEventRecord(h->ev[6], s);
     st = L->mixed_solve ? run_mixed(h, iters, sweeps, res) : run_fp64(h, h->opts.tol, h->opts.max_iter, iters, res);
     if (st) return st;
-    int used = 0;
-    double r_warm = -1, r_guess = -1;
-    if (guessed) {
-        LCK(cudaMemcpyAsync(L->host, L->scal, 8 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    int source = 0;
+    double r_warm = -1, r_guess = -1, r_base = -1;
+    if (have_hist) {
+        LCK(cudaMemcpyAsync(L->host, L->scal, 11 * sizeof(double), cudaMemcpyDeviceToHost, s));
         if ((st = check_err(h)) != MHFEM_OK) return st;  // synchronizes the stream
         r_warm = L->host[3];
-        r_guess = L->host[5];
-        used = L->host[6] != 0.0 ? 1 : 0;
-    }
-    if (training && have_features) {
-        mpnn_target(F, h->Z_iF, L->base, L->scal, L->target, s);
+        r_guess = guessed ? L->host[5] : -1;
+        r_base = L->host[9];
+        source = (int)L->host[6];
+        // the base's error in this step (and, while training, the target scaled by this step's c)
+        const bool train_now = training && have_features;
+        mpnn_target(F, h->Z_iF, L->base, L->fixed, L->scal, train_now ? L->target : nullptr, h->W.partials,
+                    h->W.counters, s);
         h->launches += 1;
-        if ((st = train_once(h, L->train_iters)) != MHFEM_OK) return st;
-        LCK(cudaStreamSynchronize(s));
-        if ((st = check_err(h)) != MHFEM_OK) return st;
-        L->last_loss = L->host[4];
-        L->trained_steps += 1;
+        if (train_now) {
+            if ((st = train_once(h, L->train_iters)) != MHFEM_OK) return st;
+            LCK(cudaStreamSynchronize(s));
+            if ((st = check_err(h)) != MHFEM_OK) return st;
+            L->last_loss = L->host[4];
+            L->trained_steps += 1;
+        }
     }
-    std::swap(L->Zn, L->Zn1);  // Zn1 <- the traces this step started from
+    L->cur = (L->cur + 1) & 3;  // this step's Zn becomes Zn1
     L->hist += 1;
     if (stats) {
-        stats->guess_used = used;
+        stats->guess_used = source == 1 ? 1 : 0;
         stats->guess_residual = r_guess;
         stats->warm_residual = r_warm;
+        stats->base_residual = r_base;
+        stats->guess_source = source;
     }
     return MHFEM_OK;
 }
@@ -490,7 +520,7 @@ mhfem_status mhfem_learned_set_options(mhfem_t h, const mhfem_learned_opts* o)
 {
     if (!h || !o) return MHFEM_ERR_INVALID_ARGUMENT;
     if (o->train_steps < 0 || o->train_iters < 1 || !(o->learning_rate > 0) || !(o->lr_final > 0) ||
-        o->lr_final > 1)
+        o->lr_final > 1 || o->extrapolation_order < 0 || o->extrapolation_order > 3)
         return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "invalid learned-form options");
     if (!h->learned) h->learned = new LearnedState();
     LearnedState* L = h->learned;
@@ -499,6 +529,7 @@ mhfem_status mhfem_learned_set_options(mhfem_t h, const mhfem_learned_opts* o)
     L->lr = (float)o->learning_rate;
     L->lr_final = o->lr_final;
     L->use_during_training = o->use_during_training;
+    L->order = o->extrapolation_order;
     L->mixed_solve = o->mixed_solve ? 1 : 0;
     if (h->desc.form == MHFEM_FORM_LEARNED && (L->mixed_solve != 0) != h->fp32_copy) {
         // the FP32 matrix copy and work vectors follow; the pattern is rebuilt at the next step

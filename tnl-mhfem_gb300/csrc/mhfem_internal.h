@@ -128,6 +128,8 @@ struct AssemblyMap {
 int launch_face_average(const DevProblem& P, cudaStream_t s);
 int launch_upwind(const DevProblem& P, cudaStream_t s);
 int launch_cell_local(const DevProblem& P, double tau, cudaStream_t s);
+// b alone (before a model's vector-coefficient hook; the cell kernel writes the same b again)
+int launch_update_b(const DevProblem& P, cudaStream_t s);
 int launch_reconstruct(const DevProblem& P, cudaStream_t s);
 
 // Launchers (k_assemble.cu)
@@ -207,14 +209,20 @@ void residual_norm_fp64(const EllMatrix& A, const double* b, const double* x, Kr
 
 int krylov_grid();
 
-// Learned form, one pass before the network: base = 2 Zn - Zn1, rbase =
-// b - A base, out[0..4] = rms(Zn), rms(Zn - Zn1) (free rows), ||rbase||,
-// ||b - A Zn|| / ||b||, ||b||.
-void learned_prep_fp64(const EllMatrix& A, const double* b, const double* Zn, const double* Zn1,
-                       const uint8_t* fixed, double* base, double* rbase, double* out, KrylovWork& W,
-                       cudaStream_t s);
+// Learned form, one pass before the network, on the extrapolated base formed
+// beforehand: rbase = b - A base, out[0..4] = rms(Zn), rms(Zn - Zn1) (free
+// rows), ||rbase||, ||b - A Zn|| / ||b||, ||b||; out[9] = ||rbase|| / ||b||,
+// out[10] = the network's output scale (out[8] when set, else out[1]);
+// out[11], out[12] = rms of the second and third time differences (free
+// rows) when hist (the traces before Zn) reaches 2 and 3.
+void learned_prep_fp64(const EllMatrix& A, const double* b, const double* Zn, const double* Zn1, const double* Zn2,
+                       const double* Zn3, int hist, const double* base, const uint8_t* fixed, double* rbase,
+                       double* out, KrylovWork& W, cudaStream_t s);
 
 // One launch of the SpMV + dot kernel on the current Krylov vectors (timing).
 void krylov_spmv_dot_once(const EllMatrix& A, KrylovWork& W, bool fp32, cudaStream_t s);
+// One launch of FP64 iteration kernel `which` (0 SpMV + dot, 1 second SpMV + dots,
+// 2 s update, 3 x / r update on W.v instead of x, 4 p update) (timing).
+void krylov_fp64_kernel_once(const EllMatrix& A, KrylovWork& W, int which, cudaStream_t s);
 
 }  // namespace mhfem

@@ -44,7 +44,7 @@ struct MpnnView {
     // guess = base + sd (h4 . wd + bd) on free rows, the Dirichlet value on fixed rows
     const double* dec_base = nullptr;
     const double* dec_rhs = nullptr;
-    const double* dec_scal = nullptr;  // device scales, sd = rms(Zn - Zn1) at [1]
+    const double* dec_scal = nullptr;  // device scalars; the output scale c at [10]
     double* dec_guess = nullptr;
 };
 
@@ -71,21 +71,32 @@ int mpnn_grid_size(int64_t F);
 struct MpnnInputs {
     const double* Zn;        // current face traces (warm start)
     const double* Zn1;       // previous step's traces
+    const double* Zn2;       // the traces two and three steps back (read when hist reaches 2, 3)
+    const double* Zn3;
+    int hist;                // traces available before Zn (0..3)
     const double* rhs;       // scaled right-hand side of the current system
     const float* stat;       // [F][16] static features (channels 3, 5..11 filled)
     const float* f_base;     // [F] face average of the source
     const float* f_psi;      // [F] face average of the source shape psi
     double src_scale;        // amplitude * sin(2 pi t / T)
     double f_norm;           // scale of the source channel
-    const double* rbase;     // residual b - A (2 Zn - Zn1) of the extrapolated guess
-    const double* scal;      // device: rms(Zn), rms(Zn - Zn1) over the free rows, ||rbase||
+    const double* rbase;     // residual b - A base of the extrapolated base
+    const double* scal;      // device scalars (k_mpnn_io.cu): rms(Zn), rms(Zn - Zn1), ||rbase||, ...
 };
 void mpnn_features(int64_t F, const MpnnInputs& in, __nv_bfloat16* x0, cudaStream_t s);
-// training target y = (Znew - base) / sd with sd = scal[1] (device)
-void mpnn_target(int64_t F, const double* Znew, const double* base, const double* scal, double* y, cudaStream_t s);
-// the learned gate: Z = guess if guess's relative residual (*rguess) is finite and
-// below the warm start's (scal[3]); scal[5] = *rguess, scal[6] = 1 if used
-void mpnn_gate(int64_t F, const double* guess, double* Z, const double* rguess, double* scal, cudaStream_t s);
+// base = polynomial extrapolation of order `order` (0..3) of Z0 (newest) .. Z3;
+// rhs on the Dirichlet rows
+void mpnn_extrapolate(int64_t F, int order, const double* Z0, const double* Z1, const double* Z2, const double* Z3,
+                      const uint8_t* fixed, const double* rhs, double* base, cudaStream_t s);
+// training target y = (Znew - base) / scal[10] (y may be null) and scal[8] =
+// rms(Znew - base) over the free rows; partials / counter: reduction scratch
+void mpnn_target(int64_t F, const double* Znew, const double* base, const uint8_t* fixed, double* scal, double* y,
+                 double* partials, uint32_t* counter, cudaStream_t s);
+// the gate: Z = the candidate with the lowest finite relative residual among
+// the warm start Z (scal[3]), base (scal[9]) and guess (*rguess; guess may be
+// null); scal[5] = *rguess, scal[6] = the choice (0 warm, 1 guess, 2 base)
+void mpnn_gate(int64_t F, const double* guess, const double* base, double* Z, const double* rguess, double* scal,
+               cudaStream_t s);
 void mpnn_features_from_host(int64_t F, const float* xf, __nv_bfloat16* x0, cudaStream_t s);
 void mpnn_out(const MpnnView& V, float* out, cudaStream_t s);
 

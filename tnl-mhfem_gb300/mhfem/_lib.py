@@ -38,10 +38,11 @@ FORM_FP64, FORM_MIXED, FORM_LEARNED = 0, 1, 2
 
 COEF_N, COEF_U, COEF_M, COEF_D, COEF_W, COEF_A, COEF_R, COEF_F, COEF_M_UPW, COEF_M_BND, COEF_PSI = range(11)
 ARRAY_B, ARRAY_R_IJKE, ARRAY_R_IK, ARRAY_M_UPW, ARRAY_Z_UPW, ARRAY_V, ARRAY_RHS, ARRAY_Z_IF, ARRAY_Z_IK = range(9)
-HOOK_PRE_ITERATE, HOOK_POST_ITERATE = 0, 1
+HOOK_PRE_ITERATE, HOOK_POST_ITERATE, HOOK_VECTOR_COEFFICIENTS = 0, 1, 2
 # void hook(void* user, double t, double tau, void* stream)
 HOOK = ct.CFUNCTYPE(None, ct.c_void_p, ct.c_double, ct.c_double, ct.c_void_p)
-KERNEL_CELL_LOCAL, KERNEL_ASSEMBLE, KERNEL_SPMV_FP64, KERNEL_SPMV_FP32, KERNEL_RECONSTRUCT = range(5)
+(KERNEL_CELL_LOCAL, KERNEL_ASSEMBLE, KERNEL_SPMV_FP64, KERNEL_SPMV_FP32, KERNEL_RECONSTRUCT, KERNEL_SPMV2_FP64,
+ KERNEL_UPDATE_S_FP64, KERNEL_UPDATE_XR_FP64, KERNEL_UPDATE_P_FP64) = range(9)
 
 
 class Desc(ct.Structure):
@@ -68,7 +69,7 @@ GMRES_CGS, GMRES_CGSR = 0, 1
 class LearnedOpts(ct.Structure):
     _fields_ = [("train_steps", ct.c_int32), ("train_iters", ct.c_int32), ("learning_rate", ct.c_double),
                 ("use_during_training", ct.c_int32), ("seed", ct.c_uint64), ("lr_final", ct.c_double),
-                ("mixed_solve", ct.c_int32)]
+                ("mixed_solve", ct.c_int32), ("extrapolation_order", ct.c_int32)]
 
 
 LEARNED_FEATURES = 16
@@ -78,7 +79,8 @@ class StepStats(ct.Structure):
     _fields_ = [("iterations", ct.c_int32), ("sweeps", ct.c_int32), ("residual", ct.c_double),
                 ("guess_used", ct.c_int32), ("guess_residual", ct.c_double), ("warm_residual", ct.c_double),
                 ("ms_pre", ct.c_double), ("ms_assemble", ct.c_double), ("ms_solve", ct.c_double),
-                ("ms_post", ct.c_double), ("ms_guess", ct.c_double)]
+                ("ms_post", ct.c_double), ("ms_guess", ct.c_double), ("base_residual", ct.c_double),
+                ("guess_source", ct.c_int32)]
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -116,6 +118,7 @@ SIGNATURES = [
     ("mhfem_get_state", ct.c_int32, [_P, _pd, _pd]),
     ("mhfem_get_array", ct.c_int32, [_P, ct.c_int32, _pd, ct.c_int64]),
     ("mhfem_get_system", ct.c_int32, [_P, _pi64, _pi32, _pd, _pd]),
+    ("mhfem_get_system32", ct.c_int32, [_P, ct.POINTER(ct.c_float)]),
     ("mhfem_get_totals", ct.c_int32, [_P, _pi64, _pi64, _pi64]),
     ("mhfem_get_stream", ct.c_int32, [_P, ct.POINTER(ct.c_void_p)]),
     ("mhfem_time_kernel", ct.c_int32, [_P, ct.c_int32, ct.c_int32, _pd, _pd, _pd]),
@@ -126,7 +129,7 @@ SIGNATURES = [
     ("mhfem_learned_gradients", ct.c_int32, [_P, ct.POINTER(ct.c_float), _pd, ct.POINTER(ct.c_float), _pd]),
     ("mhfem_learned_status", ct.c_int32, [_P, _pi32, _pd, _pi32]),
     ("mhfem_bicgstab_noalloc", ct.c_int32, [_P, _P, ct.c_int32, ct.c_int64, _P, _P, ct.c_double, ct.c_int32,
-                                            _pi32, _pd, _P]),
+                                            ct.c_double, _pi32, _pd, _P]),
 ]
 NOALLOC_MAX_ROWS = 262144
 

@@ -237,6 +237,14 @@ class Solver:
         self._ck(self.lib.mhfem_get_system(self._h, _i64ptr(rowptr), _i32ptr(cols), _dptr(vals), _dptr(rhs)))
         return rowptr, cols, vals, rhs
 
+    def system32(self) -> np.ndarray:
+        """The FP32 copy of the matrix values (mixed form), CSR order of system()."""
+        nnz = ct.c_int64()
+        self._ck(self.lib.mhfem_get_sizes(self._h, None, None, None, None, ct.byref(nnz)))
+        out = np.empty(nnz.value, np.float32)
+        self._ck(self.lib.mhfem_get_system32(self._h, out.ctypes.data_as(ct.POINTER(ct.c_float))))
+        return out
+
     def totals(self):
         """(Krylov iterations, time steps, kernel launches) since creation."""
         it = ct.c_int64(); ts = ct.c_int64(); kl = ct.c_int64()
@@ -244,10 +252,13 @@ class Solver:
         return it.value, ts.value, kl.value
 
     def set_hook(self, point: int, fn) -> None:
-        """Model hook: fn(t, tau, stream) is called at `point` (HOOK_PRE_ITERATE:
-        before upwinding and the cell kernel; HOOK_POST_ITERATE: after the
-        reconstruction) with the library's stream, on which its device work
-        must be ordered.  None removes it."""
+        """Model hook: fn(t, tau, stream) is called at `point` with the
+        library's stream, on which its device work must be ordered.
+        HOOK_PRE_ITERATE (updateNonLinearTerms): before this step's b update;
+        HOOK_VECTOR_COEFFICIENTS (updateVectorCoefficients): after the b
+        update, before upwinding, so u, w, a projections may read this step's
+        b (and a model rewrites its boundary mobility m_bnd here);
+        HOOK_POST_ITERATE: after the reconstruction.  None removes it."""
         if not hasattr(self, "_hooks"):
             self._hooks = {}
         if fn is None:
@@ -284,9 +295,9 @@ class Solver:
     # -- learned warm start (MHFEM_FORM_LEARNED) ------------------------
     def learned_options(self, train_steps: int = 200, train_iters: int = 2, learning_rate: float = 1e-3,
                         use_during_training: bool = False, seed: int = 0, lr_final: float = 1.0,
-                        mixed_solve: bool = False) -> None:
+                        mixed_solve: bool = False, extrapolation_order: int = 3) -> None:
         o = L.LearnedOpts(train_steps, train_iters, learning_rate, int(use_during_training), seed, lr_final,
-                          int(mixed_solve))
+                          int(mixed_solve), extrapolation_order)
         self._ck(self.lib.mhfem_learned_set_options(self._h, ct.byref(o)))
 
     def learned_num_params(self) -> int:
