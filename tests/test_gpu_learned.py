@@ -200,3 +200,36 @@ def test_learned_guess_with_mixed_solve():
     assert np.mean(inner_l) < np.mean(inner_m), (np.mean(inner_l), np.mean(inner_m))
     for s in (sm, smx, sf):
         s.close()
+
+
+def test_network_gain_over_the_extrapolation_alone():
+    """What the trained network adds to the method without it: on the linear
+    extrapolation base (2 Zn - Zn1, the previous two traces) the network's
+    correction wins the gate in some steps after training and the solves
+    need no more iterations than with the base alone.  (On the cubic base
+    the extrapolation is so close that the network's correction rarely wins;
+    the benchmark reports both.)"""
+    N, train, use = 12, 40, 20
+    src = (0.5, 60 * 1e-3)
+    runs = {}
+    for name, train_steps in (("net", train), ("base_only", 0)):
+        p = problems.diffusion3d_source(N=N, steps=train + use, form=L.FORM_LEARNED)
+        p.source = src
+        s = problems.make_solver(p)
+        s.learned_options(train_steps=train_steps, train_iters=4, learning_rate=2e-3, extrapolation_order=1)
+        its, won = [], 0
+        t = 0.0
+        for k in range(train + use):
+            st = s.step(t, p.dt)
+            if k >= 1:
+                _assert_gate_picked_the_lowest_residual(st)
+            if k >= train:
+                its.append(st["iterations"])
+                won += st["guess_source"] == 1
+            t += p.dt
+        runs[name] = (np.mean(its), won, s.state()[0])
+        s.close()
+    assert runs["base_only"][1] == 0
+    assert runs["net"][1] >= 1, runs["net"][:2]
+    assert runs["net"][0] <= runs["base_only"][0] + 1.0, (runs["net"][0], runs["base_only"][0])
+    assert rel_err(runs["net"][2], runs["base_only"][2]) < 1e-7

@@ -9,7 +9,8 @@
 //   3. once the network is trained: guess = base + c * net(features), c the
 //      size of the base's error in the previous step;
 //   4. of the warm start, the base and the guess, the one with the lowest
-//      relative residual ||b - A x|| / ||b|| starts the solve;
+//      relative residual ||b - A x|| / ||b|| starts the solve (a network that
+//      keeps losing this comparison is run only every few steps);
 //   5. the FP64 BiCGStab runs to the same tolerance as the plain form, so the
 //      initial guess can only change the iteration count;
 //   6. during the first `train_steps` steps the network is trained online
@@ -59,6 +60,7 @@ struct LearnedState {
     double* host = nullptr;  // pinned: scales, residuals, loss
     int32_t* err = nullptr;
     int hist = 0;
+    int net_losses = 0;   // consecutive steps whose network guess lost the gate
     int trained_steps = 0;
     int adam_t = 0;
     bool params_set = false;
@@ -79,6 +81,12 @@ struct LearnedState {
 namespace {
 
 constexpr int H = kMpnnHidden;
+// After kNetBackoff consecutive steps in which the network's guess lost the
+// gate (the extrapolated base or the warm start was closer), the network is
+// run only every kNetRetry-th step until it wins again: its inference costs
+// about as much as ten FP64 iterations on the 64^3 workload.
+constexpr int kNetBackoff = 4;
+constexpr int kNetRetry = 16;
 
 int off_W(int l) { return l == 0 ? 0 : kMpnnFeatures * H + H + (l - 1) * (2 * H * H + H); }
 int off_b(int l) { return off_W(l) + (l == 0 ? kMpnnFeatures : 2 * H) * H; }
@@ -195,7 +203,10 @@ void learned_invalidate(mhfem_t h)
 
 void learned_reset_history(mhfem_t h)
 {
-    if (h->learned) h->learned->hist = 0;
+    if (h->learned) {
+        h->learned->hist = 0;
+        h->learned->net_losses = 0;
+    }
 }
 
 void learned_release(mhfem_t h)
@@ -399,7 +410,9 @@ mhfem_status learned_solve(mhfem_t h, int* iters, int* sweeps, double* res, mhfe
     LCK(cudaMemcpyAsync(Zn, h->Z_iF, sizeof(double) * F, cudaMemcpyDeviceToDevice, s));
     const bool have_hist = L->hist >= 1;
     const bool training = L->trained_steps < L->train_steps;
-    const bool infer = have_hist && (!training || L->use_during_training) && (L->trained_steps > 0 || L->params_loaded);
+    const bool backed_off = L->net_losses >= kNetBackoff && (L->hist % kNetRetry) != 0;
+    const bool infer = have_hist && (!training || L->use_during_training) && (L->trained_steps > 0 || L->params_loaded) &&
+                       !backed_off;
     MpnnInputs in{};
     in.Zn = Zn;
     in.Zn1 = Zprev[0];
@@ -470,6 +483,7 @@ mhfem_status learned_solve(mhfem_t h, int* iters, int* sweeps, double* res, mhfe
         r_guess = guessed ? L->host[5] : -1;
         r_base = L->host[9];
         source = (int)L->host[6];
+        if (guessed) L->net_losses = (source == 1) ? 0 : L->net_losses + 1;
         // the base's error in this step (and, while training, the target scaled by this step's c)
         const bool train_now = training && have_features;
         mpnn_target(F, h->Z_iF, L->base, L->fixed, L->scal, train_now ? L->target : nullptr, h->W.partials,
@@ -570,6 +584,7 @@ mhfem_status mhfem_learned_set_params(mhfem_t h, const float* params, int64_t co
     LCK(cudaStreamSynchronize(h->stream));
     L->params_set = true;
     L->params_loaded = true;
+    L->net_losses = 0;
     return MHFEM_OK;
 }
 
