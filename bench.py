@@ -635,7 +635,7 @@ def profile_other_form(args, dev):
                 gmres_variant="cgs")
     t = 0.0
     if args.profile_form == "learned":
-        s.learned_options(train_steps=args.learned_train, train_iters=4, learning_rate=3e-3)
+        s.learned_options(train_steps=args.learned_train, train_iters=args.learned_iters, learning_rate=3e-3)
         for _ in range(args.learned_train):
             s.step(t, p.dt)
             t += p.dt
