@@ -4,8 +4,9 @@ A numpy restatement of the message-passing network the GPU trains and runs
 with tcgen05 BF16 kernels, used only by tests/ to check the GPU forward pass
 and gradients.  It evaluates in FP64; with ``bf16=True`` it rounds to BF16
 at exactly the points where the GPU stores BF16 (features, weights, hidden
-states, neighbour means, pre-activations), so the remaining difference is the
-GPU's FP32 accumulation order.
+states, neighbour means, pre-activations, and in the backward pass dZ and the
+per-face neighbour-mean gradients), so the remaining difference is the GPU's
+FP32 accumulation order.
 
 Network (hidden width H = 64), per face E with neighbour set N(E) (the faces
 sharing a cell with E, i.e. the off-diagonal pattern of the face system):
@@ -112,7 +113,7 @@ def loss_and_grads(p: dict, x, nbr, deg, y, mask, bf: bool = True):
         g[f"b{l}"] = dz.sum(axis=0)
         dx = dzr @ r(p[f"W{l}"]).T
         dself, da = dx[:, :H], dx[:, H:]
-        dh = dh + dself + neighbour_sum_transpose(da / np.maximum(deg, 1)[:, None], nbr)
+        dh = dh + dself + neighbour_sum_transpose(r(da / np.maximum(deg, 1)[:, None]), nbr)
     dz0 = dh * (c["z0"] > 0)
     g["W0"] = c["x"].T @ r(dz0)
     g["b0"] = dz0.sum(axis=0)

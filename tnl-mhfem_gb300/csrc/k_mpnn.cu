@@ -18,12 +18,13 @@
 //    (M=128, N=64, K=16) into a 64-column TMEM accumulator; the epilogue
 //    (tcgen05.ld, bias, ReLU, residual) writes h_{l+1} in BF16.
 //  - k_mpnn_bwd_dx: dX = dZ W^T (M=128, N=128, K=64) with dZ = dH * (Z > 0)
-//    formed while staging; writes dH_self + dH_next and the scaled
-//    neighbour gradient.
+//    formed while staging (dH gathers the layer above's neighbour
+//    gradients there); writes dH_self + dH_next and the scaled neighbour
+//    gradient (BF16).
 //  - k_mpnn_bwd_dw: dW = X^T dZ, split over faces: each CTA accumulates its
 //    faces' contribution in TMEM (M=128 features, N=64, K=128 faces per
 //    tile) and writes one FP32 partial; partials are summed in a fixed order.
-//  - gather/transpose, decode + loss, Adam: CUDA-core kernels.
+//  - decode + loss, the encoder's dZ, Adam: CUDA-core kernels.
 #include <cuda_bf16.h>
 
 #include "mhfem_internal.h"
@@ -385,8 +386,14 @@ __global__ void __launch_bounds__(256) k_mpnn_decode(const MpnnView V, const dou
 
 // A = dZ (128 x 64) with dZ = dH * (Z > 0), B = W_in (128 x 64: row k = input k).
 // Thread (r, qs) stages and finishes columns 16 qs .. 16 qs + 15 of row r.
-// Epilogue: dH += dX[:, :64] (residual + self path), ga = dX[:, 64:] / deg.
-__global__ void __launch_bounds__(NT) k_mpnn_bwd_dx(const MpnnView V, int layer)
+// dH of layer l + 1 is the stored partial dH (the residual and self paths)
+// plus, below the top layer, the transpose of the neighbour mean of layer
+// l + 1: the sum over the neighbours E' of g_{l+1}(E') (the adjacency is
+// symmetric), gathered here while staging instead of in a pass of its own.
+// The thread keeps its 16 values of dH in registers across the MMA.
+// Epilogue: dH_l = dH + dX[:, :64], g_l = dX[:, 64:] / deg (BF16, into the
+// other of the two g buffers: layer l reads g[(l + 1) % 2], writes g[l % 2]).
+__global__ void __launch_bounds__(NT, 2) k_mpnn_bwd_dx(const MpnnView V, int layer)
 {
     extern __shared__ __align__(128) uint8_t smem[];
     uint8_t* sA = smem;               // 128 x 64
@@ -396,6 +403,9 @@ __global__ void __launch_bounds__(NT) k_mpnn_bwd_dx(const MpnnView V, int layer)
     const int tid = threadIdx.x, warp = tid >> 5;
     const int r = tid & (TB - 1), qs = tid >> 7;
     const int64_t F = V.F;
+    const bool gather = layer < kMpnnLayers;
+    const __nv_bfloat16* gin = V.gb[(layer + 1) & 1];
+    __nv_bfloat16* gout = V.gb[layer & 1];
     const __nv_bfloat16* Wb = V.w_bwd[layer];  // [128][64]
     for (int idx = tid; idx < 2 * H * H / 8; idx += NT) {
         const int rr = idx / (H / 8), k0 = (idx % (H / 8)) * 8;
@@ -413,20 +423,57 @@ __global__ void __launch_bounds__(NT) k_mpnn_bwd_dx(const MpnnView V, int layer)
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t row = tile * TB + r;
         const bool valid = row < F;
+        float dhv[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) dhv[q] = 0.f;
+        if (valid) {
+            const float* src = V.dh + row * H + 16 * qs;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const float4 d = *reinterpret_cast<const float4*>(src + 4 * c);
+                dhv[4 * c] = d.x; dhv[4 * c + 1] = d.y; dhv[4 * c + 2] = d.z; dhv[4 * c + 3] = d.w;
+            }
+            if (gather) {
+                int32_t nb[kMpnnMaxWidth];
+#pragma unroll
+                for (int k = 0; k < kMpnnMaxWidth; ++k) {
+                    const int32_t e = (k < V.W) ? __ldg(V.nbr + (int64_t)k * F + row) : (int32_t)row;
+                    nb[k] = (e == (int32_t)row) ? -1 : e;
+                }
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    uint4 g[kMpnnMaxWidth];
+#pragma unroll
+                    for (int k = 0; k < kMpnnMaxWidth; ++k)
+                        g[k] = nb[k] >= 0 ? __ldg(reinterpret_cast<const uint4*>(gin + (int64_t)nb[k] * H + 16 * qs + 8 * c))
+                                          : make_uint4(0, 0, 0, 0);
+#pragma unroll
+                    for (int k = 0; k < kMpnnMaxWidth; ++k) {
+                        const uint32_t w4[4] = {g[k].x, g[k].y, g[k].z, g[k].w};
+#pragma unroll
+                        for (int t = 0; t < 4; ++t) {
+                            const float2 f = unpack_bf16(w4[t]);
+                            dhv[8 * c + 2 * t] += f.x;
+                            dhv[8 * c + 2 * t + 1] += f.y;
+                        }
+                    }
+                }
+            }
+        }
 #pragma unroll
         for (int c = 0; c < 2; ++c) {
             const int col = 16 * qs + 8 * c;
             uint4 out = make_uint4(0, 0, 0, 0);
             if (valid) {
-                const float4 d0 = *reinterpret_cast<const float4*>(V.dh + row * H + col);
-                const float4 d1 = *reinterpret_cast<const float4*>(V.dh + row * H + col + 4);
                 const uint4 zz = *reinterpret_cast<const uint4*>(V.z[layer] + row * H + col);
-                const float2 z0 = unpack_bf16(zz.x), z1 = unpack_bf16(zz.y), z2 = unpack_bf16(zz.z),
-                             z3 = unpack_bf16(zz.w);
-                out.x = pack_bf16(z0.x > 0 ? d0.x : 0.f, z0.y > 0 ? d0.y : 0.f);
-                out.y = pack_bf16(z1.x > 0 ? d0.z : 0.f, z1.y > 0 ? d0.w : 0.f);
-                out.z = pack_bf16(z2.x > 0 ? d1.x : 0.f, z2.y > 0 ? d1.y : 0.f);
-                out.w = pack_bf16(z3.x > 0 ? d1.z : 0.f, z3.y > 0 ? d1.w : 0.f);
+                const uint32_t zw[4] = {zz.x, zz.y, zz.z, zz.w};
+                uint32_t ow[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const float2 z2 = unpack_bf16(zw[t]);
+                    ow[t] = pack_bf16(z2.x > 0 ? dhv[8 * c + 2 * t] : 0.f, z2.y > 0 ? dhv[8 * c + 2 * t + 1] : 0.f);
+                }
+                out = make_uint4(ow[0], ow[1], ow[2], ow[3]);
                 *reinterpret_cast<uint4*>(V.dz + row * H + col) = out;
             }
             st_tile(sA, r, col, H, out);
@@ -440,21 +487,21 @@ __global__ void __launch_bounds__(NT) k_mpnn_bwd_dx(const MpnnView V, int layer)
         if (valid) {
             float* dh = V.dh + row * H + 16 * qs;
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                float4 v = *reinterpret_cast<float4*>(dh + 4 * c);
-                v.x += acc[4 * c]; v.y += acc[4 * c + 1]; v.z += acc[4 * c + 2]; v.w += acc[4 * c + 3];
-                *reinterpret_cast<float4*>(dh + 4 * c) = v;
-            }
+            for (int c = 0; c < 4; ++c)
+                *reinterpret_cast<float4*>(dh + 4 * c) =
+                    make_float4(dhv[4 * c] + acc[4 * c], dhv[4 * c + 1] + acc[4 * c + 1], dhv[4 * c + 2] + acc[4 * c + 2],
+                                dhv[4 * c + 3] + acc[4 * c + 3]);
         }
         tc::tmem_ld_x16(tlane + H + 16 * qs, acc);
         if (valid) {
             const int d = V.deg[row];
             const float inv = d > 0 ? 1.0f / (float)d : 0.f;
-            float* ga = V.ga + row * H + 16 * qs;
+            uint32_t w[8];
 #pragma unroll
-            for (int c = 0; c < 4; ++c)
-                *reinterpret_cast<float4*>(ga + 4 * c) =
-                    make_float4(acc[4 * c] * inv, acc[4 * c + 1] * inv, acc[4 * c + 2] * inv, acc[4 * c + 3] * inv);
+            for (int t = 0; t < 8; ++t) w[t] = pack_bf16(acc[2 * t] * inv, acc[2 * t + 1] * inv);
+            uint4* g = reinterpret_cast<uint4*>(gout + row * H + 16 * qs);
+            g[0] = make_uint4(w[0], w[1], w[2], w[3]);
+            g[1] = make_uint4(w[4], w[5], w[6], w[7]);
         }
         tile_done();
     }
@@ -462,42 +509,44 @@ __global__ void __launch_bounds__(NT) k_mpnn_bwd_dx(const MpnnView V, int layer)
     if (warp == 0) tc::tmem_dealloc(tbase, 2 * H);
 }
 
-// dH[E] += sum_{E' in N(E)} ga[E'] (the adjacency is symmetric, so this is
-// the transpose of the neighbour mean).  16 threads per face, 4 columns each.
-__global__ void __launch_bounds__(256) k_mpnn_gather_add(const MpnnView V)
-{
-    const int64_t gid = (int64_t)blockIdx.x * 256 + threadIdx.x;
-    const int64_t row = gid >> 4;
-    const int c = (int)(gid & 15) * 4;
-    if (row >= V.F) return;
-    int32_t nb[kMpnnMaxWidth];
-#pragma unroll
-    for (int k = 0; k < kMpnnMaxWidth; ++k) {
-        const int32_t e = (k < V.W) ? __ldg(V.nbr + (int64_t)k * V.F + row) : (int32_t)row;
-        nb[k] = (e == (int32_t)row) ? -1 : e;
-    }
-    float4 g[kMpnnMaxWidth];
-#pragma unroll
-    for (int k = 0; k < kMpnnMaxWidth; ++k)
-        g[k] = (nb[k] >= 0) ? __ldg(reinterpret_cast<const float4*>(V.ga + (int64_t)nb[k] * H + c))
-                            : make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 s = *reinterpret_cast<const float4*>(V.dh + row * H + c);
-#pragma unroll
-    for (int k = 0; k < kMpnnMaxWidth; ++k) {
-        s.x += g[k].x; s.y += g[k].y; s.z += g[k].z; s.w += g[k].w;
-    }
-    *reinterpret_cast<float4*>(V.dh + row * H + c) = s;
-}
-
-
-// dz0 = dh * (z0 > 0) in BF16 (encoder)
+// Encoder: dz0 = dH_1 * (z0 > 0) in BF16, with dH_1 = the stored dH plus the
+// neighbour sum of g_1 (as in k_mpnn_bwd_dx).  One thread per 8 columns of a face.
 __global__ void __launch_bounds__(256) k_mpnn_dz0(const MpnnView V)
 {
     const int64_t gid = (int64_t)blockIdx.x * 256 + threadIdx.x;
-    if (gid >= V.F * (H / 2)) return;
-    const float2 d = *reinterpret_cast<const float2*>(V.dh + 2 * gid);
-    const float2 z = unpack_bf16(*reinterpret_cast<const uint32_t*>(V.z[0] + 2 * gid));
-    *reinterpret_cast<uint32_t*>(V.dz + 2 * gid) = pack_bf16(z.x > 0 ? d.x : 0.f, z.y > 0 ? d.y : 0.f);
+    const int64_t row = gid >> 3;
+    const int col = (int)(gid & 7) * 8;
+    if (row >= V.F) return;
+    const __nv_bfloat16* gin = V.gb[1 & 1];  // written by layer 1
+    float d[8];
+    const float4 d0 = *reinterpret_cast<const float4*>(V.dh + row * H + col);
+    const float4 d1 = *reinterpret_cast<const float4*>(V.dh + row * H + col + 4);
+    d[0] = d0.x; d[1] = d0.y; d[2] = d0.z; d[3] = d0.w; d[4] = d1.x; d[5] = d1.y; d[6] = d1.z; d[7] = d1.w;
+    uint4 g[kMpnnMaxWidth];
+#pragma unroll
+    for (int k = 0; k < kMpnnMaxWidth; ++k) {
+        const int32_t e = (k < V.W) ? __ldg(V.nbr + (int64_t)k * V.F + row) : (int32_t)row;
+        g[k] = e != (int32_t)row ? __ldg(reinterpret_cast<const uint4*>(gin + (int64_t)e * H + col)) : make_uint4(0, 0, 0, 0);
+    }
+#pragma unroll
+    for (int k = 0; k < kMpnnMaxWidth; ++k) {
+        const uint32_t w4[4] = {g[k].x, g[k].y, g[k].z, g[k].w};
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const float2 f = unpack_bf16(w4[t]);
+            d[2 * t] += f.x;
+            d[2 * t + 1] += f.y;
+        }
+    }
+    const uint4 zz = *reinterpret_cast<const uint4*>(V.z[0] + row * H + col);
+    const uint32_t zw[4] = {zz.x, zz.y, zz.z, zz.w};
+    uint32_t o[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        const float2 z2 = unpack_bf16(zw[t]);
+        o[t] = pack_bf16(z2.x > 0 ? d[2 * t] : 0.f, z2.y > 0 ? d[2 * t + 1] : 0.f);
+    }
+    *reinterpret_cast<uint4*>(V.dz + row * H + col) = make_uint4(o[0], o[1], o[2], o[3]);
 }
 
 // ---- backward: dW = X^T dZ (split over faces) -----------------------------------
@@ -780,15 +829,13 @@ void mpnn_backward(const MpnnView& V, const double* target, double inv_nt, MpnnG
     const int gdx = resident_grid(k_mpnn_bwd_dx, smdx, V.F);
     const int gdw = resident_grid(k_mpnn_bwd_dw<128>, smdw, V.F);
     const int gdw0 = resident_grid(k_mpnn_bwd_dw<16>, smdw, V.F);
-    const unsigned gadd = (unsigned)((V.F * 16 + 255) / 256);
     for (int l = kMpnnLayers; l >= 1; --l) {
         k_mpnn_bwd_dx<<<gdx, NT, smdx, s>>>(V, l);
         k_mpnn_bwd_dw<128><<<gdw, NT, smdw, s>>>(V, l, G.partials);
         k_mpnn_reduce_dw<<<(2 * H * H + H + 255) / 256, 256, 0, s>>>(G.partials, gdw, 2 * H, G.g + G.off_W[l],
                                                                       G.g + G.off_b[l]);
-        k_mpnn_gather_add<<<gadd, 256, 0, s>>>(V);
     }
-    k_mpnn_dz0<<<(unsigned)((V.F * (H / 2) + 255) / 256), 256, 0, s>>>(V);
+    k_mpnn_dz0<<<(unsigned)((V.F * (H / 8) + 255) / 256), 256, 0, s>>>(V);
     k_mpnn_bwd_dw<16><<<gdw0, NT, smdw, s>>>(V, 0, G.partials);
     k_mpnn_reduce_dw<<<(16 * H + H + 255) / 256, 256, 0, s>>>(G.partials, gdw0, 16, G.g + G.off_W[0],
                                                               G.g + G.off_b[0]);

@@ -40,7 +40,7 @@ struct LearnedState {
     __nv_bfloat16* z[kMpnnLayers + 1] = {};
     __nv_bfloat16* dz = nullptr;
     float* dh = nullptr;
-    float* ga = nullptr;
+    __nv_bfloat16* gb[2] = {};
     float* params = nullptr;
     float* grads = nullptr;
     float* m1 = nullptr;
@@ -155,7 +155,8 @@ MpnnView make_view(mhfem_t h)
     }
     V.dz = L->dz;
     V.dh = L->dh;
-    V.ga = L->ga;
+    V.gb[0] = L->gb[0];
+    V.gb[1] = L->gb[1];
     V.wd = L->params + off_wd();
     V.bd = L->params + off_bd();
     V.dec_partials = L->dec_partials;
@@ -327,7 +328,7 @@ static mhfem_status learned_prepare(mhfem_t h)
     for (int l = 0; l <= kMpnnLayers; ++l) LCK(lalloc(L, &L->z[l], (size_t)F * H));
     LCK(lalloc(L, &L->dz, (size_t)F * H));
     LCK(lalloc(L, &L->dh, (size_t)F * H));
-    LCK(lalloc(L, &L->ga, (size_t)F * H));
+    for (auto& g : L->gb) LCK(lalloc(L, &g, (size_t)F * H));
     LCK(lalloc(L, &L->params, kMpnnParams));
     LCK(lalloc(L, &L->grads, kMpnnParams));
     LCK(lalloc(L, &L->m1, kMpnnParams));
@@ -391,7 +392,7 @@ static mhfem_status train_once(mhfem_t h, int iters)
         L->adam_t += 1;
         mpnn_adam(L->params, L->grads, L->m1, L->m2, kMpnnParams, lr, L->adam_t, h->stream);
         publish(h);
-        h->launches += 4 + 2 + 4 * kMpnnLayers + 3 + 1 + 4;
+        h->launches += 4 + 2 + 3 * kMpnnLayers + 3 + 1 + 4;
     }
     LCK(cudaMemcpyAsync(&L->host[4], L->loss, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     LCK(cudaGetLastError());

@@ -32,7 +32,7 @@ struct MpnnView {
     __nv_bfloat16* z[kMpnnLayers + 1] = {};  // z[0..3] [F][64] (training)
     __nv_bfloat16* dz = nullptr;      // [F][64]
     float* dh = nullptr;              // [F][64]
-    float* ga = nullptr;              // [F][64]
+    __nv_bfloat16* gb[2] = {};        // [F][64] each: neighbour-mean gradients, layer l writes gb[l % 2]
     const __nv_bfloat16* w_fwd[kMpnnLayers + 1] = {};  // [64][K_l]
     const __nv_bfloat16* w_bwd[kMpnnLayers + 1] = {};  // [K_l][64]
     const float* bias[kMpnnLayers + 1] = {};           // [64]
