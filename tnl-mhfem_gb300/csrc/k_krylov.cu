@@ -119,17 +119,25 @@ __device__ __forceinline__ void spmv_rows(const int32_t* __restrict__ cols, cons
 // (grid-stride sequence) before gathering for the current group, so the two
 // memory round trips of a row (ELL entries, then the gathered x) overlap
 // with the neighbouring group's.  It doubles the registers that hold ELL
-// entries, so it pays where latency, not the FP64 pipe, bounds the kernel
+// entries (40 -> 64 for the FP64 width-6 SpMVs: 4 instead of 6 CTAs per
+// SM), and pays where latency, not the FP64 pipe, bounds the kernel
 // (measured on GB300):
 //  - FP64, width 10 (cuboids): 172.8 against 198.9 us per launch on 6.3M rows
 //    (79% against 69% of HBM);
+//  - FP64, width 6 (tetrahedra, 3.17M rows), once the block reductions left
+//    the FP64 pipe (block_reduce_store): second SpMV 54.6 against 57.1 us,
+//    the whole in-step iteration 172.7 against 179.4 us (the first SpMV
+//    alone 53.4 against 53.0 us); before that change the plain loop was
+//    faster (58.2 against 60.2 us).  With the first row's ELL words loaded
+//    before the dependency wait (as in the plain loop): 52.3 and 53.0 us,
+//    iteration 171.2 us;
 //  - FP32, 4 rows per thread (the mixed form's inner solve, tetrahedra):
-//    5.37 against 4.87 TB/s, mixed form 1.69x against 1.59x the FP64 form;
-//  - FP64, width 6 (tetrahedra): slower (60.2 against 58.2 us), kept plain.
+//    5.37 against 4.87 TB/s, mixed form 1.69x against 1.59x the FP64 form.
 template <typename T>
 constexpr bool spmv_pipelined(int WW, int RPT)
 {
-    return (sizeof(T) == 8 && RPT == 1 && WW == 10) || (sizeof(T) == 4 && RPT == 4 && (WW == 4 || WW == 6));
+    return (sizeof(T) == 8 && RPT == 1 && (WW == 10 || WW == 6)) ||
+           (sizeof(T) == 4 && RPT == 4 && (WW == 4 || WW == 6));
 }
 
 // RPT consecutive rows of the ELL matrix (one 16-byte word per slot when RPT > 1)
@@ -193,7 +201,7 @@ __device__ __forceinline__ void ell_apply(const EllRows<T, WW, RPT>& e, const T*
 // done; a phase calls it exactly once, before it touches the previous
 // kernel's outputs or the scalars.
 
-// v = A p ; acc = (rh, v).  The FP64 plain loop loads the ELL words of its
+// v = A p ; acc = (rh, v).  The FP64 loops load the ELL words of their
 // first row before gate(); the pipelined FP32 loop starts after it.
 template <typename T, int WW, int RPT, typename Gate>
 __device__ __forceinline__ bool phase_spmv_dot(const int32_t* cols, const T* vals, int W, int64_t rows,
@@ -211,10 +219,13 @@ __device__ __forceinline__ bool phase_spmv_dot(const int32_t* cols, const T* val
         for (int j = 0; j < RPT; ++j) acc[0] = fma(h.v[j], y[j], acc[0]);
     };
     if constexpr (spmv_pipelined<T>(WW, RPT)) {
-        if (!gate()) return false;
         int64_t q = gtid;
         EllRows<T, WW, RPT> cur;
-        if (q < ng) ell_load<T, WW, RPT>(cols, vals, rows, q, cur);
+        if constexpr (sizeof(T) == 8)
+            if (q < ng) ell_load<T, WW, RPT>(cols, vals, rows, q, cur);
+        if (!gate()) return false;
+        if constexpr (sizeof(T) == 4)
+            if (q < ng) ell_load<T, WW, RPT>(cols, vals, rows, q, cur);
         for (; q < ng; q += gstride) {
             EllRows<T, WW, RPT> nxt;
             const int64_t qn = q + gstride;
@@ -315,7 +326,7 @@ __device__ __forceinline__ void phase_update_s(int64_t rows, const T* r, const T
 }
 
 // t = A s ; acc = (t, s), (t, t) and, on a check iteration, (s, s).  The
-// FP64 plain loop loads the ELL words of its first row before gate().
+// FP64 loops load the ELL words of their first row before gate().
 template <typename T, int WW, int RPT, bool CHECK, typename Gate>
 __device__ __forceinline__ bool phase_spmv_dots2(const int32_t* cols, const T* vals, int W, int64_t rows,
                                                  const T* s, T* t, int64_t gtid, int64_t gstride,
@@ -334,10 +345,13 @@ __device__ __forceinline__ bool phase_spmv_dots2(const int32_t* cols, const T* v
         stv<T, RPT>(t, q, yv);
     };
     if constexpr (spmv_pipelined<T>(WW, RPT)) {
-        if (!gate()) return false;
         int64_t q = gtid;
         EllRows<T, WW, RPT> cur;
-        if (q < ng) ell_load<T, WW, RPT>(cols, vals, rows, q, cur);
+        if constexpr (sizeof(T) == 8)
+            if (q < ng) ell_load<T, WW, RPT>(cols, vals, rows, q, cur);
+        if (!gate()) return false;
+        if constexpr (sizeof(T) == 4)
+            if (q < ng) ell_load<T, WW, RPT>(cols, vals, rows, q, cur);
         for (; q < ng; q += gstride) {
             EllRows<T, WW, RPT> nxt;
             const int64_t qn = q + gstride;
@@ -701,8 +715,10 @@ void krylov_init_fp64(const EllMatrix& A, const double* b, double* x, KrylovWork
                                               W.r, W.rh, W.p, W.sc, W.partials, W.counters)));
 }
 
-// The FP64 SpMV keeps one row per thread: it is bound by the FP64 pipe as
-// much as by HBM, and more rows per thread only lower the occupancy.
+// The FP64 SpMV keeps one row per thread (pipelined for the widths 6 and
+// 10): it is bound by the FP64 pipe as much as by HBM.  Two rows per thread
+// with 16-byte ELL loads (plain loop) measured 175.2 us per iteration on the
+// 64^3 workload, against 171.2 us for the pipelined single row.
 void krylov_iterate_fp64(const EllMatrix& A, double* x, KrylovWork& W, int iters, cudaStream_t s)
 {
     if (vec_ok<double>({x, W.r, W.rh, W.p, W.v, W.s, W.t}))

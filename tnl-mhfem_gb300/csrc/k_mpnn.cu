@@ -385,23 +385,42 @@ __global__ void __launch_bounds__(256) k_mpnn_decode(const MpnnView V, const dou
 // ---- backward: dX = dZ W^T ------------------------------------------------------
 
 // A = dZ (128 x 64) with dZ = dH * (Z > 0), B = W_in (128 x 64: row k = input k).
-// Thread (r, qs) stages and finishes columns 16 qs .. 16 qs + 15 of row r.
 // dH of layer l + 1 is the stored partial dH (the residual and self paths)
 // plus, below the top layer, the transpose of the neighbour mean of layer
 // l + 1: the sum over the neighbours E' of g_{l+1}(E') (the adjacency is
 // symmetric), gathered here while staging instead of in a pass of its own.
-// The thread keeps its 16 values of dH in registers across the MMA.
 // Epilogue: dH_l = dH + dX[:, :64], g_l = dX[:, 64:] / deg (BF16, into the
 // other of the two g buffers: layer l reads g[(l + 1) % 2], writes g[l % 2]).
+//
+// Global traffic is row-coalesced, as in the forward layer: thread
+// (slot, c8) = (t / 8, t % 8) moves columns 4 c8 .. 4 c8 + 3 and
+// 32 + 4 c8 .. 32 + 4 c8 + 3 of rows slot and slot + 64, so the eight lanes
+// of a row cover 128 contiguous bytes of its FP32 dH row per load (64 of a
+// BF16 row), and a warp instruction touches four rows -- for the neighbour
+// gather too.  (A row per thread made every instruction touch 32 rows,
+// which bound the kernel by L1 wavefronts at about a third of HBM.)  The
+// thread keeps its 16 dH values in registers across the MMA.  The TMEM
+// epilogue is row-per-thread ((r, qs) = (t % 128, t / 128); warp % 4 is the
+// TMEM lane quarter), so it passes dX through shared memory: the FP32 half
+// into sD, the scaled BF16 neighbour half into the A tile's space (the MMA
+// has read it by then), both with 16-byte chunks XOR-swizzled by row % 8 so
+// the row-per-thread stores and the row-coalesced loads are free of bank
+// conflicts.
+constexpr int kDxSmem = (TB + 2 * H) * H * 2 + TB * H * 4;  // A, B tiles (BF16) + FP32 dX staging
+
+__device__ __forceinline__ int swz(int r, int chunk) { return chunk ^ (r & 7); }
+
 __global__ void __launch_bounds__(NT, 2) k_mpnn_bwd_dx(const MpnnView V, int layer)
 {
     extern __shared__ __align__(128) uint8_t smem[];
-    uint8_t* sA = smem;               // 128 x 64
-    uint8_t* sB = smem + TB * H * 2;  // 128 x 64
+    uint8_t* sA = smem;                                                   // 128 x 64 BF16: dZ, then g
+    uint8_t* sB = smem + TB * H * 2;                                      // 128 x 64 BF16: W_in
+    float* sD = reinterpret_cast<float*>(smem + (TB + 2 * H) * H * 2);   // 128 x 64 FP32: dX[:, :64]
     __shared__ uint64_t mbar;
     __shared__ uint32_t tbase;
     const int tid = threadIdx.x, warp = tid >> 5;
-    const int r = tid & (TB - 1), qs = tid >> 7;
+    const int r = tid & (TB - 1), qs = tid >> 7;  // epilogue mapping
+    const int c8 = tid & 7, slot = tid >> 3;      // row-coalesced mapping
     const int64_t F = V.F;
     const bool gather = layer < kMpnnLayers;
     const __nv_bfloat16* gin = V.gb[(layer + 1) & 1];
@@ -420,88 +439,112 @@ __global__ void __launch_bounds__(NT, 2) k_mpnn_bwd_dx(const MpnnView V, int lay
     const uint32_t tlane = tbase + ((uint32_t)(32 * (warp & 3)) << 16);
     TileSync ts{&mbar, 0};
     const int64_t ntiles = (F + TB - 1) / TB;
+    const int col0 = 4 * c8, col1 = H / 2 + 4 * c8;  // the thread's two column quads
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int64_t row = tile * TB + r;
-        const bool valid = row < F;
-        float dhv[16];
+        // ---- staging: dH (+ the neighbours' g), dZ = dH * (Z > 0)
+        float dhv[2][8];
+        int32_t nb[2][kMpnnMaxWidth];
 #pragma unroll
-        for (int q = 0; q < 16; ++q) dhv[q] = 0.f;
-        if (valid) {
-            const float* src = V.dh + row * H + 16 * qs;
+        for (int ps = 0; ps < 2; ++ps) {
+            const int64_t row = tile * TB + slot + 64 * ps;
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                const float4 d = *reinterpret_cast<const float4*>(src + 4 * c);
-                dhv[4 * c] = d.x; dhv[4 * c + 1] = d.y; dhv[4 * c + 2] = d.z; dhv[4 * c + 3] = d.w;
-            }
-            if (gather) {
-                int32_t nb[kMpnnMaxWidth];
+            for (int q = 0; q < 8; ++q) dhv[ps][q] = 0.f;
 #pragma unroll
-                for (int k = 0; k < kMpnnMaxWidth; ++k) {
-                    const int32_t e = (k < V.W) ? __ldg(V.nbr + (int64_t)k * F + row) : (int32_t)row;
-                    nb[k] = (e == (int32_t)row) ? -1 : e;
-                }
-#pragma unroll
-                for (int c = 0; c < 2; ++c) {
-                    uint4 g[kMpnnMaxWidth];
-#pragma unroll
-                    for (int k = 0; k < kMpnnMaxWidth; ++k)
-                        g[k] = nb[k] >= 0 ? __ldg(reinterpret_cast<const uint4*>(gin + (int64_t)nb[k] * H + 16 * qs + 8 * c))
-                                          : make_uint4(0, 0, 0, 0);
+            for (int k = 0; k < kMpnnMaxWidth; ++k) nb[ps][k] = -1;
+            if (row < F) {
+                const float4 a = *reinterpret_cast<const float4*>(V.dh + row * H + col0);
+                const float4 b = *reinterpret_cast<const float4*>(V.dh + row * H + col1);
+                dhv[ps][0] = a.x; dhv[ps][1] = a.y; dhv[ps][2] = a.z; dhv[ps][3] = a.w;
+                dhv[ps][4] = b.x; dhv[ps][5] = b.y; dhv[ps][6] = b.z; dhv[ps][7] = b.w;
+                if (gather)
 #pragma unroll
                     for (int k = 0; k < kMpnnMaxWidth; ++k) {
-                        const uint32_t w4[4] = {g[k].x, g[k].y, g[k].z, g[k].w};
-#pragma unroll
-                        for (int t = 0; t < 4; ++t) {
-                            const float2 f = unpack_bf16(w4[t]);
-                            dhv[8 * c + 2 * t] += f.x;
-                            dhv[8 * c + 2 * t + 1] += f.y;
-                        }
+                        const int32_t e = (k < V.W) ? __ldg(V.nbr + (int64_t)k * F + row) : (int32_t)row;
+                        nb[ps][k] = (e == (int32_t)row) ? -1 : e;
                     }
-                }
             }
         }
+        if (gather)
 #pragma unroll
-        for (int c = 0; c < 2; ++c) {
-            const int col = 16 * qs + 8 * c;
-            uint4 out = make_uint4(0, 0, 0, 0);
-            if (valid) {
-                const uint4 zz = *reinterpret_cast<const uint4*>(V.z[layer] + row * H + col);
-                const uint32_t zw[4] = {zz.x, zz.y, zz.z, zz.w};
-                uint32_t ow[4];
+            for (int ps = 0; ps < 2; ++ps) {
+                uint2 g[kMpnnMaxWidth][2];
 #pragma unroll
-                for (int t = 0; t < 4; ++t) {
-                    const float2 z2 = unpack_bf16(zw[t]);
-                    ow[t] = pack_bf16(z2.x > 0 ? dhv[8 * c + 2 * t] : 0.f, z2.y > 0 ? dhv[8 * c + 2 * t + 1] : 0.f);
+                for (int k = 0; k < kMpnnMaxWidth; ++k) {
+                    const __nv_bfloat16* src = gin + (int64_t)(nb[ps][k] >= 0 ? nb[ps][k] : 0) * H;
+                    g[k][0] = nb[ps][k] >= 0 ? __ldg(reinterpret_cast<const uint2*>(src + col0)) : make_uint2(0, 0);
+                    g[k][1] = nb[ps][k] >= 0 ? __ldg(reinterpret_cast<const uint2*>(src + col1)) : make_uint2(0, 0);
                 }
-                out = make_uint4(ow[0], ow[1], ow[2], ow[3]);
-                *reinterpret_cast<uint4*>(V.dz + row * H + col) = out;
+#pragma unroll
+                for (int k = 0; k < kMpnnMaxWidth; ++k)
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const float2 lo = unpack_bf16(g[k][h].x), hi = unpack_bf16(g[k][h].y);
+                        dhv[ps][4 * h] += lo.x;
+                        dhv[ps][4 * h + 1] += lo.y;
+                        dhv[ps][4 * h + 2] += hi.x;
+                        dhv[ps][4 * h + 3] += hi.y;
+                    }
             }
-            st_tile(sA, r, col, H, out);
+#pragma unroll
+        for (int ps = 0; ps < 2; ++ps) {
+            const int rl = slot + 64 * ps;
+            const int64_t row = tile * TB + rl;
+            uint2 out[2] = {make_uint2(0, 0), make_uint2(0, 0)};
+            if (row < F) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int col = h ? col1 : col0;
+                    const uint2 zz = *reinterpret_cast<const uint2*>(V.z[layer] + row * H + col);
+                    const float2 z0 = unpack_bf16(zz.x), z1 = unpack_bf16(zz.y);
+                    const float* d = dhv[ps] + 4 * h;
+                    out[h] = make_uint2(pack_bf16(z0.x > 0 ? d[0] : 0.f, z0.y > 0 ? d[1] : 0.f),
+                                        pack_bf16(z1.x > 0 ? d[2] : 0.f, z1.y > 0 ? d[3] : 0.f));
+                    *reinterpret_cast<uint2*>(V.dz + row * H + col) = out[h];
+                }
+            }
+            *reinterpret_cast<uint2*>(sA + tc::kmajor_offset(rl, col0, H)) = out[0];
+            *reinterpret_cast<uint2*>(sA + tc::kmajor_offset(rl, col1, H)) = out[1];
         }
         if (!tile_mma<TB, 2 * H, H>(sA, sB, tbase, ts, false)) {
             if (tid == 0) atomicOr(V.err, 4);
             break;
         }
-        float acc[16];
-        tc::tmem_ld_x16(tlane + 16 * qs, acc);
-        if (valid) {
-            float* dh = V.dh + row * H + 16 * qs;
+        // ---- epilogue, row-per-thread: dX into the staging tiles
+        {
+            const int64_t row = tile * TB + r;
+            float acc[16];
+            tc::tmem_ld_x16(tlane + 16 * qs, acc);
 #pragma unroll
             for (int c = 0; c < 4; ++c)
-                *reinterpret_cast<float4*>(dh + 4 * c) =
-                    make_float4(dhv[4 * c] + acc[4 * c], dhv[4 * c + 1] + acc[4 * c + 1], dhv[4 * c + 2] + acc[4 * c + 2],
-                                dhv[4 * c + 3] + acc[4 * c + 3]);
-        }
-        tc::tmem_ld_x16(tlane + H + 16 * qs, acc);
-        if (valid) {
-            const int d = V.deg[row];
+                *reinterpret_cast<float4*>(sD + r * H + 4 * swz(r, 4 * qs + c)) =
+                    make_float4(acc[4 * c], acc[4 * c + 1], acc[4 * c + 2], acc[4 * c + 3]);
+            tc::tmem_ld_x16(tlane + H + 16 * qs, acc);
+            const int d = row < F ? V.deg[row] : 0;
             const float inv = d > 0 ? 1.0f / (float)d : 0.f;
             uint32_t w[8];
 #pragma unroll
             for (int t = 0; t < 8; ++t) w[t] = pack_bf16(acc[2 * t] * inv, acc[2 * t + 1] * inv);
-            uint4* g = reinterpret_cast<uint4*>(gout + row * H + 16 * qs);
-            g[0] = make_uint4(w[0], w[1], w[2], w[3]);
-            g[1] = make_uint4(w[4], w[5], w[6], w[7]);
+#pragma unroll
+            for (int c = 0; c < 2; ++c)
+                *reinterpret_cast<uint4*>(sA + r * (2 * H) + 16 * swz(r, 2 * qs + c)) =
+                    make_uint4(w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]);
+        }
+        __syncthreads();
+        // ---- row-coalesced writes: dH_l = dH + dX[:, :64], g_l
+#pragma unroll
+        for (int ps = 0; ps < 2; ++ps) {
+            const int rl = slot + 64 * ps;
+            const int64_t row = tile * TB + rl;
+            if (row >= F) continue;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int col = h ? col1 : col0;
+                const float4 x = *reinterpret_cast<const float4*>(sD + rl * H + 4 * swz(rl, col / 4));
+                const float* d = dhv[ps] + 4 * h;
+                *reinterpret_cast<float4*>(V.dh + row * H + col) = make_float4(d[0] + x.x, d[1] + x.y, d[2] + x.z, d[3] + x.w);
+                const uint2 gv = *reinterpret_cast<const uint2*>(sA + rl * (2 * H) + 16 * swz(rl, col / 8) + 2 * (col & 7));
+                *reinterpret_cast<uint2*>(gout + row * H + col) = gv;
+            }
         }
         tile_done();
     }
@@ -819,7 +862,7 @@ void mpnn_backward(const MpnnView& V, const double* target, double inv_nt, MpnnG
     const int gdec = mpnn_grid(V.F);
     k_mpnn_decode<<<gdec, 256, 0, s>>>(V, target, inv_nt);
     k_mpnn_reduce_dec<<<1, 128, 0, s>>>(V.dec_partials, gdec, G.g + G.off_wd, G.g + G.off_bd, G.loss, inv_nt);
-    const int smdx = smem_req((TB + 2 * H) * H * 2);
+    const int smdx = smem_req(kDxSmem);
     const int smdw = smem_req((TB + H) * TB * 2);
     set_smem(k_mpnn_bwd_dx, smdx);
     set_smem(k_mpnn_bwd_dw<128>, smdw);

@@ -110,26 +110,53 @@ constexpr double kRestartEps = 1e-14;
 // Per-block partial sums: up to kPartStride values per block.
 constexpr int kPartStride = 8;
 
+// FP64 sums: every thread parks its sums in shared memory and warp 0 adds
+// them, each lane the KB/32 values of its column in order, then a shuffle
+// tree; that is 12 FP64 additions per sum for the block, against 5 in each
+// of the 8 warps plus 8 in thread 0 for a shuffle tree per warp.  The FP64
+// pipe (about 2 operations per clock per SM on GB300) co-limits the FP64
+// iteration kernels with HBM, and at one wave of CTAs over 3.2M rows those
+// trees were about 12% of their FP64 operations.  FP32 sums keep the
+// per-warp trees (their additions use the FP32 pipe).
 template <typename T, int NV>
 __device__ __forceinline__ void block_reduce_store(T (&acc)[NV], double* partials)
 {
     static_assert(NV <= kPartStride, "too many partial sums");
-    __shared__ double sh[KB / 32][kPartStride];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if constexpr (sizeof(T) == 8) {
+        __shared__ double col[NV][KB];
 #pragma unroll
-    for (int q = 0; q < NV; ++q) {
-        T v = acc[q];
+        for (int q = 0; q < NV; ++q) col[q][threadIdx.x] = acc[q];
+        __syncthreads();
+        if (warp == 0) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) sh[warp][q] = (double)v;
+            for (int q = 0; q < NV; ++q) {
+                double v = col[q][lane];
+#pragma unroll
+                for (int w = 1; w < KB / 32; ++w) v += col[q][lane + 32 * w];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+                if (lane == 0) partials[(int64_t)blockIdx.x * kPartStride + q] = v;
+            }
+        }
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
+    else {
+        __shared__ double sh[KB / 32][kPartStride];
 #pragma unroll
         for (int q = 0; q < NV; ++q) {
-            double s = 0;
-            for (int w = 0; w < KB / 32; ++w) s += sh[w][q];
-            partials[(int64_t)blockIdx.x * kPartStride + q] = s;
+            T v = acc[q];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) sh[warp][q] = (double)v;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int q = 0; q < NV; ++q) {
+                double s = 0;
+                for (int w = 0; w < KB / 32; ++w) s += sh[w][q];
+                partials[(int64_t)blockIdx.x * kPartStride + q] = s;
+            }
         }
     }
 }
