@@ -492,6 +492,8 @@ mhfem_status ensure_pattern(mhfem_t h)
     dfree(h, h->A.cols);
     dfree(h, h->A.vals);
     dfree(h, h->A.vals32);
+    dfree(h, h->A.cols_lo);
+    dfree(h, h->A.cols_hi);
     dfree(h, h->amap.qmap);
     dfree(h, h->amap.qdiag);
     dfree(h, h->rhs);
@@ -505,6 +507,27 @@ mhfem_status ensure_pattern(mhfem_t h)
     if (h->fp32_copy) {
         CK(dalloc(h, &h->A.vals32, (size_t)W * rows));
         CK(cudaMemset(h->A.vals32, 0, sizeof(float) * W * rows));
+        // 24-bit column offsets for the FP32 SpMVs (the widths with an
+        // FP32 4-rows-per-thread kernel), if every offset fits
+        std::vector<uint16_t> lo;
+        std::vector<uint8_t> hi;
+        bool fits = (W == 4 || W == 6) && rows % 4 == 0;
+        if (fits) {
+            lo.resize((size_t)W * rows);
+            hi.resize((size_t)W * rows);
+            for (int64_t q = 0; q < (int64_t)W * rows && fits; ++q) {
+                const int64_t d = (int64_t)h->pat.ell_cols[q] - q % rows + kCol24Bias;
+                if (d < 0 || d >= (int64_t)1 << 24) fits = false;
+                lo[q] = (uint16_t)(d & 0xffff);
+                hi[q] = (uint8_t)(d >> 16);
+            }
+        }
+        if (fits) {
+            CK(dalloc(h, &h->A.cols_lo, (size_t)W * rows));
+            CK(dalloc(h, &h->A.cols_hi, (size_t)W * rows));
+            CK(cudaMemcpy(h->A.cols_lo, lo.data(), sizeof(uint16_t) * W * rows, cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(h->A.cols_hi, hi.data(), W * rows, cudaMemcpyHostToDevice));
+        }
     }
     if (h->nf > 4) {  // 12 positions of 4 bits: one 64-bit word per face
         uint64_t* q = nullptr;
@@ -1038,7 +1061,7 @@ mhfem_status mhfem_time_kernel(mhfem_t h, int32_t kernel, int32_t reps, double* 
         case MHFEM_KERNEL_UPDATE_P_FP64: B = R * 32; FL = 4 * R; break;
         case MHFEM_KERNEL_SPMV_FP32:
             if (!h->fp32_copy) return fail(h, MHFEM_ERR_STATE, "FP32 SpMV needs the FP32 matrix (mixed form or mixed learned solve)");
-            B = R * (8 * W + 12); FL = 2 * R * (W + 1); break;
+            B = R * ((h->A.cols_lo ? 7 : 8) * W + 12); FL = 2 * R * (W + 1); break;
         case MHFEM_KERNEL_RECONSTRUCT:
             B = 4 * nf * C + 8 * n * F + 8 * n * n * nf * C + 8 * n * C + 8 * n * C;
             FL = 2 * C * n * (n * nf + 1);

@@ -176,6 +176,62 @@ __device__ __forceinline__ void ell_apply(const EllRows<T, WW, RPT>& e, const T*
     }
 }
 
+// The FP32 SpMVs' column indices as 24-bit offsets (EllMatrix::cols_lo,
+// cols_hi): four rows per thread, so one slot is an 8-byte word of four low
+// halves and a 4-byte word of four high bytes.  Three bytes per entry
+// instead of four: the FP32 SpMV moves 7W + 12 instead of 8W + 12 bytes per
+// row, and it is bound by HBM.  Measured on the tetrahedral workloads (mixed
+// form, same iteration counts): the first FP32 SpMV 211 against 219 us at
+// 128^3 (25.3M rows), the mixed step 746 against 766 ms (2.6%); at 64^3
+// 27.4 against 29.7 us and 39.6 against 40.3 ms.
+struct Cols24 {
+    const uint16_t* lo = nullptr;
+    const uint8_t* hi = nullptr;
+};
+
+template <int WW>
+struct EllRows24 {
+    uint2 lo[WW];
+    uint32_t hi[WW];
+    VecT<float, 4> a[WW];
+};
+
+template <int WW>
+__device__ __forceinline__ void ell_load24(Cols24 pc, const float* __restrict__ vals, int64_t rows, int64_t q,
+                                           EllRows24<WW>& e)
+{
+#pragma unroll
+    for (int k = 0; k < WW; ++k) {
+        e.lo[k] = __ldcs(reinterpret_cast<const uint2*>(pc.lo + (int64_t)k * rows) + q);
+        e.hi[k] = __ldcs(reinterpret_cast<const unsigned int*>(pc.hi + (int64_t)k * rows) + q);
+        e.a[k] = ldv_stream<float, 4>(vals + (int64_t)k * rows, q);
+    }
+}
+
+// Rows 4q .. 4q + 3: column = row + (hi << 16 | lo) - 2^23.
+template <int WW>
+__device__ __forceinline__ void ell_apply24(const EllRows24<WW>& e, int64_t q, const float* __restrict__ x,
+                                            const VecT<float, 4>& self, float (&y)[4])
+{
+    const int32_t r0 = (int32_t)(4 * q) - kCol24Bias;
+    float xg[WW][4];
+#pragma unroll
+    for (int k = 0; k < WW; ++k) {
+        const uint32_t l01 = e.lo[k].x, l23 = e.lo[k].y, h = e.hi[k];
+        xg[k][0] = x[r0 + (int32_t)((l01 & 0xffffu) | ((h & 0xffu) << 16))];
+        xg[k][1] = x[r0 + 1 + (int32_t)((l01 >> 16) | ((h & 0xff00u) << 8))];
+        xg[k][2] = x[r0 + 2 + (int32_t)((l23 & 0xffffu) | (h & 0xff0000u))];
+        xg[k][3] = x[r0 + 3 + (int32_t)((l23 >> 16) | ((h >> 8) & 0xff0000u))];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        float acc = self.v[j];
+#pragma unroll
+        for (int k = 0; k < WW; ++k) acc = fmaf(e.a[k].v[j], xg[k][j], acc);
+        y[j] = acc;
+    }
+}
+
 // Grid-stride bounds: threads of the whole grid, this thread's first index.
 #define MHFEM_GRID_STRIDE                                                  \
     const int64_t gstride = (int64_t)gridDim.x * KB;                       \
@@ -203,10 +259,10 @@ __device__ __forceinline__ void ell_apply(const EllRows<T, WW, RPT>& e, const T*
 
 // v = A p ; acc = (rh, v).  The FP64 loops load the ELL words of their
 // first row before gate(); the pipelined FP32 loop starts after it.
-template <typename T, int WW, int RPT, typename Gate>
+template <typename T, int WW, int RPT, bool PK = false, typename Gate>
 __device__ __forceinline__ bool phase_spmv_dot(const int32_t* cols, const T* vals, int W, int64_t rows,
                                                const T* p, const T* rh, T* v, int64_t gtid, int64_t gstride,
-                                               T (&acc)[1], Gate&& gate)
+                                               T (&acc)[1], Gate&& gate, Cols24 pc = {})
 {
     const int64_t ng = rows / RPT;
     auto finish = [&](int64_t q, const T (&y)[RPT]) {
@@ -218,7 +274,23 @@ __device__ __forceinline__ bool phase_spmv_dot(const int32_t* cols, const T* val
 #pragma unroll
         for (int j = 0; j < RPT; ++j) acc[0] = fma(h.v[j], y[j], acc[0]);
     };
-    if constexpr (spmv_pipelined<T>(WW, RPT)) {
+    if constexpr (PK) {
+        static_assert(sizeof(T) == 4 && RPT == 4 && WW > 0, "24-bit columns: FP32, 4 rows per thread");
+        if (!gate()) return false;
+        int64_t q = gtid;
+        EllRows24<WW> cur;
+        if (q < ng) ell_load24<WW>(pc, vals, rows, q, cur);
+        for (; q < ng; q += gstride) {
+            EllRows24<WW> nxt;
+            const int64_t qn = q + gstride;
+            if (qn < ng) ell_load24<WW>(pc, vals, rows, qn, nxt);
+            T y[RPT];
+            ell_apply24<WW>(cur, q, p, ldv<T, RPT>(p, q), y);
+            finish(q, y);
+            cur = nxt;
+        }
+    }
+    else if constexpr (spmv_pipelined<T>(WW, RPT)) {
         int64_t q = gtid;
         EllRows<T, WW, RPT> cur;
         if constexpr (sizeof(T) == 8)
@@ -327,10 +399,10 @@ __device__ __forceinline__ void phase_update_s(int64_t rows, const T* r, const T
 
 // t = A s ; acc = (t, s), (t, t) and, on a check iteration, (s, s).  The
 // FP64 loops load the ELL words of their first row before gate().
-template <typename T, int WW, int RPT, bool CHECK, typename Gate>
+template <typename T, int WW, int RPT, bool CHECK, bool PK = false, typename Gate>
 __device__ __forceinline__ bool phase_spmv_dots2(const int32_t* cols, const T* vals, int W, int64_t rows,
                                                  const T* s, T* t, int64_t gtid, int64_t gstride,
-                                                 T (&acc)[CHECK ? 3 : 2], Gate&& gate)
+                                                 T (&acc)[CHECK ? 3 : 2], Gate&& gate, Cols24 pc = {})
 {
     const int64_t ng = rows / RPT;
     auto finish = [&](int64_t q, const T (&y)[RPT], const T (&sv)[RPT]) {
@@ -344,7 +416,26 @@ __device__ __forceinline__ bool phase_spmv_dots2(const int32_t* cols, const T* v
         }
         stv<T, RPT>(t, q, yv);
     };
-    if constexpr (spmv_pipelined<T>(WW, RPT)) {
+    if constexpr (PK) {
+        static_assert(sizeof(T) == 4 && RPT == 4 && WW > 0, "24-bit columns: FP32, 4 rows per thread");
+        if (!gate()) return false;
+        int64_t q = gtid;
+        EllRows24<WW> cur;
+        if (q < ng) ell_load24<WW>(pc, vals, rows, q, cur);
+        for (; q < ng; q += gstride) {
+            EllRows24<WW> nxt;
+            const int64_t qn = q + gstride;
+            if (qn < ng) ell_load24<WW>(pc, vals, rows, qn, nxt);
+            const VecT<T, RPT> svv = ldv<T, RPT>(s, q);
+            T y[RPT], sv[RPT];
+            ell_apply24<WW>(cur, q, s, svv, y);
+#pragma unroll
+            for (int j = 0; j < RPT; ++j) sv[j] = svv.v[j];
+            finish(q, y, sv);
+            cur = nxt;
+        }
+    }
+    else if constexpr (spmv_pipelined<T>(WW, RPT)) {
         int64_t q = gtid;
         EllRows<T, WW, RPT> cur;
         if constexpr (sizeof(T) == 8)
@@ -568,6 +659,23 @@ __global__ void __launch_bounds__(KB) k_spmv_dot(const int32_t* cols, const T* v
     if (threadIdx.x == 0) scalars_alpha(sc, s);
 }
 
+// The FP32 SpMV over 24-bit column offsets (the mixed form's inner solve).
+template <int WW>
+__global__ void __launch_bounds__(KB) k_spmv_dot24(Cols24 pc, const float* vals, int64_t rows, const float* p,
+                                                   const float* rh, float* v, KrylovScalars* sc, double* partials,
+                                                   uint32_t* counter)
+{
+    MHFEM_GRID_STRIDE;
+    float acc[1] = {0};
+    if (!phase_spmv_dot<float, WW, 4, true>(nullptr, vals, WW, rows, p, rh, v, gtid, gstride, acc, MHFEM_GATE(sc), pc))
+        return;
+    block_reduce_store<float, 1>(acc, partials);
+    if (!ticket_last(counter)) return;
+    double s[1];
+    final_sums<1>(partials, s);
+    if (threadIdx.x == 0) scalars_alpha(sc, s);
+}
+
 template <typename T, int V>
 __global__ void __launch_bounds__(KB) k_update_s(int64_t rows, const T* r, const T* v, T* s, const KrylovScalars* sc)
 {
@@ -591,6 +699,23 @@ __global__ void __launch_bounds__(KB) k_spmv_dots2(const int32_t* cols, const T*
     T acc[NS] = {};
     if (!phase_spmv_dots2<T, WW, RPT, CHECK>(cols, vals, W, rows, s, t, gtid, gstride, acc, MHFEM_GATE(sc))) return;
     block_reduce_store<T, NS>(acc, partials);
+    if (!ticket_last(counter)) return;
+    double sum[NS];
+    final_sums<NS>(partials, sum);
+    if (threadIdx.x == 0) scalars_omega<CHECK>(sc, sum);
+}
+
+template <int WW, bool CHECK>
+__global__ void __launch_bounds__(KB) k_spmv_dots2_24(Cols24 pc, const float* vals, int64_t rows, const float* s,
+                                                      float* t, KrylovScalars* sc, double* partials, uint32_t* counter)
+{
+    constexpr int NS = CHECK ? 3 : 2;
+    MHFEM_GRID_STRIDE;
+    float acc[NS] = {};
+    if (!phase_spmv_dots2<float, WW, 4, CHECK, true>(nullptr, vals, WW, rows, s, t, gtid, gstride, acc,
+                                                     MHFEM_GATE(sc), pc))
+        return;
+    block_reduce_store<float, NS>(acc, partials);
     if (!ticket_last(counter)) return;
     double sum[NS];
     final_sums<NS>(partials, sum);
@@ -681,20 +806,45 @@ static void iterate(const EllMatrix& A, const T* vals, T* x, T* r, T* rh, T* p, 
                     KrylovScalars* sc, KrylovWork& W, int iters, cudaStream_t st)
 {
     const int32_t* cols = A.cols;
-    for (int it = 0; it < iters; ++it) {
-        const bool check = (it == iters - 1);  // the last iteration before the host's check
+    const Cols24 pc{A.cols_lo, A.cols_hi};
+    // 24-bit column offsets: FP32, 4 rows per thread, widths 4 and 6
+    const bool pk = sizeof(T) == 4 && RPT == 4 && A.cols_lo && A.cols_hi && (A.width == 4 || A.width == 6);
+    auto spmv1 = [&]() {
+        if constexpr (sizeof(T) == 4 && RPT == 4)
+            if (pk) {
+                if (A.width == 4) launch_pdl(k_spmv_dot24<4>, st, A.rows, pc, vals, A.rows, (const T*)p, (const T*)rh, v, sc,
+                                             W.partials, W.counters);
+                else launch_pdl(k_spmv_dot24<6>, st, A.rows, pc, vals, A.rows, (const T*)p, (const T*)rh, v, sc,
+                                W.partials, W.counters);
+                return;
+            }
         MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dot<T, WW, spmv_rpt(WW, RPT)>, st, A.rows, cols, vals, A.width,
                                                  A.rows, (const T*)p, (const T*)rh, v, sc, W.partials, W.counters));
+    };
+    auto spmv2 = [&](auto ctag) {
+        constexpr bool C = decltype(ctag)::value;
+        if constexpr (sizeof(T) == 4 && RPT == 4)
+            if (pk) {
+                if (A.width == 4) launch_pdl(k_spmv_dots2_24<4, C>, st, A.rows, pc, vals, A.rows, (const T*)s, t, sc,
+                                             W.partials, W.counters);
+                else launch_pdl(k_spmv_dots2_24<6, C>, st, A.rows, pc, vals, A.rows, (const T*)s, t, sc, W.partials,
+                                W.counters);
+                return;
+            }
+        MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dots2<T, WW, spmv_rpt(WW, RPT), C>, st, A.rows, cols, vals,
+                                                 A.width, A.rows, (const T*)s, t, sc, W.partials, W.counters));
+    };
+    for (int it = 0; it < iters; ++it) {
+        const bool check = (it == iters - 1);  // the last iteration before the host's check
+        spmv1();
         launch_pdl(k_update_s<T, V>, st, A.rows, A.rows, (const T*)r, (const T*)v, s, (const KrylovScalars*)sc);
         if (check) {
-            MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dots2<T, WW, spmv_rpt(WW, RPT), true>, st, A.rows, cols, vals,
-                                                     A.width, A.rows, (const T*)s, t, sc, W.partials, W.counters));
+            spmv2(std::true_type{});
             launch_pdl(k_update_xr<T, V, true>, st, A.rows, A.rows, x, (const T*)p, (const T*)s, (const T*)t, r,
                        (const T*)rh, sc, W.partials, W.counters);
         }
         else {
-            MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dots2<T, WW, spmv_rpt(WW, RPT), false>, st, A.rows, cols, vals,
-                                                     A.width, A.rows, (const T*)s, t, sc, W.partials, W.counters));
+            spmv2(std::false_type{});
             launch_pdl(k_update_xr<T, V, false>, st, A.rows, A.rows, x, (const T*)p, (const T*)s, (const T*)t, r,
                        (const T*)rh, sc, W.partials, W.counters);
         }
@@ -969,7 +1119,14 @@ void krylov_iterate_fp32(const EllMatrix& A, KrylovWork& W, int iters, cudaStrea
 void krylov_spmv_dot_once(const EllMatrix& A, KrylovWork& W, bool fp32, cudaStream_t s)
 {
     if (fp32) {
-        if (spmv4_ok(A, {W.p32, W.rh32, W.v32}))
+        const Cols24 pc{A.cols_lo, A.cols_hi};
+        if (spmv4_ok(A, {W.p32, W.rh32, W.v32}) && A.cols_lo && A.cols_hi) {
+            if (A.width == 4) launch_pdl(k_spmv_dot24<4>, s, A.rows, pc, (const float*)A.vals32, A.rows, (const float*)W.p32,
+                                         (const float*)W.rh32, W.v32, W.sc32, W.partials, W.counters);
+            else launch_pdl(k_spmv_dot24<6>, s, A.rows, pc, (const float*)A.vals32, A.rows, (const float*)W.p32,
+                            (const float*)W.rh32, W.v32, W.sc32, W.partials, W.counters);
+        }
+        else if (spmv4_ok(A, {W.p32, W.rh32, W.v32}))
             MHFEM_WIDTH_DISPATCH(A.width, launch_pdl(k_spmv_dot<float, WW, spmv_rpt(WW, 4)>, s, A.rows,
                                                      (const int32_t*)A.cols, (const float*)A.vals32, A.width, A.rows,
                                                      (const float*)W.p32, (const float*)W.rh32, W.v32, W.sc32,

@@ -114,7 +114,14 @@ struct EllMatrix {
     int32_t* cols = nullptr;     // [width][rows]
     double* vals = nullptr;      // [width][rows]
     float* vals32 = nullptr;     // [width][rows] (mixed form)
+    // The FP32 SpMVs' column indices as 24-bit offsets from the row (mixed
+    // form, when every |col - row| < 2^23): col - row + 2^23 split into the
+    // low 16 bits and the high 8 bits, each [width][rows].  Three bytes per
+    // entry instead of four; null when not built.
+    uint16_t* cols_lo = nullptr;
+    uint8_t* cols_hi = nullptr;
 };
+constexpr int32_t kCol24Bias = 1 << 23;
 
 // Per-row assembly map: which ELL slot each (side, local face) goes to.
 struct AssemblyMap {
