@@ -550,12 +550,14 @@ mhfem_status ensure_pattern(mhfem_t h)
     // Krylov workspace (7 vectors as in Solver::estimateMemoryDemands, Solver.hpp:1424-1425)
     KrylovWork& Wk = h->W;
     dfree(h, Wk.r); dfree(h, Wk.rh); dfree(h, Wk.p); dfree(h, Wk.v); dfree(h, Wk.s); dfree(h, Wk.t);
+    dfree(h, Wk.p2); dfree(h, Wk.v2);
     dfree(h, Wk.r32); dfree(h, Wk.rh32); dfree(h, Wk.p32); dfree(h, Wk.v32); dfree(h, Wk.s32); dfree(h, Wk.t32);
     dfree(h, Wk.x32); dfree(h, Wk.partials); dfree(h, Wk.counters); dfree(h, Wk.sc); dfree(h, Wk.sc32);
     Wk.rows = rows;
     Wk.grid = krylov_grid();
     CK(dalloc(h, &Wk.r, (size_t)rows)); CK(dalloc(h, &Wk.rh, (size_t)rows)); CK(dalloc(h, &Wk.p, (size_t)rows));
     CK(dalloc(h, &Wk.v, (size_t)rows)); CK(dalloc(h, &Wk.s, (size_t)rows)); CK(dalloc(h, &Wk.t, (size_t)rows));
+    if (rows <= krylov_small_rows()) { CK(dalloc(h, &Wk.p2, (size_t)rows)); CK(dalloc(h, &Wk.v2, (size_t)rows)); }
     if (h->fp32_copy) {
         CK(dalloc(h, &Wk.r32, (size_t)rows)); CK(dalloc(h, &Wk.rh32, (size_t)rows)); CK(dalloc(h, &Wk.p32, (size_t)rows));
         CK(dalloc(h, &Wk.v32, (size_t)rows)); CK(dalloc(h, &Wk.s32, (size_t)rows)); CK(dalloc(h, &Wk.t32, (size_t)rows));
@@ -702,6 +704,27 @@ mhfem_status mhfem::run_fp64(mhfem_t h, double tol, int max_iter, int* iters, do
     if (h->opts.linear_solver == MHFEM_SOLVER_GMRES) return run_gmres(h, tol, max_iter, iters, res);
     const auto t0 = std::chrono::steady_clock::now();
     krylov_init_fp64(h->A, h->rhs, h->Z_iF, h->W, tol, max_iter, h->stream);
+    if (h->A.rows <= krylov_small_rows() && h->W.p2 && h->W.v2) {
+        // small system: chunks of iterations in one persistent launch each
+        // (k_bicgstab_small), one host round trip per chunk
+        constexpr int kChunk = 256;
+        h->launches += 1;
+        for (;;) {
+            CK(krylov_small_fp64(h->A, h->Z_iF, h->W, kChunk, h->stream));
+            h->launches += 1;
+            CK(cudaMemcpyAsync(h->W.host_sc, h->W.sc, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaMemcpyAsync(h->host_err, h->W.counters + 3, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+            if (*h->host_err)
+                return fail(h, MHFEM_ERR_CUDA, "FP64 BiCGStab (small system): a grid barrier wait gave up");
+            if (h->W.host_sc->done) break;
+            if (h->opts.timeout_s > 0 && elapsed_s(t0) > h->opts.timeout_s)
+                return fail(h, MHFEM_ERR_TIMEOUT, "Krylov solve exceeded %.1f s", h->opts.timeout_s);
+        }
+        *iters = h->W.host_sc->it;
+        *res = h->W.host_sc->res;
+        return status_from_krylov(h, *h->W.host_sc, "FP64 BiCGStab");
+    }
     CK(cudaMemcpyAsync(h->W.host_sc, h->W.sc, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaGetLastError());

@@ -18,6 +18,7 @@
 //    convergence checks;
 //  - FP32 kernels accumulate per-thread sums in FP32 and block sums in FP64:
 //    GB300 issues FP64 at 1/57 of the FP32 rate.
+#include <algorithm>
 #include <initializer_list>
 #include <type_traits>
 
@@ -772,6 +773,243 @@ __global__ void __launch_bounds__(KB) k_update_p(int64_t rows, T* p, const T* r,
     }
 }
 
+// ---- small systems: one persistent launch per chunk of iterations ----------------
+//
+// A system of a few ten thousand rows (the 128^2 heat-equation workload:
+// 49,408 rows, about 2 MB of matrix and vectors, all L2-resident) leaves the
+// five-kernel iteration bound by launch and drain latency: about 30 us per
+// iteration for a few microseconds of memory traffic.  Here one cooperative
+// launch (every CTA resident) runs a chunk of iterations:
+//  - the five phases of an iteration are separated by grid barriers;
+//  - each reduction's per-CTA partials are summed by every CTA itself, in
+//    the same fixed order, so every CTA holds the same scalars (in shared
+//    memory) with no last-block step, and the result is deterministic;
+//  - the convergence test runs every iteration, as in the reference's loop
+//    (the five-kernel path tests every check_every iterations);
+//  - a thread owns the same rows in every phase, so its own rows need no
+//    synchronization; values of other CTAs' rows (the SpMV gathers, the
+//    partials) are loaded past L1 (ld.global.cg), which is not coherent
+//    between SMs; the matrix, constant during the solve, stays in L1.
+// Every barrier wait is bounded: a CTA that polls kBarrierPolls times
+// records the failure in *bar_err and returns, and the others then fail
+// their next wait at once.
+
+constexpr unsigned int kBarrierPolls = 1u << 22;  // seconds, far beyond any barrier of a working launch
+
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p)
+{
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Arrive at the grid barrier whose cumulative arrival count is `target`
+// (the count starts at 0 for a launch and grows by gridDim.x per barrier)
+// and wait for every CTA.  False (in every thread of the CTA) when the wait
+// gave up.
+__device__ __forceinline__ bool grid_barrier(unsigned int* count, int* err, unsigned int target)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int good = 1;
+        __threadfence();
+        atomicAdd(count, 1u);
+        unsigned int polls = 0;
+        while (ld_acquire_u32(count) < target) {
+            if (++polls > kBarrierPolls || *(volatile int*)err != 0) {
+                good = 0;
+                atomicExch(err, 1);
+                break;
+            }
+            __nanosleep(32);
+        }
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Sum of the per-CTA partials [cta][kPartStride] in CTA order, identical in
+// every CTA (same loads, same order); the result is in out[] of every thread.
+template <int NV>
+__device__ __forceinline__ void grid_sums(const double* partials, double (&out)[NV])
+{
+    __shared__ double col[NV][KB];
+    __shared__ double tot[NV];
+    const int nb = (int)gridDim.x;
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+        col[q][threadIdx.x] = threadIdx.x < nb ? __ldcg(partials + (int64_t)threadIdx.x * kPartStride + q) : 0.0;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            double v = col[q][lane];
+#pragma unroll
+            for (int w = 1; w < KB / 32; ++w) v += col[q][lane + 32 * w];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) tot[q] = v;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NV; ++q) out[q] = tot[q];
+}
+
+// y = self + sum_k a_k g(c_k), where g(j) forms the gathered vector's value
+// at row j (loaded past L1); same operation order as spmv_rows, so the
+// products match the five-kernel path's.
+template <int WW, typename G>
+__device__ __forceinline__ double small_row(const int32_t* __restrict__ cols, const double* __restrict__ vals, int W,
+                                            int64_t rows, int64_t q, double self, G&& g)
+{
+    double acc = self;
+    if constexpr (WW > 0) {
+        int32_t c[WW];
+        double a[WW], xg[WW];
+#pragma unroll
+        for (int k = 0; k < WW; ++k) {
+            c[k] = __ldg(cols + (int64_t)k * rows + q);
+            a[k] = __ldg(vals + (int64_t)k * rows + q);
+        }
+#pragma unroll
+        for (int k = 0; k < WW; ++k) xg[k] = g(c[k]);
+#pragma unroll
+        for (int k = 0; k < WW; ++k) acc = fma(a[k], xg[k], acc);
+    }
+    else
+        for (int k = 0; k < W; ++k) {
+            const int64_t o = (int64_t)k * rows + q;
+            acc = fma(__ldg(vals + o), g(__ldg(cols + o)), acc);
+        }
+    return acc;
+}
+
+// Three phases and three grid barriers per iteration: the p update of the
+// previous iteration and the s update are formed where they are needed,
+// for the own rows and again for each gathered neighbour (the same
+// operations, so the same values), instead of in phases of their own.  p
+// and v therefore alternate between two buffers: the neighbours' old p and
+// v stay readable while the new ones are written.
+//  1. p = r + beta (p' - omega v') (on a restart and in the first
+//     iteration p = rh = r), v = A p, (rh, v) -> alpha;
+//  2. s = r - alpha v, t = A s, (t, s), (t, t), (s, s) -> the half-step
+//     test and omega;
+//  3. x += alpha p + omega s, r = s - omega t, (rh, r), (r, r) -> the
+//     convergence test, the restart test and beta.
+template <int WW>
+__global__ void __launch_bounds__(KB) k_bicgstab_small(const int32_t* __restrict__ cols,
+                                                       const double* __restrict__ vals, int W, int64_t rows,
+                                                       double* x, double* r, double* rh, double* p0, double* p1,
+                                                       double* v0, double* v1, double* s, double* t,
+                                                       KrylovScalars* sc, double* partials, unsigned int* bar,
+                                                       int* bar_err, int max_its)
+{
+    __shared__ KrylovScalars S;
+    if (threadIdx.x == 0) S = *sc;
+    __syncthreads();
+    if (S.done) return;
+    MHFEM_GRID_STRIDE;
+    const unsigned int nb = gridDim.x;
+    unsigned int target = 0;
+    double* pa = partials;
+    double* pc = partials + (int64_t)nb * kPartStride;
+    double* pd = partials + 2 * (int64_t)nb * kPartStride;
+    for (int k = 0; k < max_its; ++k) {
+        const int cur = S.it & 1;
+        const double* P = cur ? p1 : p0;
+        double* Pn = cur ? p0 : p1;
+        const double* V = cur ? v1 : v0;
+        double* Vn = cur ? v0 : v1;
+        // 1. p, v = A p, (rh, v) -> alpha
+        {
+            const bool fresh = S.restart || S.it == 0;
+            const double beta = S.beta, omega = S.omega;
+            auto pval = [&](int64_t j) {
+                const double rj = __ldcg(r + j);
+                return fresh ? rj : fma(beta, fma(-omega, __ldcg(V + j), __ldcg(P + j)), rj);
+            };
+            double acc[1] = {0};
+            for (int64_t q = gtid; q < rows; q += gstride) {
+                const double pq = pval(q);
+                const double y = small_row<WW>(cols, vals, W, rows, q, pq, pval);
+                Pn[q] = pq;
+                Vn[q] = y;
+                double hq;
+                if (fresh) { hq = __ldcg(r + q); rh[q] = hq; }
+                else hq = rh[q];
+                acc[0] = fma(hq, y, acc[0]);
+            }
+            block_reduce_store<double, 1>(acc, pa);
+            if (!grid_barrier(bar, bar_err, target += nb)) return;
+            double sum[1];
+            grid_sums<1>(pa, sum);
+            if (threadIdx.x == 0) scalars_alpha(&S, sum);
+            __syncthreads();
+            if (S.done) break;
+        }
+        const double alpha = S.alpha;
+        // 2. s = r - alpha v, t = A s, (t, s), (t, t), (s, s) -> half step, omega
+        {
+            auto sval = [&](int64_t j) { return fma(-alpha, __ldcg(Vn + j), __ldcg(r + j)); };
+            double acc[3] = {0, 0, 0};
+            for (int64_t q = gtid; q < rows; q += gstride) {
+                const double sv = sval(q);
+                const double y = small_row<WW>(cols, vals, W, rows, q, sv, sval);
+                s[q] = sv;
+                t[q] = y;
+                acc[0] = fma(y, sv, acc[0]);
+                acc[1] = fma(y, y, acc[1]);
+                acc[2] = fma(sv, sv, acc[2]);
+            }
+            block_reduce_store<double, 3>(acc, pc);
+            if (!grid_barrier(bar, bar_err, target += nb)) return;
+            double sum[3];
+            grid_sums<3>(pc, sum);
+            if (threadIdx.x == 0) scalars_omega<true>(&S, sum);
+            __syncthreads();
+        }
+        if (S.half) {
+            for (int64_t q = gtid; q < rows; q += gstride) x[q] = fma(alpha, Pn[q], x[q]);
+            if (threadIdx.x == 0) scalars_half(&S);
+            __syncthreads();
+            break;
+        }
+        if (S.done) break;
+        // 3. x, r, (rh, r), (r, r) -> convergence, restart, beta
+        {
+            const double omega = S.omega;
+            double acc[2] = {0, 0};
+            for (int64_t q = gtid; q < rows; q += gstride) {
+                const double sv = s[q];
+                x[q] = fma(omega, sv, fma(alpha, Pn[q], x[q]));
+                const double rv = fma(-omega, t[q], sv);
+                r[q] = rv;
+                acc[0] = fma(rh[q], rv, acc[0]);
+                acc[1] = fma(rv, rv, acc[1]);
+            }
+            block_reduce_store<double, 2>(acc, pd);
+            if (!grid_barrier(bar, bar_err, target += nb)) return;
+            double sum[2];
+            grid_sums<2>(pd, sum);
+            if (threadIdx.x == 0) {
+                scalars_beta<true>(&S, sum);
+                if (!S.done && S.restart) {  // rh = r (formed in phase 1): rho = (r, r)
+                    S.rho = S.rr;
+                    S.rhnorm = sqrt(S.rr);
+                }
+            }
+            __syncthreads();
+            if (S.done) break;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *sc = S;
+}
+
 // ---- launch shapes ---------------------------------------------------------------
 
 
@@ -1179,6 +1417,53 @@ void krylov_fp64_kernel_once(const EllMatrix& A, KrylovWork& W, int which, cudaS
     };
     if (v2) run(std::integral_constant<int, 2>{});
     else run(std::integral_constant<int, 1>{});
+}
+
+
+// ---- small systems: host side ----------------------------------------------------
+
+// Rows up to which the FP64 solve takes the persistent path, and rows per
+// thread it aims at (more CTAs spread the memory traffic over more SMs, but
+// every CTA adds an arrival to each grid barrier).
+constexpr int64_t kSmallSystemRows = (int64_t)1 << 18;
+constexpr int kSmallRowsPerThread = 2;
+
+int64_t krylov_small_rows() { return kSmallSystemRows; }
+
+cudaError_t krylov_small_fp64(const EllMatrix& A, double* x, KrylovWork& W, int iters, cudaStream_t s)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const int sms = sm_count(dev);
+    int nb = 0;
+    MHFEM_WIDTH_DISPATCH(A.width, e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_bicgstab_small<WW>, KB, 0));
+    if (e != cudaSuccess) return e;
+    if (nb < 1) return cudaErrorCooperativeLaunchTooLarge;
+    const int64_t want = (A.rows + (int64_t)KB * kSmallRowsPerThread - 1) / ((int64_t)KB * kSmallRowsPerThread);
+    // every CTA resident (a cooperative launch), at most one per SM, and few
+    // enough that the three reductions' partials fit the per-CTA buffer
+    int grid = (int)std::min<int64_t>(std::min<int64_t>(want, (int64_t)sms), (int64_t)nb * sms);
+    grid = std::max(1, std::min(grid, W.grid / 3));
+    unsigned int* bar = W.counters + 2;
+    int* bar_err = reinterpret_cast<int*>(W.counters + 3);
+    e = cudaMemsetAsync(bar, 0, 2 * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    const int32_t* cols = A.cols;
+    const double* vals = A.vals;
+    int W_ = A.width;
+    int64_t rows = A.rows;
+    double *r = W.r, *rh = W.rh, *p0 = W.p, *p1 = W.p2, *v0 = W.v, *v1 = W.v2, *sv = W.s, *t = W.t;
+    if (!p1 || !v1) return cudaErrorInvalidValue;
+    KrylovScalars* sc = W.sc;
+    double* partials = W.partials;
+    int its = iters;
+    void* args[] = {(void*)&cols, (void*)&vals, (void*)&W_, (void*)&rows, (void*)&x, (void*)&r, (void*)&rh,
+                    (void*)&p0, (void*)&p1, (void*)&v0, (void*)&v1, (void*)&sv, (void*)&t, (void*)&sc,
+                    (void*)&partials, (void*)&bar, (void*)&bar_err, (void*)&its};
+    MHFEM_WIDTH_DISPATCH(A.width, e = cudaLaunchCooperativeKernel((const void*)k_bicgstab_small<WW>, dim3(grid), dim3(KB),
+                                                                 args, 0, s));
+    return e;
 }
 
 void mixed_apply_correction(double* x, KrylovWork& W, cudaStream_t s)

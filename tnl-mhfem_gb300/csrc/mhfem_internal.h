@@ -148,6 +148,7 @@ struct KrylovWork {
     int64_t rows = 0;
     int grid = 0, block = 256;
     double *r = nullptr, *rh = nullptr, *p = nullptr, *v = nullptr, *s = nullptr, *t = nullptr;
+    double *p2 = nullptr, *v2 = nullptr;  // second p and v buffers of the small-system solve
     float *r32 = nullptr, *rh32 = nullptr, *p32 = nullptr, *v32 = nullptr, *s32 = nullptr,
           *t32 = nullptr, *x32 = nullptr;
     double* partials = nullptr;      // [grid][8]
@@ -202,6 +203,13 @@ void gmres_iterate(const EllMatrix& A, GmresWork& G, KrylovWork& W, int iters, b
 // end of a cycle: solve the triangular system and update x
 void gmres_update(double* x, GmresWork& G, int64_t rows, cudaStream_t s);
 void krylov_iterate_fp64(const EllMatrix& A, double* x, KrylovWork& W, int iters, cudaStream_t s);
+// Small systems (rows <= krylov_small_rows()): up to `iters` FP64 BiCGStab
+// iterations in one cooperative launch on a solve set up by krylov_init_fp64
+// (p and v alternate between W.p / W.p2 and W.v / W.v2); the two words at
+// W.counters + 2 are the grid barrier's arrival count and its failure flag
+// (non-zero after a barrier wait gave up).
+int64_t krylov_small_rows();
+cudaError_t krylov_small_fp64(const EllMatrix& A, double* x, KrylovWork& W, int iters, cudaStream_t s);
 
 // mixed: outer residual r = b - A x (FP64) -> sc; scale into r32; inner FP32 solve; x += scale*e
 void mixed_outer_residual(const EllMatrix& A, const double* b, const double* x, KrylovWork& W,
