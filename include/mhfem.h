@@ -112,7 +112,9 @@ typedef struct {
     int32_t max_iter;         /* max-iterations of the Krylov solver */
     double  inner_tol;        /* mixed form: relative tolerance of each FP32 sweep */
     int32_t max_sweeps;       /* mixed form: cap on refinement sweeps */
-    int32_t check_every;      /* Krylov iterations between host convergence checks */
+    int32_t check_every;      /* Krylov iterations between host convergence checks (systems
+                                 above 2^18 rows; smaller FP64 BiCGStab solves run in one
+                                 persistent launch and test every iteration) */
     double  timeout_s;        /* host wall-clock limit of one solve (<= 0: none) */
     int32_t inner_adaptive;   /* mixed form: relax the last sweeps' inner tolerance to what the outer
                                  tolerance still needs (never tighter than inner_tol) */
