@@ -74,8 +74,9 @@ def parse_args():
                     help="polynomial extrapolation order of the base the network corrects (0-3)")
     ap.add_argument("--profile-run", action="store_true",
                     help="only the warm-up and timed steps (for an ncu launch list)")
-    ap.add_argument("--profile-form", choices=["fp64", "mixed", "learned", "box", "gmres"], default="fp64",
-                    help="form used by --profile-run (learned: --learned-train training steps first)")
+    ap.add_argument("--profile-form", choices=["fp64", "mixed", "learned", "box", "gmres", "heat2d"], default="fp64",
+                    help="form used by --profile-run (learned: --learned-train training steps first; heat2d: "
+                         "the FP64 form on the 128^2 heat-equation workload, a small-system solve)")
     return ap.parse_args()
 
 
@@ -613,8 +614,9 @@ def learned_protocol_leg(args, dev, world):
 
 
 def profile_other_form(args, dev):
-    """Warm-up + timed steps of the mixed or learned form, or of the FP64 form on
-    (2 grid)^3 cuboids ("box"), only (for ncu launch lists)."""
+    """Warm-up + timed steps of the mixed or learned form, of the FP64 form on
+    (2 grid)^3 cuboids ("box"), with GMRES ("gmres"), or on the 128^2
+    heat-equation workload ("heat2d"), only (for ncu launch lists)."""
     import torch
 
     from mhfem import _lib as L
@@ -626,6 +628,8 @@ def profile_other_form(args, dev):
         p = problems.diffusion3d_box(N=2 * args.grid)
     elif args.profile_form == "gmres":
         p = problems.diffusion3d(N=args.grid)
+    elif args.profile_form == "heat2d":
+        p = problems.heat2d(N=128)
     else:
         p = problems.diffusion3d_source(N=args.grid, steps=1000, form=L.FORM_LEARNED)
     p.config.device = dev

@@ -124,6 +124,14 @@ typedef struct {
     int32_t gmres_restart;    /* gmres-restarting-max: restart length, 1 to 32 (default 30) */
     int32_t gmres_variant;    /* gmres-variant: MHFEM_GMRES_CGS (default) or MHFEM_GMRES_CGSR
                                  (classical Gram-Schmidt with one reorthogonalization pass) */
+    int32_t gmres_restart_min;      /* gmres-restarting-min: with gmres_restart_step_min > 0 and a
+                                       value below gmres_restart, the restart length varies between
+                                       the two from cycle to cycle (Baker, Jessup and Kolev's rule on
+                                       the ratio of consecutive restart residuals); 0 (default): fixed
+                                       at gmres_restart */
+    int32_t gmres_restart_step_min; /* gmres-restarting-step-min: decrement of the restart length */
+    int32_t gmres_restart_step_max; /* gmres-restarting-step-max: decrement after a well-converging
+                                       cycle (at least gmres_restart_step_min) */
 } mhfem_solver_opts;
 
 #define MHFEM_SOLVER_BICGSTAB 0

@@ -48,6 +48,15 @@ def test_config_schema(tmp_path):
     (tmp_path / "tfqmr.ini").write_text(CONFIG.replace("linear-solver = gmres", "linear-solver = tfqmr"))
     c3 = config.parse(tmp_path / "tfqmr.ini")
     assert c3["_solver"] == "bicgstab" and any("BiCGStab" in n for n in c3.notices)
+    # fixed restart length unless gmres-restarting-min and a step are given
+    assert cfg["_gmres_restart_min"] == 0 and cfg["_gmres_restart_steps"] == (0, 0)
+    # the reference example's adaptive keys (examples/HeatEquation/config.ini:15-22)
+    (tmp_path / "adaptive.ini").write_text(CONFIG.replace(
+        "gmres-restarting-max = 30",
+        "gmres-restarting-max = 30\ngmres-restarting-min = 3\ngmres-restarting-step-max = 4\n"
+        "gmres-restarting-step-min = 2"))
+    c4 = config.parse(tmp_path / "adaptive.ini")
+    assert c4["_gmres_restart"] == 30 and c4["_gmres_restart_min"] == 3 and c4["_gmres_restart_steps"] == (2, 4)
     (tmp_path / "bad.ini").write_text(CONFIG + "no-such-key = 1\n")
     with pytest.raises(config.ConfigError, match="unknown"):
         config.parse(tmp_path / "bad.ini")

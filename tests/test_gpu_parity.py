@@ -372,6 +372,27 @@ def test_gmres_heat2d_full_size():
     s.close()
 
 
+def test_gmres_adaptive_restart_full_size():
+    """The reference example's adaptive restart keys (gmres-restarting-min 3,
+    -max 30, -step-min 2, -step-max 4) on the 128^2 heat-equation workload
+    and on the 512^2 ADR workload: every step's face traces and cell values
+    within 1e-10 of the oracle, as with the fixed restart length."""
+    for p in (problems.heat2d(N=128, steps=3), problems.adr2d(N=512, steps=2)):
+        s, m = _pair(p, check_every=8)
+        s.setup(tol=1e-13, max_iter=20000, check_every=8, linear_solver="gmres", gmres_restart=30,
+                gmres_variant="cgs", gmres_restart_min=3, gmres_restart_step_min=2, gmres_restart_step_max=4)
+        t = 0.0
+        for _ in range(p.steps):
+            st = s.step(t, p.dt)
+            m.step(t, p.dt, 1e-13)
+            assert st["residual"] < 1e-13
+            t += p.dt
+        zf, zk = s.state()
+        assert rel_err(zf, m.Z_iF) < TOL_STATE, p.name
+        assert rel_err(zk, m.Z_iK) < TOL_STATE, p.name
+        s.close()
+
+
 def test_gmres_not_converged_is_reported():
     p = problems.diffusion3d(N=6, steps=1)
     s = problems.make_solver(p)

@@ -2,6 +2,7 @@
 symbol include/mhfem.h declares, refuses to run without a device, and the
 model builders reproduce the workload sizes."""
 import ctypes as ct
+import math
 import re
 from pathlib import Path
 
@@ -173,3 +174,49 @@ def test_integer_pipe_conversions_match_ieee_casts(tmp_path):
     assert r.returncode == 0, r.stderr
     r = subprocess.run([str(out)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout[-2000:]
+
+
+def _next_restart(m_min, m_max, step_min, step_max, m, cr):
+    """Baker, Jessup and Kolev's restart-length rule with the step as the
+    library applies it (restated independently of gmres_restart.h)."""
+    if not (0 < m_min < m_max and step_min > 0):
+        return m_max
+    max_cr, min_cr = math.cos(math.radians(8.0)), math.cos(math.radians(80.0))
+    if not cr <= max_cr:
+        return m_max
+    if cr < min_cr:
+        return m
+    d = max(step_max, step_min) if cr < 0.5 * (min_cr + max_cr) else step_min
+    return m - d if m - d >= m_min else m_max
+
+
+def test_gmres_restart_rule(tmp_path):
+    """The host rule of the adaptive GMRES restart length (gmres_restart.h,
+    compiled here as plain C++) against its restatement, over restart
+    ratios across all three bands, the band edges, a non-finite ratio, the
+    wrap below the minimum and the fixed-length settings."""
+    import shutil
+    import subprocess
+
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not available")
+    out = tmp_path / "gmres_restart_check"
+    r = subprocess.run([cxx, "-std=c++17", "-O2", "-I", str(REPO / "tnl-mhfem_gb300" / "csrc"),
+                        str(REPO / "tests" / "gmres_restart_check.cpp"), "-o", str(out)], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    rng = np.random.default_rng(5)
+    edges = [math.cos(math.radians(8.0)), math.cos(math.radians(80.0)),
+             0.5 * (math.cos(math.radians(8.0)) + math.cos(math.radians(80.0)))]
+    cases = []
+    for rule in [(3, 30, 2, 4), (3, 30, 3, 3), (1, 8, 1, 2), (0, 30, 2, 4), (30, 30, 2, 4), (3, 30, 0, 0)]:
+        for m in (30, 29, 12, 5, 4, 3, 1):
+            for cr in list(rng.uniform(0.0, 1.2, 12)) + edges + [0.0, 1.0, float("nan"), float("inf")]:
+                cases.append((*rule, m, cr))
+    text = "\n".join(f"{a} {b} {c} {d} {m} {float(cr)!r}" for a, b, c, d, m, cr in cases) + "\n"
+    r = subprocess.run([str(out)], input=text, capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0
+    got = [int(v) for v in r.stdout.split()]
+    want = [_next_restart(*c) for c in cases]
+    assert got == want

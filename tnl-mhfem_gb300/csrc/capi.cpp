@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 
+#include "gmres_restart.h"
 #include "mhfem_internal.h"
 #include "topology.h"
 
@@ -181,6 +182,9 @@ void mhfem_default_solver_opts(mhfem_solver_opts* o)
     o->linear_solver = MHFEM_SOLVER_BICGSTAB;
     o->gmres_restart = 30;
     o->gmres_variant = MHFEM_GMRES_CGS;
+    o->gmres_restart_min = 0;
+    o->gmres_restart_step_min = 0;
+    o->gmres_restart_step_max = 0;
 }
 
 mhfem_status mhfem_create(const mhfem_desc* desc, mhfem_t* out)
@@ -245,6 +249,7 @@ mhfem_status mhfem_destroy(mhfem_t h)
     h->allocs.clear();
     if (h->W.host_sc) cudaFreeHost(h->W.host_sc);
     if (h->G.host) cudaFreeHost(h->G.host);
+    if (h->G.host_m) cudaFreeHost(h->G.host_m);
     if (h->host_err) cudaFreeHost(h->host_err);
     for (auto& e : h->ev)
         if (e) cudaEventDestroy(e);
@@ -466,6 +471,10 @@ mhfem_status mhfem_set_solver(mhfem_t h, const mhfem_solver_opts* o)
         return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "gmres restart must be 1 to %d", kGmresMaxM);
     if (o->gmres_variant != MHFEM_GMRES_CGS && o->gmres_variant != MHFEM_GMRES_CGSR)
         return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "unknown gmres variant %d", o->gmres_variant);
+    if (o->gmres_restart_min < 0 || o->gmres_restart_min > o->gmres_restart || o->gmres_restart_step_min < 0 ||
+        o->gmres_restart_step_max < 0)
+        return fail(h, MHFEM_ERR_INVALID_ARGUMENT, "gmres restart range %d..%d, steps %d..%d", o->gmres_restart_min,
+                    o->gmres_restart, o->gmres_restart_step_min, o->gmres_restart_step_max);
     const bool regraph = (o->check_every != h->opts.check_every) || (o->gmres_restart != h->opts.gmres_restart) ||
                          (o->gmres_variant != h->opts.gmres_variant);
     h->opts = *o;
@@ -655,6 +664,12 @@ mhfem_status run_gmres(mhfem_t h, double tol, int max_iter, int* iters, double* 
         G.m = m;
     }
     if (!G.host) CK(cudaMallocHost((void**)&G.host, sizeof(GmresCtl)));
+    if (!G.host_m) CK(cudaMallocHost((void**)&G.host_m, sizeof(int32_t)));
+    // adaptive restart length (gmres_restart.h): the first cycle runs m
+    const RestartRule rule{h->opts.gmres_restart_min, m, h->opts.gmres_restart_step_min,
+                           h->opts.gmres_restart_step_max};
+    const bool adaptive = restart_adaptive(rule);
+    int m_cur = m;
     GmresState init{};
     init.tol = tol;
     init.m = m;
@@ -665,6 +680,7 @@ mhfem_status run_gmres(mhfem_t h, double tol, int max_iter, int* iters, double* 
     CK(cudaMemcpyAsync(G.host, &G.st->ctl, sizeof(GmresCtl), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaGetLastError());
+    double res_prev = G.host->res;
     const bool reorth = h->opts.gmres_variant == MHFEM_GMRES_CGSR;
     if (!h->ggm) {
         cudaGraph_t g = nullptr;
@@ -677,7 +693,8 @@ mhfem_status run_gmres(mhfem_t h, double tol, int max_iter, int* iters, double* 
         if (e != cudaSuccess) return fail(h, MHFEM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
     }
     while (!G.host->done) {
-        if (G.host->cycle_end) {
+        const bool restarted = G.host->cycle_end != 0;
+        if (restarted) {
             gmres_update(h->Z_iF, G, rows, h->stream);
             gmres_init(h->A, h->rhs, h->Z_iF, G, h->W, false, h->stream);
             h->launches += 3;
@@ -688,6 +705,17 @@ mhfem_status run_gmres(mhfem_t h, double tol, int max_iter, int* iters, double* 
             h->launches += (reorth ? 4 : 2) * h->opts.check_every;
         }
         CK(cudaStreamSynchronize(h->stream));
+        if (restarted && adaptive && !G.host->done) {
+            // the next cycle's length from the ratio of the true residuals at
+            // the last two restarts; the device reads st->m in every iteration
+            const int next = next_restart(m_cur, res_prev > 0 ? G.host->res / res_prev : 0.0, rule);
+            res_prev = G.host->res;
+            if (next != m_cur) {
+                m_cur = next;
+                *G.host_m = next;
+                CK(cudaMemcpyAsync(&G.st->m, G.host_m, sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+            }
+        }
         if (h->opts.timeout_s > 0 && elapsed_s(t0) > h->opts.timeout_s)
             return fail(h, MHFEM_ERR_TIMEOUT, "Krylov solve exceeded %.1f s", h->opts.timeout_s);
     }

@@ -1,0 +1,55 @@
+// Adaptive restart length of GMRES(m), host side.
+//
+// The reference's example configuration varies the restart length between
+// gmres-restarting-min and gmres-restarting-max in steps between
+// gmres-restarting-step-min and gmres-restarting-step-max
+// (examples/HeatEquation/config.ini: 3, 30, 2, 4).  The rule that applies
+// them lives in TNL's GMRES, which is not in the reference tree; this
+// restates the published strategy those keys parametrize (A. H. Baker,
+// E. R. Jessup, Tz. V. Kolev, "A simple strategy for varying the restart
+// parameter in GMRES(m)", J. Comput. Appl. Math. 230 (2009) 751-761).  With
+// cr = ||r_j|| / ||r_{j-1}||, the ratio of the true residual norms at two
+// consecutive restarts:
+//  - cr > cos(8 deg) (the last cycle stagnated): m = m_max;
+//  - cr < cos(80 deg) (it converged well): m stays;
+//  - otherwise m decreases by the step d, and wraps to m_max when it would
+//    fall below m_min.
+// The paper keeps d fixed.  Here d is step_max when the cycle reduced the
+// residual by more than the middle of that band (cr below the mean of the
+// two cosines) and step_min otherwise, so the length shrinks faster while
+// the cycles still converge well; with step_min == step_max this is the
+// paper's rule.  The first cycle runs m_max.
+//
+// The header compiles as plain C++ too, so the host test suite checks the
+// rule against a restatement.
+#pragma once
+
+#include <cmath>
+
+namespace mhfem {
+
+struct RestartRule {
+    int m_min = 0, m_max = 30;       // m_min == 0 or m_min >= m_max: fixed at m_max
+    int step_min = 0, step_max = 0;  // step_min <= 0: fixed at m_max
+};
+
+inline bool restart_adaptive(const RestartRule& R)
+{
+    return R.m_min > 0 && R.m_min < R.m_max && R.step_min > 0;
+}
+
+// Restart length of the next cycle after a cycle of length m whose restart
+// residual ratio was cr.
+inline int next_restart(int m, double cr, const RestartRule& R)
+{
+    if (!restart_adaptive(R)) return R.m_max;
+    const double max_cr = std::cos(8.0 * 3.14159265358979323846 / 180.0);
+    const double min_cr = std::cos(80.0 * 3.14159265358979323846 / 180.0);
+    if (!(cr <= max_cr)) return R.m_max;  // stagnation (or a non-finite ratio)
+    if (cr < min_cr) return m;
+    const int step_max = R.step_max > R.step_min ? R.step_max : R.step_min;
+    const int d = cr < 0.5 * (min_cr + max_cr) ? step_max : R.step_min;
+    return m - d >= R.m_min ? m - d : R.m_max;
+}
+
+}  // namespace mhfem

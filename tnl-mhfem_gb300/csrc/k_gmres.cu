@@ -10,9 +10,10 @@
 // classical Gram-Schmidt (optionally one reorthogonalization pass), Givens
 // rotations of the Hessenberg matrix, the least-squares solution at the end
 // of a cycle and restarts from the true residual.  The restart length is
-// fixed (gmres-restarting-max); TNL's adaptive choice between
-// gmres-restarting-min and -max is not reproduced, which changes iteration
-// counts, not the converged solution.
+// gmres-restarting-max, or, with gmres-restarting-min and the steps set,
+// varies between the two from cycle to cycle (gmres_restart.h: Baker,
+// Jessup and Kolev's rule, applied by the host between cycles; the device
+// reads the cycle length from its state in every iteration).
 //
 // Design for GB300:
 //  - the basis is stored unnormalized (v_i = inv_i u_i), so no pass only

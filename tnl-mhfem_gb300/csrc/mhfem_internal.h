@@ -193,6 +193,7 @@ struct GmresWork {
     double* partials = nullptr;   // [grid][kGmStride]
     GmresState* st = nullptr;     // device
     GmresCtl* host = nullptr;     // pinned mirror of st->ctl
+    int32_t* host_m = nullptr;    // pinned: the next cycle's restart length (adaptive restarting)
 };
 
 // r = b - A x into u_0 and the restart scalars; first: also ||b|| and it = 0

@@ -59,7 +59,8 @@ class SolverOpts(ct.Structure):
     _fields_ = [("tol", ct.c_double), ("max_iter", ct.c_int32), ("inner_tol", ct.c_double),
                 ("max_sweeps", ct.c_int32), ("check_every", ct.c_int32), ("timeout_s", ct.c_double),
                 ("inner_adaptive", ct.c_int32), ("linear_solver", ct.c_int32), ("gmres_restart", ct.c_int32),
-                ("gmres_variant", ct.c_int32)]
+                ("gmres_variant", ct.c_int32), ("gmres_restart_min", ct.c_int32),
+                ("gmres_restart_step_min", ct.c_int32), ("gmres_restart_step_max", ct.c_int32)]
 
 
 SOLVER_BICGSTAB, SOLVER_GMRES = 0, 1

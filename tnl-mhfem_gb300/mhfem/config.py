@@ -105,6 +105,7 @@ def parse(path, overrides: dict | None = None) -> Config:
         raise ConfigError(f"linear-solver {solver!r} is not a TNL solver name")
     # the solver this library runs: BiCGStab or restarted GMRES (the others map to BiCGStab)
     values["_solver"], values["_gmres_restart"], values["_gmres_variant"] = "bicgstab", 30, "cgs"
+    values["_gmres_restart_min"], values["_gmres_restart_steps"] = 0, (0, 0)
     if solver == "gmres":
         values["_solver"] = "gmres"
         variant = (values["gmres-variant"] or "CGS").upper()
@@ -119,10 +120,15 @@ def parse(path, overrides: dict | None = None) -> Config:
         if restart > 32:
             notices.append(f"gmres-restarting-max = {restart}: restarts after 32 iterations (the longest cycle)")
             restart = 32
-        if values["gmres-restarting-min"] is not None and values["gmres-restarting-min"] != restart:
-            notices.append("gmres-restarting-min/-step: the restart length is fixed at gmres-restarting-max "
-                           f"({restart})")
         values["_gmres_restart"] = int(restart)
+        rmin = values["gmres-restarting-min"]
+        if rmin is not None and 0 < rmin < restart:
+            smin = values["gmres-restarting-step-min"]
+            smax = values["gmres-restarting-step-max"]
+            smin = 3 if smin is None else smin  # the published rule's decrement when no step is given
+            smax = smin if smax is None else max(smax, smin)
+            if smin > 0:
+                values["_gmres_restart_min"], values["_gmres_restart_steps"] = int(rmin), (int(smin), int(smax))
     elif solver != "bicgstab":
         notices.append(f"linear-solver = {solver}: this library's Krylov solvers are BiCGStab and GMRES; it "
                        "runs BiCGStab with the same convergence-residue and max-iterations")

@@ -101,7 +101,9 @@ def run(cfg: config.Config, log: Logger, device: int = 0) -> dict:
         z0 = np.zeros(s.C)
     s.setup(tol=cfg["convergence-residue"], max_iter=min(cfg["max-iterations"], 2 ** 31 - 1),
             inner_tol=cfg["inner-tolerance"], linear_solver=cfg["_solver"], gmres_restart=cfg["_gmres_restart"],
-            gmres_variant=cfg["_gmres_variant"])
+            gmres_variant=cfg["_gmres_variant"], gmres_restart_min=cfg["_gmres_restart_min"],
+            gmres_restart_step_min=cfg["_gmres_restart_steps"][0],
+            gmres_restart_step_max=cfg["_gmres_restart_steps"][1])
     if cfg["solver-form"] == "learned":
         s.learned_options(train_steps=cfg["learned-train-steps"])
     s.setInitialCondition(z0)
@@ -115,7 +117,9 @@ def run(cfg: config.Config, log: Logger, device: int = 0) -> dict:
     log.param("Mesh type:", ("rectangles" if dim == 2 else "cuboids") if box else
               ("triangles" if dim == 2 else "tetrahedra"))
     log.param("Sparse matrix:", "ELL (off-diagonal part, unit diagonal)")
-    log.param("Linear solver:", f"GMRES({cfg['_gmres_restart']}, {cfg['_gmres_variant'].upper()})"
+    restart = (f"{cfg['_gmres_restart_min']}..{cfg['_gmres_restart']}" if cfg["_gmres_restart_min"]
+               else f"{cfg['_gmres_restart']}")
+    log.param("Linear solver:", f"GMRES({restart}, {cfg['_gmres_variant'].upper()})"
               if cfg["_solver"] == "gmres" else "BiCGStab")
     log.param("Mass lumping:", cfg["mass-lumping"])
     log.param("Advection discretization:", "explicit upwind")

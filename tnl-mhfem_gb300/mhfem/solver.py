@@ -151,14 +151,18 @@ class Solver:
 
     def setup(self, tol: float = 1e-10, max_iter: int = 10000, inner_tol: float = 1e-4, max_sweeps: int = 50,
               check_every: int = 8, timeout_s: float = 0.0, inner_adaptive: bool = True,
-              linear_solver: str = "bicgstab", gmres_restart: int = 30, gmres_variant: str = "cgs") -> None:
+              linear_solver: str = "bicgstab", gmres_restart: int = 30, gmres_variant: str = "cgs",
+              gmres_restart_min: int = 0, gmres_restart_step_min: int = 0, gmres_restart_step_max: int = 0) -> None:
         """Solver::setup (Solver.hpp:88-258): the Krylov solver ("bicgstab" or
-        "gmres" with restart length gmres_restart and variant "cgs" / "cgsr"),
-        its tolerance and caps, and the mixed form's inner-solve options."""
+        "gmres" with restart length gmres_restart and variant "cgs" / "cgsr";
+        with gmres_restart_min and the steps set, the restart length varies
+        between gmres_restart_min and gmres_restart), its tolerance and caps,
+        and the mixed form's inner-solve options."""
         solvers = {"bicgstab": L.SOLVER_BICGSTAB, "gmres": L.SOLVER_GMRES}
         variants = {"cgs": L.GMRES_CGS, "cgsr": L.GMRES_CGSR}
         o = L.SolverOpts(tol, max_iter, inner_tol, max_sweeps, check_every, timeout_s, int(inner_adaptive),
-                         solvers[linear_solver.lower()], gmres_restart, variants[gmres_variant.lower()])
+                         solvers[linear_solver.lower()], gmres_restart, variants[gmres_variant.lower()],
+                         gmres_restart_min, gmres_restart_step_min, gmres_restart_step_max)
         self._ck(self.lib.mhfem_set_solver(self._h, ct.byref(o)))
 
     def setInitialCondition(self, Z_iK: np.ndarray, Z_iF: np.ndarray | None = None) -> None:
