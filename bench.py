@@ -454,7 +454,7 @@ def mixed_leg(args, dev, world, el_fp64_ms):
 
 
 def heat2d_leg(args, dev, world):
-    """BASELINE config 1: the plain FP64 heat equation on the 128^2 triangle
+    """The plain FP64 heat equation on the 128^2 triangle
     mesh (49,408 faces), 100 steps of dt = 1e-4 from the Gaussian bump, tol
     1e-12; every step timed, in lockstep with the FP64 form at 1e-13; the CPU
     oracle over the same 100 steps beside it."""
@@ -464,7 +464,7 @@ def heat2d_leg(args, dev, world):
     a = Arm("fp64", _solver(p, dev), dev)
     exact = Arm("exact", _solver(problems.heat2d(N=128), dev, tol=1e-13), dev)
     lockstep([a], exact, p.dt, p.steps)
-    out = {"workload": "heat2d_128 (BASELINE config 1)", "cells": a.sol.C, "faces": a.sol.F, "tol": p.tol,
+    out = {"workload": "heat2d_128", "cells": a.sol.C, "faces": a.sol.F, "tol": p.tol,
            "dt": p.dt, "steps_from_initial_condition": p.steps, "fp64": arm_summary(a, world, full_errors=False)}
     out["fp64"]["face_dof_per_s"] = out["fp64"]["value"] * a.sol.F
     a.close()
@@ -476,7 +476,7 @@ def heat2d_leg(args, dev, world):
 
 
 def adr2d_leg(args, dev, world):
-    """BASELINE config 3: coupled two-component advection-diffusion-reaction on
+    """Coupled two-component advection-diffusion-reaction on
     the 512^2 triangle mesh (n = 2, 1,574,912 rows), 200 steps of dt = 5e-4,
     tol 1e-10; every step timed, in lockstep with the FP64 form at 1e-13."""
     from mhfem import problems
@@ -485,7 +485,7 @@ def adr2d_leg(args, dev, world):
     a = Arm("fp64", _solver(p, dev), dev)
     exact = Arm("exact", _solver(problems.adr2d(N=512), dev, tol=1e-13), dev)
     lockstep([a], exact, p.dt, p.steps)
-    out = {"workload": "adr2d_512 (BASELINE config 3)", "cells": a.sol.C, "faces": a.sol.F, "rows": 2 * a.sol.F,
+    out = {"workload": "adr2d_512", "cells": a.sol.C, "faces": a.sol.F, "rows": 2 * a.sol.F,
            "tol": p.tol, "dt": p.dt, "steps_from_initial_condition": p.steps,
            "fp64": arm_summary(a, world, full_errors=False)}
     out["fp64"]["face_dof_per_s"] = out["fp64"]["value"] * 2 * a.sol.F
@@ -499,7 +499,7 @@ def adr2d_leg(args, dev, world):
 
 
 def mixed128_leg(args, dev, world):
-    """BASELINE config 4: the mixed form on the 128^3 cube (12,582,912
+    """The mixed form on the 128^3 cube (12,582,912
     tetrahedra, 25,264,128 faces), 20 steps from the initial state, with the
     plain FP64 form on the same steps, both in lockstep with the FP64 form
     solved to 1e-13; the assembly kernel timed at this size."""
@@ -513,7 +513,7 @@ def mixed128_leg(args, dev, world):
     exact = Arm("exact", _solver(problems.diffusion3d(N=128), dev, tol=1e-13), dev)
     p = problems.diffusion3d(N=2)
     lockstep([fp, mx], exact, p.dt, steps)
-    out = {"workload": "diffusion3d_128 (BASELINE config 4)", "cells": fp.sol.C, "faces": fp.sol.F, "tol": p.tol,
+    out = {"workload": "diffusion3d_128", "cells": fp.sol.C, "faces": fp.sol.F, "tol": p.tol,
            "dt": p.dt, "inner_tol": 1e-4, "steps_from_initial_condition": steps,
            "fp64": arm_summary(fp, world), "mixed": arm_summary(mx, world)}
     out["mixed"]["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
@@ -535,7 +535,7 @@ def mixed128_leg(args, dev, world):
 
 
 def learned_protocol_leg(args, dev, world):
-    """BASELINE config 5, the whole protocol: the time-varying source
+    """The learned form's whole protocol: the time-varying source
     f = 1 + 0.5 sin(2 pi t / T) psi(x) on the 64^3 workload (T = the
     protocol's span), the network trained online on the first
     `learned_train` steps and used for the next `learned_used`.  Four forms
@@ -575,7 +575,7 @@ def learned_protocol_leg(args, dev, world):
     arms = [fp, mx, ln, lm, bo, l1, b1]
     lockstep(arms, exact, p.dt, total)
     nt = args.learned_train
-    out = {"workload": f"diffusion3d_source_{args.grid} (BASELINE config 5: f = 1 + 0.5 sin(2 pi t/T) psi, "
+    out = {"workload": f"diffusion3d_source_{args.grid} (f = 1 + 0.5 sin(2 pi t/T) psi, "
                        f"T = {total} dt)",
            "train_steps": nt, "used_steps": args.learned_used, "adam_iterations_per_training_step": args.learned_iters,
            "extrapolation_order": args.learned_order,
