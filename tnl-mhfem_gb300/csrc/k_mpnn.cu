@@ -594,16 +594,37 @@ __global__ void __launch_bounds__(256) k_mpnn_dz0(const MpnnView V)
 
 // ---- backward: dW = X^T dZ (split over faces) -----------------------------------
 
-// X = [h_l, a_l] (KF = 128) or x0 (KF = 16, zero-padded to 128 rows).  The
-// staging transposes both operands into K-major tiles over the face index:
-// thread (r, qs) loads 16 features (and 16 dZ columns) of face r with vector
-// loads and scatters them into column r of the tiles.
+// X = [h_l, a_l] (KF = 128) or x0 (KF = 16, zero-padded to 128 rows).  Each
+// CTA accumulates dW over its tiles of 128 faces in TMEM (M = 128 features,
+// N = 64 outputs, K = 128 faces), writes one FP32 partial (summed in a fixed
+// order by k_mpnn_reduce_dw) and its share of db = the sum of dZ over faces.
+// The MMA operands are K-major over the face index, the transpose of the
+// face-major rows in global memory, so a tile is staged in two steps:
+//  1. the CTA copies the tile's rows (X | dZ) with row-coalesced 16-byte
+//     loads (eight lanes per 128-byte row) into a face-major shared tile;
+//  2. each thread assembles 16-byte core-matrix rows (eight consecutive
+//     faces of one feature) from it and stores them into the operand tiles:
+//     a warp reads 32 consecutive features of one face per 2-byte load (no
+//     bank conflicts) and each 8-lane phase of the 16-byte stores fills one
+//     128-byte core matrix.
+// (Loading with a row per thread and scattering 2-byte values into the
+// operand tiles made every load touch 32 rows and every store conflict.)
+template <int KF>
+struct DwShape {
+    static constexpr int XW = KF == 16 ? 16 : 2 * H;  // X columns of a staged face row
+    static constexpr int ROW = XW + H + 8;             // staged row: X | dZ | 16 bytes of padding (bf16)
+};
+constexpr int kDwSmem = (TB + H) * TB * 2 + TB * DwShape<128>::ROW * 2;
+
 template <int KF>
 __global__ void __launch_bounds__(NT) k_mpnn_bwd_dw(const MpnnView V, int layer, float* partials)
 {
     extern __shared__ __align__(128) uint8_t smem[];
-    uint8_t* sA = smem;                // 128 features x 128 faces
-    uint8_t* sB = smem + TB * TB * 2;  // 64 outputs x 128 faces
+    uint8_t* sA = smem;                // 128 features x 128 faces (K-major)
+    uint8_t* sB = smem + TB * TB * 2;  // 64 outputs x 128 faces (K-major)
+    uint8_t* sR = smem + (TB + H) * TB * 2;  // [128 faces][ROW] bf16, face-major
+    constexpr int XW = DwShape<KF>::XW, ROW = DwShape<KF>::ROW;
+    constexpr int XCH = XW / 8, RCH = XCH + H / 8;  // 16-byte chunks of X and of a staged row
     __shared__ uint64_t mbar;
     __shared__ uint32_t tbase;
     __shared__ float red[NT / 32][16];
@@ -629,40 +650,41 @@ __global__ void __launch_bounds__(NT) k_mpnn_bwd_dw(const MpnnView V, int layer,
     for (int q = 0; q < 16; ++q) dbs[q] = 0.f;
     const int64_t ntiles = (F + TB - 1) / TB;
     bool first = true;
-    __nv_bfloat16* sAh = reinterpret_cast<__nv_bfloat16*>(sA);
-    __nv_bfloat16* sBh = reinterpret_cast<__nv_bfloat16*>(sB);
-    auto scatter = [&](__nv_bfloat16* tile, int m0, uint4 v) {
-        const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            const __nv_bfloat162 p = *reinterpret_cast<const __nv_bfloat162*>(&w4[t]);
-            tile[tc::kmajor_offset(m0 + 2 * t, r, TB) / 2] = p.x;
-            tile[tc::kmajor_offset(m0 + 2 * t + 1, r, TB) / 2] = p.y;
-        }
-    };
+    const __nv_bfloat16* hl = V.h[layer];
+    const __nv_bfloat16* al = V.a[layer];
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int64_t row = tile * TB + r;
-        const bool valid = row < F;
-        const uint4 zero = make_uint4(0, 0, 0, 0);
-        if constexpr (KF == 16) {
-            if (qs == 0) {
-                scatter(sAh, 0, valid ? *reinterpret_cast<const uint4*>(V.x0 + row * 16) : zero);
-                scatter(sAh, 8, valid ? *reinterpret_cast<const uint4*>(V.x0 + row * 16 + 8) : zero);
+        // 1. the tile's rows, row-coalesced, into the face-major staging tile
+        for (int idx = tid; idx < TB * RCH; idx += NT) {
+            const int f = idx / RCH, ch = idx - f * RCH;
+            const int64_t row = tile * TB + f;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (row < F) {
+                const __nv_bfloat16* src;
+                if (ch >= XCH) src = V.dz + row * H + 8 * (ch - XCH);
+                else if constexpr (KF == 16) src = V.x0 + row * 16 + 8 * ch;
+                else src = ch < H / 8 ? hl + row * H + 8 * ch : al + row * H + 8 * (ch - H / 8);
+                v = *reinterpret_cast<const uint4*>(src);
             }
+            *reinterpret_cast<uint4*>(sR + (f * ROW + 8 * ch) * 2) = v;
         }
-        else {
+        __syncthreads();
+        // 2. transpose into the K-major operand tiles: column c of the staged
+        //    rows (X: feature c; dZ: output c - XW), faces 8 kg .. 8 kg + 7
+        const uint16_t* sRh = reinterpret_cast<const uint16_t*>(sR);
+        for (int idx = tid; idx < (XW + H) * (TB / 8); idx += NT) {
+            const int kg = idx / (XW + H), c = idx - kg * (XW + H);
+            uint32_t w[4];
 #pragma unroll
-            for (int c = 0; c < 2; ++c) {
-                const int m = 16 * qs + 8 * c;
-                scatter(sAh, m, valid ? *reinterpret_cast<const uint4*>(V.h[layer] + row * H + m) : zero);
-                scatter(sAh, H + m, valid ? *reinterpret_cast<const uint4*>(V.a[layer] + row * H + m) : zero);
-            }
+            for (int j = 0; j < 4; ++j)
+                w[j] = (uint32_t)sRh[(8 * kg + 2 * j) * ROW + c] | ((uint32_t)sRh[(8 * kg + 2 * j + 1) * ROW + c] << 16);
+            const uint4 v = make_uint4(w[0], w[1], w[2], w[3]);
+            if (c < XW) st_tile(sA, c, 8 * kg, TB, v);
+            else st_tile(sB, c - XW, 8 * kg, TB, v);
         }
+        // db: thread (r, qs) adds dZ[r][16 qs .. 16 qs + 15]
 #pragma unroll
         for (int c = 0; c < 2; ++c) {
-            const int n = 16 * qs + 8 * c;
-            const uint4 v = valid ? *reinterpret_cast<const uint4*>(V.dz + row * H + n) : zero;
-            scatter(sBh, n, v);
+            const uint4 v = *reinterpret_cast<const uint4*>(sR + (r * ROW + XW + 16 * qs + 8 * c) * 2);
             const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
@@ -863,7 +885,7 @@ void mpnn_backward(const MpnnView& V, const double* target, double inv_nt, MpnnG
     k_mpnn_decode<<<gdec, 256, 0, s>>>(V, target, inv_nt);
     k_mpnn_reduce_dec<<<1, 128, 0, s>>>(V.dec_partials, gdec, G.g + G.off_wd, G.g + G.off_bd, G.loss, inv_nt);
     const int smdx = smem_req(kDxSmem);
-    const int smdw = smem_req((TB + H) * TB * 2);
+    const int smdw = smem_req(kDwSmem);
     set_smem(k_mpnn_bwd_dx, smdx);
     set_smem(k_mpnn_bwd_dw<128>, smdw);
     set_smem(k_mpnn_bwd_dw<16>, smdw);
