@@ -346,6 +346,18 @@ mhfem_status mhfem_get_stream(mhfem_t h, void** stream);
 mhfem_status mhfem_time_kernel(mhfem_t h, int32_t kernel, int32_t reps, double* ms_per_launch,
                                double* bytes_per_launch, double* flops_per_launch);
 
+/* Check of the bounded grid barrier that the small-system FP64 BiCGStab
+ * (systems of at most 2^18 rows, one cooperative launch per solve) places
+ * between its phases.  One cooperative launch of `ctas` CTAs on `device`
+ * passes through the barrier once, every wait polling at most `max_polls`
+ * times; CTA `skip_cta` (none if negative) never arrives, so the others'
+ * waits run out, set the failure flag and return -- the kernel ends without
+ * a fault or a hang and the context stays usable.  Returns the CTAs that
+ * passed and that gave up, and the flag (the solve turns it into
+ * MHFEM_ERR_CUDA).  The launch allocates a few bytes of device memory. */
+mhfem_status mhfem_check_grid_barrier(int32_t device, int32_t ctas, int32_t skip_cta, int32_t max_polls,
+                                      int32_t* ctas_passed, int32_t* ctas_gave_up, int32_t* failure_flag);
+
 /* ---- learned warm start (MHFEM_FORM_LEARNED) ----------------------------
  * No counterpart in the reference: a message-passing network over the face
  * adjacency graph (3 layers, hidden width 64, BF16 weights, FP32

@@ -1078,6 +1078,25 @@ mhfem_status mhfem_get_stream(mhfem_t h, void** stream)
     return MHFEM_OK;
 }
 
+mhfem_status mhfem_check_grid_barrier(int32_t device, int32_t ctas, int32_t skip_cta, int32_t max_polls,
+                                      int32_t* ctas_passed, int32_t* ctas_gave_up, int32_t* failure_flag)
+{
+    if (!ctas_passed || !ctas_gave_up || !failure_flag || ctas < 1 || max_polls < 1)
+        return MHFEM_ERR_INVALID_ARGUMENT;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return MHFEM_ERR_NO_DEVICE;
+    if (device < 0 || device >= n) return MHFEM_ERR_INVALID_ARGUMENT;
+    if (cudaSetDevice(device) != cudaSuccess) return MHFEM_ERR_CUDA;
+    int passed = 0, gave_up = 0, flag = 0;
+    const cudaError_t e = grid_barrier_check(ctas, skip_cta, (unsigned int)max_polls, &passed, &gave_up, &flag);
+    if (e == cudaErrorInvalidValue) return MHFEM_ERR_INVALID_ARGUMENT;
+    if (e != cudaSuccess) return MHFEM_ERR_CUDA;
+    *ctas_passed = passed;
+    *ctas_gave_up = gave_up;
+    *failure_flag = flag;
+    return MHFEM_OK;
+}
+
 mhfem_status mhfem_time_kernel(mhfem_t h, int32_t kernel, int32_t reps, double* ms, double* bytes, double* flops)
 {
     mhfem_status st = require_ready(h);

@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <initializer_list>
 #include <type_traits>
+#include <vector>
 
 #include "fp_convert.h"
 #include "krylov_common.cuh"
@@ -807,7 +808,8 @@ __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p)
 // (the count starts at 0 for a launch and grows by gridDim.x per barrier)
 // and wait for every CTA.  False (in every thread of the CTA) when the wait
 // gave up.
-__device__ __forceinline__ bool grid_barrier(unsigned int* count, int* err, unsigned int target)
+__device__ __forceinline__ bool grid_barrier(unsigned int* count, int* err, unsigned int target,
+                                             unsigned int max_polls = kBarrierPolls)
 {
     __shared__ int ok;
     __syncthreads();
@@ -817,7 +819,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* count, int* err, unsi
         atomicAdd(count, 1u);
         unsigned int polls = 0;
         while (ld_acquire_u32(count) < target) {
-            if (++polls > kBarrierPolls || *(volatile int*)err != 0) {
+            if (++polls > max_polls || *(volatile int*)err != 0) {
                 good = 0;
                 atomicExch(err, 1);
                 break;
@@ -829,6 +831,20 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* count, int* err, unsi
     }
     __syncthreads();
     return ok != 0;
+}
+
+// Check of the bounded barrier: every CTA but `skip` (none if negative)
+// arrives once and reports 1 (passed) or 0 (gave up); CTA `skip` never
+// arrives and reports -1, so the others' waits run out after max_polls.
+__global__ void __launch_bounds__(KB) k_grid_barrier_check(unsigned int* count, int* err, int skip,
+                                                           unsigned int max_polls, int* result)
+{
+    if ((int)blockIdx.x == skip) {
+        if (threadIdx.x == 0) result[blockIdx.x] = -1;
+        return;
+    }
+    const bool ok = grid_barrier(count, err, gridDim.x, max_polls);
+    if (threadIdx.x == 0) result[blockIdx.x] = ok ? 1 : 0;
 }
 
 // Sum of the per-CTA partials [cta][kPartStride] in CTA order, identical in
@@ -1464,6 +1480,40 @@ cudaError_t krylov_small_fp64(const EllMatrix& A, double* x, KrylovWork& W, int 
     MHFEM_WIDTH_DISPATCH(A.width, e = cudaLaunchCooperativeKernel((const void*)k_bicgstab_small<WW>, dim3(grid), dim3(KB),
                                                                  args, 0, s));
     return e;
+}
+
+cudaError_t grid_barrier_check(int ctas, int skip, unsigned int max_polls, int* passed, int* gave_up, int* flag)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    int nb = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_grid_barrier_check, KB, 0);
+    if (e != cudaSuccess) return e;
+    if (ctas < 1 || ctas > nb * sm_count(dev)) return cudaErrorInvalidValue;
+    unsigned int* buf = nullptr;  // [0] arrival count, [1] failure flag, [2 ..] per-CTA results
+    e = cudaMalloc(&buf, sizeof(unsigned int) * (2 + (size_t)ctas));
+    if (e != cudaSuccess) return e;
+    std::vector<int> res((size_t)ctas + 2, 0);
+    e = cudaMemset(buf, 0, sizeof(unsigned int) * (2 + (size_t)ctas));
+    if (e == cudaSuccess) {
+        unsigned int* count = buf;
+        int* err = reinterpret_cast<int*>(buf + 1);
+        int* result = reinterpret_cast<int*>(buf + 2);
+        void* args[] = {(void*)&count, (void*)&err, (void*)&skip, (void*)&max_polls, (void*)&result};
+        e = cudaLaunchCooperativeKernel((const void*)k_grid_barrier_check, dim3(ctas), dim3(KB), args, 0, 0);
+        if (e == cudaSuccess) e = cudaMemcpy(res.data(), buf, sizeof(int) * (2 + (size_t)ctas), cudaMemcpyDeviceToHost);
+    }
+    cudaFree(buf);
+    if (e != cudaSuccess) return e;
+    *passed = 0;
+    *gave_up = 0;
+    for (int b = 0; b < ctas; ++b) {
+        *passed += res[2 + b] == 1;
+        *gave_up += res[2 + b] == 0;
+    }
+    *flag = res[1];
+    return cudaSuccess;
 }
 
 void mixed_apply_correction(double* x, KrylovWork& W, cudaStream_t s)

@@ -211,6 +211,10 @@ void krylov_iterate_fp64(const EllMatrix& A, double* x, KrylovWork& W, int iters
 // (non-zero after a barrier wait gave up).
 int64_t krylov_small_rows();
 cudaError_t krylov_small_fp64(const EllMatrix& A, double* x, KrylovWork& W, int iters, cudaStream_t s);
+// One cooperative launch of `ctas` CTAs through the small-system solve's
+// bounded grid barrier, CTA `skip` (none if negative) never arriving; counts
+// the CTAs that passed and that gave up, and returns the failure flag.
+cudaError_t grid_barrier_check(int ctas, int skip, unsigned int max_polls, int* passed, int* gave_up, int* flag);
 
 // mixed: outer residual r = b - A x (FP64) -> sc; scale into r32; inner FP32 solve; x += scale*e
 void mixed_outer_residual(const EllMatrix& A, const double* b, const double* x, KrylovWork& W,

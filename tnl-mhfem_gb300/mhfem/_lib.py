@@ -123,6 +123,7 @@ SIGNATURES = [
     ("mhfem_get_totals", ct.c_int32, [_P, _pi64, _pi64, _pi64]),
     ("mhfem_get_stream", ct.c_int32, [_P, ct.POINTER(ct.c_void_p)]),
     ("mhfem_time_kernel", ct.c_int32, [_P, ct.c_int32, ct.c_int32, _pd, _pd, _pd]),
+    ("mhfem_check_grid_barrier", ct.c_int32, [ct.c_int32, ct.c_int32, ct.c_int32, ct.c_int32, _pi32, _pi32, _pi32]),
     ("mhfem_learned_set_options", ct.c_int32, [_P, ct.POINTER(LearnedOpts)]),
     ("mhfem_learned_get_params", ct.c_int32, [_P, ct.POINTER(ct.c_float), ct.c_int64]),
     ("mhfem_learned_set_params", ct.c_int32, [_P, ct.POINTER(ct.c_float), ct.c_int64]),
