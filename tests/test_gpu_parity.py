@@ -12,7 +12,7 @@ import dataclasses
 import numpy as np
 import pytest
 
-from helpers import golden_case, golden_names, rel_err, small_cases
+from helpers import golden_case, golden_names, rel_err, small_cases, variant
 from mhfem import _lib as L
 from mhfem import problems
 from oracle.oracle import OracleModel
@@ -87,6 +87,51 @@ def test_step_parity(name):
 
 def p_faces(s):
     return s.F
+
+
+def _form_step_parity(name, form, **setup):
+    """Every step of the case in the given form against the FP64 oracle at
+    the FP64 bar, both solved to 1e-13 (the mobility-upwind cases start each
+    step from the GPU's velocities, as in test_step_parity)."""
+    p = variant(CASES[name], form=form)
+    s, m = _pair(p)
+    s.setup(tol=1e-13, max_iter=20000, check_every=4, **setup)
+    n, C = p.n, p.C
+    nf = p.config.faces_per_cell
+    t = 0.0
+    for step in range(p.steps):
+        if p.config.mobility_upwind and step > 0:
+            m.v_iKe[:] = s.array("v_iKe", n * nf * C)
+        st = s.step(t, p.dt)
+        m.step(t, p.dt, 1e-13)
+        zf, zk = s.state()
+        assert st["residual"] < 1e-13
+        assert rel_err(zf, m.Z_iF) < TOL_STATE, f"step {step}: Z_iF"
+        assert rel_err(zk, m.Z_iK) < TOL_STATE, f"step {step}: Z_iK"
+        t += p.dt
+    s.close()
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_mixed_step_parity(name):
+    """The mixed form (FP32 inner BiCGStab, FP64 iterative refinement) on
+    every model case, refined to 1e-13: its FP64 outer residuals take it to
+    FP64 accuracy, so it meets the FP64 form's 1e-10 bar against the oracle
+    after every step -- n = 1 to 3, lumping, the advection schemes, mobility
+    upwinding, box cells and the dummy-equation rows, through the FP32
+    kernels of every ELL width."""
+    _form_step_parity(name, L.FORM_MIXED, max_sweeps=60)
+
+
+LEARNED_CASES = [n for n in sorted(CASES) if CASES[n].n == 1 and CASES[n].config.cell == L.CELL_SIMPLEX]
+
+
+@pytest.mark.parametrize("name", LEARNED_CASES)
+def test_learned_step_parity(name):
+    """The learned form (one equation, simplex cells) on the model cases:
+    its initial guess only changes where the FP64 solve starts, so every
+    step meets the FP64 bar against the oracle."""
+    _form_step_parity(name, L.FORM_LEARNED)
 
 
 @pytest.mark.parametrize("name", golden_names())
