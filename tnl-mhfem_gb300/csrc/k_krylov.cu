@@ -781,7 +781,10 @@ __global__ void __launch_bounds__(KB) k_update_p(int64_t rows, T* p, const T* r,
 // five-kernel iteration bound by launch and drain latency: about 30 us per
 // iteration for a few microseconds of memory traffic.  Here one cooperative
 // launch (every CTA resident) runs a chunk of iterations:
-//  - the five phases of an iteration are separated by grid barriers;
+//  - an iteration is three phases separated by grid barriers (below:
+//    k_bicgstab_small), the p and s updates being formed where they are
+//    gathered; measured on the 128^2 system: 24.7 us per iteration against
+//    26.8 us with five phases and 30.6 us for the five-kernel iteration;
 //  - each reduction's per-CTA partials are summed by every CTA itself, in
 //    the same fixed order, so every CTA holds the same scalars (in shared
 //    memory) with no last-block step, and the result is deterministic;
