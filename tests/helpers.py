@@ -54,8 +54,16 @@ def small_cases():
                                             coeffs={"a": np.asarray(p.coeffs["a"]) * 0.02})
     cases["adr2d_mobility"] = variant(p, mobility_upwind=True,
                                       coeffs={"m": np.random.default_rng(3).uniform(0.5, 2.0, 2 * p.C)})
-    # two components on tetrahedra with coupled reaction and a full w field
-    p3 = problems.diffusion3d(N=3, steps=2)
+    cases["diffusion3d_n2"] = diffusion3d_n2(3)
+    cases.update(three_component_cases())
+    cases.update(box_cases())
+    cases.update(dummy_row_cases())
+    return cases
+
+
+def diffusion3d_n2(N: int, steps: int = 2) -> problems.Problem:
+    """Two components on tetrahedra with coupled reaction and a full w field."""
+    p3 = problems.diffusion3d(N=N, steps=steps)
     C = p3.C
     rng = np.random.default_rng(11)
     Nc = np.zeros((2, 2, C)); Nc[0, 0] = 1.0; Nc[1, 1] = 2.0
@@ -72,11 +80,7 @@ def small_cases():
     q = variant(p3, n_eq=2, coeffs={"N": Nc.ravel(), "D": D.ravel(), "r": r.ravel(), "w": w.ravel(), "f": 0.5})
     q.bc_fn = bc2
     q.Z0 = rng.uniform(0, 1, 2 * C)
-    cases["diffusion3d_n2"] = q
-    cases.update(three_component_cases())
-    cases.update(box_cases())
-    cases.update(dummy_row_cases())
-    return cases
+    return q
 
 
 def isolated_interior_cells(cells: np.ndarray, stride: int = 5) -> np.ndarray:

@@ -12,7 +12,7 @@ import dataclasses
 import numpy as np
 import pytest
 
-from helpers import golden_case, golden_names, rel_err, small_cases, variant
+from helpers import diffusion3d_n2, golden_case, golden_names, rel_err, small_cases, variant
 from mhfem import _lib as L
 from mhfem import problems
 from oracle.oracle import OracleModel
@@ -220,6 +220,24 @@ def test_adr2d_full_size():
     assert rel_err(zk, m.Z_iK) < TOL_STATE
     rowptr, cols, _, _ = s.system()
     assert np.array_equal(rowptr, m.rowptr) and np.array_equal(cols, m.cols)
+    s.close()
+
+
+def test_diffusion3d_n2_large():
+    """Two components on the 24^3 tetrahedral mesh (338,688 rows, ELL width
+    13, above the small-system size: the five-kernel FP64 iteration at that
+    width): 2 steps against the oracle."""
+    p = diffusion3d_n2(24)
+    s, m = _pair(p, check_every=8)
+    assert s.F * 2 > 1 << 18
+    t = 0.0
+    for _ in range(p.steps):
+        s.step(t, p.dt)
+        m.step(t, p.dt, 1e-13)
+        t += p.dt
+    zf, zk = s.state()
+    assert rel_err(zf, m.Z_iF) < TOL_STATE
+    assert rel_err(zk, m.Z_iK) < TOL_STATE
     s.close()
 
 
