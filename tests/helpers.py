@@ -253,6 +253,67 @@ def three_component_cases():
     return cases
 
 
+def _restrict(p: problems.Problem, keep) -> problems.Problem:
+    """p on the cells `keep` only (n = 1; vertices renumbered in order of use)."""
+    q = variant(p)
+    cells = p.cells[keep]
+    used, inv = np.unique(cells.ravel(), return_inverse=True)
+    q.coords = p.coords[used]
+    q.cells = inv.reshape(cells.shape).astype(p.cells.dtype)
+    for k, v in p.coeffs.items():
+        if np.ndim(v) and np.size(v) == p.C:
+            q.coeffs[k] = np.asarray(v)[keep]
+    q.Z0 = np.asarray(p.Z0)[keep]
+    return q
+
+
+def _flux_bc(values=0.5, dirichlet=1.0):
+    """Every boundary face carries the flux `values` (FixedFlux) except the
+    first face, a Dirichlet face with value `dirichlet`."""
+    def bc_fn(face_verts, face_cells):
+        F = face_cells.shape[0]
+        tags = np.full(F, 1, np.uint8)
+        tags[0] = 0
+        vals = np.full(F, values)
+        return tags, vals, np.full(F, dirichlet)
+    return bc_fn
+
+
+def minimal_cases():
+    """The smallest meshes: one cell (every face on the boundary), including
+    a system that is the identity (every face Dirichlet: no off-diagonal
+    entry, ELL width 0), and the one-square / one-cube splits whose cells
+    share faces; n = 2 on the two-triangle square."""
+    cases = {}
+    p = problems.heat2d(N=1, steps=3)
+    q = _restrict(p, [0])
+
+    def all_dirichlet(face_verts, face_cells):
+        F = face_cells.shape[0]
+        return np.zeros(F, np.uint8), np.zeros(F), np.linspace(-0.7, 1.1, F)
+    q.bc_fn = all_dirichlet
+    cases["one_triangle_dirichlet"] = q
+    q = _restrict(p, [1])
+    q.bc_fn = _flux_bc()
+    cases["one_triangle"] = q
+    q = problems.heat2d(N=1, steps=3)
+    q.bc_fn = _flux_bc(-0.25, 0.5)
+    cases["one_square"] = q
+    p = problems.diffusion3d(N=1, steps=3)
+    q = _restrict(p, [0])
+    q.bc_fn = _flux_bc()
+    cases["one_tetrahedron"] = q
+    cases["one_cube"] = p
+    q = problems.heat2d_rect(N=1, steps=3)
+    q.bc_fn = _flux_bc()
+    cases["one_rectangle"] = q
+    q = problems.diffusion3d_box(N=1, steps=3)
+    q.bc_fn = _flux_bc(0.25, -1.0)
+    cases["one_cuboid"] = q
+    cases["one_square_n2"] = problems.adr2d(N=1, steps=3)
+    return cases
+
+
 def golden_names():
     return sorted(f.stem for f in GOLDEN.glob("*.npz"))
 

@@ -510,7 +510,8 @@ mhfem_status ensure_pattern(mhfem_t h)
     h->A.rows = rows;
     h->A.width = W;
     CK(dalloc(h, &h->A.cols, (size_t)W * rows));
-    CK(cudaMemcpy(h->A.cols, h->pat.ell_cols.data(), sizeof(int32_t) * W * rows, cudaMemcpyHostToDevice));
+    if (W > 0)  // width 0: every row is its unit diagonal (all faces Dirichlet)
+        CK(cudaMemcpy(h->A.cols, h->pat.ell_cols.data(), sizeof(int32_t) * W * rows, cudaMemcpyHostToDevice));
     CK(dalloc(h, &h->A.vals, (size_t)W * rows));
     CK(cudaMemset(h->A.vals, 0, sizeof(double) * W * rows));
     if (h->fp32_copy) {
@@ -813,6 +814,8 @@ mhfem_status mhfem::run_mixed(mhfem_t h, int* iters, int* sweeps, double* res)
         total_inner += inner.it;
         if (inner.status == KS_NOTFINITE)
             return fail(h, MHFEM_ERR_NOT_FINITE, "FP32 inner solve produced a non-finite value");
+        if (inner.status == KS_BREAKDOWN && inner.it == 0)  // no correction: the next sweep would repeat it
+            return fail(h, MHFEM_ERR_BREAKDOWN, "mixed-precision refinement: FP32 BiCGStab breakdown in its first iteration");
         mixed_apply_correction(h->Z_iF, h->W, h->stream);
         h->launches += 1;
     }
@@ -1010,7 +1013,8 @@ mhfem_status mhfem_get_system(mhfem_t h, int64_t* rowptr, int32_t* cols, double*
     const int64_t rows = h->pat.rows;
     const int W = h->pat.W;
     std::vector<double> ev((size_t)W * rows);
-    CK(cudaMemcpyAsync(ev.data(), h->A.vals, sizeof(double) * W * rows, cudaMemcpyDeviceToHost, h->stream));
+    if (W > 0)
+        CK(cudaMemcpyAsync(ev.data(), h->A.vals, sizeof(double) * W * rows, cudaMemcpyDeviceToHost, h->stream));
     if (rhs) CK(cudaMemcpyAsync(rhs, h->rhs, sizeof(double) * rows, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     int64_t pos = 0;
@@ -1046,7 +1050,8 @@ mhfem_status mhfem_get_system32(mhfem_t h, float* vals32)
     const int64_t rows = h->pat.rows;
     const int W = h->pat.W;
     std::vector<float> ev((size_t)W * rows);
-    CK(cudaMemcpyAsync(ev.data(), h->A.vals32, sizeof(float) * W * rows, cudaMemcpyDeviceToHost, h->stream));
+    if (W > 0)
+        CK(cudaMemcpyAsync(ev.data(), h->A.vals32, sizeof(float) * W * rows, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     int64_t pos = 0;
     for (int64_t r = 0; r < rows; ++r) {

@@ -499,7 +499,18 @@ __device__ __forceinline__ void scalars_omega(KrylovScalars* sc, const double (&
     sc->ts = sum[0];
     sc->tt = sum[1];
     if (!finite(sum[0]) || !finite(sum[1])) { sc->status = KS_NOTFINITE; sc->done = 1; }
-    else if (sum[1] == 0) { sc->status = KS_BREAKDOWN; sc->done = 1; }
+    else if (sum[1] == 0) {
+        if constexpr (CHECK) { sc->status = KS_BREAKDOWN; sc->done = 1; }  // ||s|| >= tol, yet A s = 0
+        else {
+            // A s = 0 on an iteration that does not form ||s||: the matrix is
+            // nonsingular, so s = 0 and x + alpha p solves the system -- the
+            // half step, which the reference's loop takes on its ||s|| test
+            // (a system whose every row is its unit diagonal gets here on
+            // the first iteration)
+            sc->snorm = 0;
+            sc->half = 1;
+        }
+    }
     else sc->omega = sum[0] / sum[1];
 }
 
