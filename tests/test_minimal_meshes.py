@@ -5,10 +5,12 @@ one-square and one-cube splits whose cells share faces, and n = 2 on the
 two-triangle square.
 
 CPU: the oracle solves every case and holds each Dirichlet face at its value.
-GPU: the FP64 BiCGStab, mixed-precision and GMRES paths against the oracle
-after every step, at the bars of test_gpu_parity.py (face numbering and the
-pattern bit-exact, traces and cell values within 1e-10, both sides solved to
-1e-13).
+GPU: the FP64 BiCGStab, mixed-precision and GMRES paths, and the learned
+form on the one-equation simplex meshes (training in every step, the network
+and its gate over a graph of 0 to 6 neighbours per face, all inside one
+128-face tile), against the oracle after every step, at the bars of
+test_gpu_parity.py (face numbering and the pattern bit-exact, traces and cell
+values within 1e-10, both sides solved to 1e-13).
 """
 import numpy as np
 import pytest
@@ -46,8 +48,14 @@ def test_oracle_minimal_mesh(name):
         assert int(np.diff(m.rowptr).max()) == 1  # every row is its diagonal only
 
 
+FORMS = {"fp64": L.FORM_FP64, "mixed": L.FORM_MIXED, "gmres": L.FORM_FP64, "learned": L.FORM_LEARNED}
+# the learned form takes one equation on simplex cells
+PAIRS = [(name, form) for name in sorted(CASES) for form in FORMS
+         if form != "learned" or (CASES[name].n == 1 and CASES[name].config.cell == L.CELL_SIMPLEX)]
+
+
 def _solver(p, form):
-    q = variant(p, form=L.FORM_MIXED if form == "mixed" else L.FORM_FP64)
+    q = variant(p, form=FORMS[form])
     q.tol = 1e-13
     s = problems.make_solver(q, check_every=4)
     opts = {"tol": 1e-13, "max_iter": 20000, "check_every": 4}
@@ -60,8 +68,7 @@ def _solver(p, form):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("form", ["fp64", "mixed", "gmres"])
-@pytest.mark.parametrize("name", sorted(CASES))
+@pytest.mark.parametrize("name,form", PAIRS)
 def test_minimal_mesh_parity(name, form):
     q, s = _solver(CASES[name], form)
     m = OracleModel.from_problem(q)
