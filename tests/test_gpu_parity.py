@@ -303,6 +303,31 @@ def test_mixed_128_cube():
     sf.close()
 
 
+def test_128_cube_against_oracle():
+    """The largest workload (the 128^3 cube: 25,264,128 face rows, 176M
+    nonzeros) against the oracle for one step: the FP64 form and the mixed
+    form both solved to 1e-13, face traces and cell values within 1e-10 of the
+    oracle's, the CSR pattern bit-exact."""
+    p = problems.diffusion3d(N=128, steps=1)
+    s, m = _pair(p, check_every=8)
+    pm = variant(p, form=L.FORM_MIXED)
+    sm = problems.make_solver(pm, check_every=8)
+    sm.setup(tol=1e-13, max_iter=20000, check_every=8, max_sweeps=60)
+    assert s.F == 25264128 and s.C == 12582912
+    a = s.step(0.0, p.dt)
+    b = sm.step(0.0, p.dt)
+    m.step(0.0, p.dt, 1e-13)
+    assert a["residual"] < 1e-13 and b["residual"] < 1e-13
+    for sv in (s, sm):
+        zf, zk = sv.state()
+        assert rel_err(zf, m.Z_iF) < TOL_STATE
+        assert rel_err(zk, m.Z_iK) < TOL_STATE
+    sm.close()
+    rowptr, cols, _, _ = s.system()
+    assert np.array_equal(rowptr, m.rowptr) and np.array_equal(cols, m.cols)
+    s.close()
+
+
 def test_mixed_fp32_matrix_is_the_rounded_fp64_matrix():
     """The mixed form's FP32 copy of the assembled values (converted on the
     integer pipes) equals the FP64 values rounded to nearest even, bit for
