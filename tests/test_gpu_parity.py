@@ -278,10 +278,10 @@ def test_mixed_box():
 
 def test_mixed_128_cube():
     """Mixed precision on the 128^3 cube (12,582,912 tetrahedra, 25,264,128
-    faces), where the CPU oracle is too slow: 2 steps at tol 1e-12, face
-    traces and cell values within 1e-8 of the GPU FP64 form (checked against
-    the oracle at 64^3 above), the final FP64 residual below the tolerance in
-    every step."""
+    faces) over 2 steps at tol 1e-12: face traces and cell values within 1e-8
+    of the GPU FP64 form, the final FP64 residual below the tolerance in
+    every step (one step of both forms against the oracle:
+    test_128_cube_against_oracle)."""
     p = problems.diffusion3d(N=128, steps=2, form=L.FORM_MIXED)
     p.tol = 1e-12  # at 1e-10 the two forms already differ by ~1.5e-8 through the tolerance alone
     sm = problems.make_solver(p, check_every=8)
