@@ -55,18 +55,33 @@ mhfem_status set_coef_device(mhfem_t h, int which, const double* data, int64_t c
         CK(dalloc(h, &h->coef[which].p, (size_t)count));
     }
     const bool dev = is_device_pointer(data);
-    h->h_coef[which].resize(count);
     CK(cudaMemcpyAsync(h->coef[which].p, data, sizeof(double) * count,
                        dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
-    if (dev)
-        CK(cudaMemcpyAsync(h->h_coef[which].data(), data, sizeof(double) * count, cudaMemcpyDeviceToHost, h->stream));
-    else
-        std::copy(data, data + count, h->h_coef[which].begin());
     h->coef[which].count = count;
-    CK(cudaStreamSynchronize(h->stream));
-    bool nz = false;
-    for (int64_t q = 0; q < count && !nz; ++q) nz = (h->h_coef[which][q] != 0.0);
-    h->coef_nonzero[which] = nz;
+    // A host copy is kept only where the host reads the values: the zero
+    // test of the advection coefficients (it selects the advection terms of
+    // the kernels) and the learned form's static features (D, f, psi).  A
+    // per-step upload of a full field (the source f of a time-varying
+    // model) then costs its transfer and no host-side copy.
+    const bool flag = which == MHFEM_COEF_A || which == MHFEM_COEF_U;
+    const bool shadow = flag || (h->desc.form == MHFEM_FORM_LEARNED &&
+                                 (which == MHFEM_COEF_D || which == MHFEM_COEF_F || which == MHFEM_COEF_PSI));
+    if (shadow) {
+        h->h_coef[which].resize(count);
+        if (dev)
+            CK(cudaMemcpyAsync(h->h_coef[which].data(), data, sizeof(double) * count, cudaMemcpyDeviceToHost,
+                               h->stream));
+        else
+            std::copy(data, data + count, h->h_coef[which].begin());
+    }
+    else
+        std::vector<double>().swap(h->h_coef[which]);
+    CK(cudaStreamSynchronize(h->stream));  // the caller may reuse its buffer on return
+    if (flag) {
+        bool nz = false;
+        for (int64_t q = 0; q < count && !nz; ++q) nz = (h->h_coef[which][q] != 0.0);
+        h->coef_nonzero[which] = nz;
+    }
     return MHFEM_OK;
 }
 

@@ -82,7 +82,8 @@ struct mhfem_solver_s {
     bool guess_timed = false;
     std::vector<void*> allocs;
 
-    // host copies used to build the learned form's static features
+    // host copies: the coordinates and (learned form) D, f, psi build the
+    // learned form's static features; a and u give the advection zero test
     std::vector<double> h_coords;
     std::vector<double> h_coef[NCOEF];
     mhfem::LearnedState* learned = nullptr;
