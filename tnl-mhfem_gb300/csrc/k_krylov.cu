@@ -919,6 +919,42 @@ __device__ __forceinline__ double small_row(const int32_t* __restrict__ cols, co
     return acc;
 }
 
+// The ELL words of one row held in registers for a whole launch (the
+// matrix does not change during a solve).
+template <int WW>
+struct SmallEll {
+    int32_t c[WW > 0 ? WW : 1];
+    double a[WW > 0 ? WW : 1];
+};
+
+template <int WW>
+__device__ __forceinline__ void small_load(const int32_t* __restrict__ cols, const double* __restrict__ vals,
+                                           int64_t rows, int64_t q, SmallEll<WW>& e)
+{
+#pragma unroll
+    for (int k = 0; k < WW; ++k) {
+        e.c[k] = __ldg(cols + (int64_t)k * rows + q);
+        e.a[k] = __ldg(vals + (int64_t)k * rows + q);
+    }
+}
+
+template <int WW, typename G>
+__device__ __forceinline__ double small_apply(const SmallEll<WW>& e, double self, G&& g)
+{
+    double xg[WW > 0 ? WW : 1];
+#pragma unroll
+    for (int k = 0; k < WW; ++k) xg[k] = g(e.c[k]);
+    double acc = self;
+#pragma unroll
+    for (int k = 0; k < WW; ++k) acc = fma(e.a[k], xg[k], acc);
+    return acc;
+}
+
+// Rows per thread whose ELL words stay in registers for the launch: two for
+// the compile-time widths up to 6, one for the wider ones, none for the
+// run-time width.
+constexpr int small_rows_in_registers(int WW) { return WW == 0 ? 0 : (WW <= 6 ? 2 : 1); }
+
 // Three phases and three grid barriers per iteration: the p update of the
 // previous iteration and the s update are formed where they are needed,
 // for the own rows and again for each gathered neighbour (the same
@@ -949,6 +985,39 @@ __global__ void __launch_bounds__(KB) k_bicgstab_small(const int32_t* __restrict
     double* pa = partials;
     double* pc = partials + (int64_t)nb * kPartStride;
     double* pd = partials + 2 * (int64_t)nb * kPartStride;
+    // The ELL words of the thread's first RK rows, loaded once: both SpMVs of
+    // every iteration then start with the gathers, one L2 round trip instead
+    // of two behind each grid barrier.
+    constexpr int RK = small_rows_in_registers(WW);
+    SmallEll<WW> er[RK > 0 ? RK : 1];
+#pragma unroll
+    for (int j = 0; j < RK; ++j) {
+        const int64_t q = gtid + (int64_t)j * gstride;
+        if (q < rows) small_load<WW>(cols, vals, rows, q, er[j]);
+    }
+    // y = A x over the thread's rows with x given by xval (own row and
+    // gathered neighbours); the register rows first, all their loads ahead of
+    // their stores, then any further rows from the matrix in memory.
+    auto spmv_rows = [&](auto&& xval, auto&& finish) {
+        double xr[RK > 0 ? RK : 1], yr[RK > 0 ? RK : 1];
+#pragma unroll
+        for (int j = 0; j < RK; ++j) {
+            const int64_t q = gtid + (int64_t)j * gstride;
+            if (q < rows) {
+                xr[j] = xval(q);
+                yr[j] = small_apply<WW>(er[j], xr[j], xval);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < RK; ++j) {
+            const int64_t q = gtid + (int64_t)j * gstride;
+            if (q < rows) finish(q, xr[j], yr[j]);
+        }
+        for (int64_t q = gtid + (int64_t)RK * gstride; q < rows; q += gstride) {
+            const double xq = xval(q);
+            finish(q, xq, small_row<WW>(cols, vals, W, rows, q, xq, xval));
+        }
+    };
     for (int k = 0; k < max_its; ++k) {
         const int cur = S.it & 1;
         const double* P = cur ? p1 : p0;
@@ -964,16 +1033,14 @@ __global__ void __launch_bounds__(KB) k_bicgstab_small(const int32_t* __restrict
                 return fresh ? rj : fma(beta, fma(-omega, __ldcg(V + j), __ldcg(P + j)), rj);
             };
             double acc[1] = {0};
-            for (int64_t q = gtid; q < rows; q += gstride) {
-                const double pq = pval(q);
-                const double y = small_row<WW>(cols, vals, W, rows, q, pq, pval);
+            spmv_rows(pval, [&](int64_t q, double pq, double y) {
                 Pn[q] = pq;
                 Vn[q] = y;
                 double hq;
                 if (fresh) { hq = __ldcg(r + q); rh[q] = hq; }
                 else hq = rh[q];
                 acc[0] = fma(hq, y, acc[0]);
-            }
+            });
             block_reduce_store<double, 1>(acc, pa);
             if (!grid_barrier(bar, bar_err, target += nb)) return;
             double sum[1];
@@ -987,15 +1054,13 @@ __global__ void __launch_bounds__(KB) k_bicgstab_small(const int32_t* __restrict
         {
             auto sval = [&](int64_t j) { return fma(-alpha, __ldcg(Vn + j), __ldcg(r + j)); };
             double acc[3] = {0, 0, 0};
-            for (int64_t q = gtid; q < rows; q += gstride) {
-                const double sv = sval(q);
-                const double y = small_row<WW>(cols, vals, W, rows, q, sv, sval);
+            spmv_rows(sval, [&](int64_t q, double sv, double y) {
                 s[q] = sv;
                 t[q] = y;
                 acc[0] = fma(y, sv, acc[0]);
                 acc[1] = fma(y, y, acc[1]);
                 acc[2] = fma(sv, sv, acc[2]);
-            }
+            });
             block_reduce_store<double, 3>(acc, pc);
             if (!grid_barrier(bar, bar_err, target += nb)) return;
             double sum[3];
