@@ -830,9 +830,11 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* count, int* err, unsi
     if (threadIdx.x == 0) {
         int good = 1;
         __threadfence();
-        atomicAdd(count, 1u);
+        // the last CTA to arrive sees the target in its own add and does not
+        // poll: it is the one the others wait for in the next phase too
+        const unsigned int seen = atomicAdd(count, 1u) + 1u;
         unsigned int polls = 0;
-        while (ld_acquire_u32(count) < target) {
+        while (seen < target && ld_acquire_u32(count) < target) {
             if (++polls > max_polls || *(volatile int*)err != 0) {
                 good = 0;
                 atomicExch(err, 1);
