@@ -418,7 +418,7 @@ mhfem_status mhfem_learned_status(mhfem_t h, int32_t* trained_steps, double* las
  * solve and a system with any other index is refused with
  * MHFEM_ERR_INVALID_ARGUMENT (nothing else runs).
  * All work vectors live in one static device array of fixed size (about
- * 12.8 MB), so systems with more than MHFEM_NOALLOC_MAX_ROWS rows are
+ * 17 MB), so systems with more than MHFEM_NOALLOC_MAX_ROWS rows are
  * rejected with MHFEM_ERR_INVALID_ARGUMENT.  Under CUDA's default lazy module
  * loading that array is committed on a device at the FIRST call there (which
  * looks its address up with cudaGetSymbolAddress and may synchronize the
@@ -427,14 +427,19 @@ mhfem_status mhfem_learned_status(mhfem_t h, int32_t* trained_steps, double* las
  * initialization, before any stream capture.  Every call shares the array:
  * calls that overlap on the GPU (other streams, other threads) race and must
  * be serialized by the caller.
+ * The solve is the persistent small-system BiCGStab that mhfem_solve runs
+ * for systems of this size (one cooperative launch per chunk of up to 256
+ * iterations, the convergence test in every iteration), so the two entry
+ * points return the same iterates.
  * The call blocks until the solve ends: at most max_iter iterations, and at
- * most timeout_s seconds of wall-clock time when timeout_s > 0 (checked every
- * 8 iterations, after the queued work has drained; then MHFEM_ERR_TIMEOUT).
- * Returns MHFEM_OK, MHFEM_ERR_NOT_CONVERGED, MHFEM_ERR_BREAKDOWN or
- * MHFEM_ERR_NOT_FINITE like mhfem_solve.  *residual is the relative residual
- * ||b - Ax|| / ||b|| of the last iteration that formed it (every 8th
- * iteration and the converged one): on MHFEM_ERR_NOT_CONVERGED and
- * MHFEM_ERR_TIMEOUT it can be up to 7 iterations older than x. */
+ * most timeout_s seconds of wall-clock time when timeout_s > 0 (checked
+ * between chunks, after the queued work has drained; then
+ * MHFEM_ERR_TIMEOUT).  Returns MHFEM_OK, MHFEM_ERR_NOT_CONVERGED,
+ * MHFEM_ERR_BREAKDOWN or MHFEM_ERR_NOT_FINITE like mhfem_solve, and
+ * MHFEM_ERR_CUDA if a grid barrier wait of the solve ran out (no fault: the
+ * context stays usable).  *residual is the relative residual ||b - Ax|| /
+ * ||b|| of the last iteration: on MHFEM_ERR_TIMEOUT that of the last
+ * completed chunk. */
 #define MHFEM_NOALLOC_MAX_ROWS 262144
 mhfem_status mhfem_bicgstab_noalloc(const int32_t* cols, const double* vals, int32_t width, int64_t rows,
                                     const double* rhs, double* x, double tol, int32_t max_iter, double timeout_s,

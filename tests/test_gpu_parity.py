@@ -241,6 +241,24 @@ def test_diffusion3d_n2_large():
     s.close()
 
 
+def test_heat2d_above_small_system_size():
+    """The heat equation on a 300^2 triangle mesh (270,600 rows, ELL width
+    4, just above the persistent small-system size): the five-kernel FP64
+    iteration at width 4, 2 steps against the oracle."""
+    p = problems.heat2d(N=300, steps=2)
+    s, m = _pair(p, check_every=8)
+    assert s.F > 1 << 18
+    t = 0.0
+    for _ in range(p.steps):
+        s.step(t, p.dt)
+        m.step(t, p.dt, 1e-13)
+        t += p.dt
+    zf, zk = s.state()
+    assert rel_err(zf, m.Z_iF) < TOL_STATE
+    assert rel_err(zk, m.Z_iK) < TOL_STATE
+    s.close()
+
+
 def test_box_full_size():
     """Box cells at full size: 128^2 graded rectangles (3 steps) and 64^3
     graded cuboids (2 steps) against the oracle; the pattern bit-exact."""

@@ -8,10 +8,8 @@ caller-side buffers from the assembled systems of the 128^2 heat-equation
 workload (49,408 rows) and of a 7^2 grid (161 rows, an odd count), solve them
 through the new entry point, and compare the solutions with the ones
 mhfem_solve (the existing entry point) returns from the same warm start, on
-two consecutive time steps.  At these sizes mhfem_solve runs the persistent
-small-system kernel (one cooperative launch per solve) while the
-allocation-free entry point runs the five-kernel iteration, so the
-comparison also checks the two FP64 BiCGStab paths against each other.  They also check that a repeated call leaves the
+two consecutive time steps (both run the persistent small-system solve at
+these sizes).  They also check that a repeated call leaves the
 device's free memory unchanged, that a system beyond the size limit or with
 a column index outside the system is refused, and that the wall-clock limit
 ends a solve that cannot converge with MHFEM_ERR_TIMEOUT.

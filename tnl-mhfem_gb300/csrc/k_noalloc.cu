@@ -9,7 +9,10 @@
 // right-hand side and the solution; this entry point borrows nothing else.
 //
 // The Krylov work vectors, the per-CTA partial sums and the device scalars
-// live in one file-scope static device array of fixed size (about 12.8 MB).
+// live in one file-scope static device array of fixed size (about 17 MB).
+// Every system it takes fits the persistent small-system solve (one
+// cooperative launch per chunk of 256 iterations, the convergence test in
+// every iteration), which mhfem_solve runs for the same sizes.
 // Under CUDA's lazy module loading the array is committed on a device at the
 // first call there (the cudaGetSymbolAddress below loads the module), not when
 // the library is loaded, and it stays until the process exits; systems with
@@ -24,10 +27,13 @@ namespace {
 
 constexpr int64_t kMaxRows = MHFEM_NOALLOC_MAX_ROWS;   // even: the vectors below are spaced by an even count
 constexpr int64_t kMaxGrid = 4096;                     // per-CTA partials (>= any Krylov grid here)
-constexpr int64_t kVecDoubles = 6 * kMaxRows;          // r, rh, p, v, s, t
+constexpr int64_t kVecDoubles = 8 * kMaxRows;          // r, rh, p, v, s, t and the second p, v buffers
 constexpr int64_t kPartialDoubles = 8 * kMaxGrid;
 constexpr int64_t kScalarDoubles = (sizeof(mhfem::KrylovScalars) + 7) / 8;
-constexpr int64_t kCounterDoubles = 2;                 // 4 uint32: [0] reduction ticket, [2] bad-column count
+// 8 uint32: [0] reduction ticket, [2] grid-barrier count and [3] its failure
+// flag (the small-system solve), [4] bad-column count
+constexpr int64_t kCounterDoubles = 4;
+constexpr int kBadColumns = 4;
 constexpr int64_t kScratchDoubles = kVecDoubles + kPartialDoubles + kScalarDoubles + kCounterDoubles;
 
 // The scratch.  Host code must not use this name as a device address: in host
@@ -108,31 +114,39 @@ extern "C" mhfem_status mhfem_bicgstab_noalloc(const int32_t* cols, const double
     W.v = base + 3 * ld;
     W.s = base + 4 * ld;
     W.t = base + 5 * ld;
+    W.p2 = base + 6 * ld;
+    W.v2 = base + 7 * ld;
     W.partials = base + kVecDoubles;
     W.sc = reinterpret_cast<mhfem::KrylovScalars*>(base + kVecDoubles + kPartialDoubles);
     W.counters = reinterpret_cast<uint32_t*>(base + kVecDoubles + kPartialDoubles + kScalarDoubles);
     if (W.grid > kMaxGrid) return MHFEM_ERR_UNSUPPORTED;
 
-    // the ticket counter and the bad-column count must start at zero; every
-    // other scratch word is written before it is read
+    // the ticket counter, the barrier words and the bad-column count must
+    // start at zero; every other scratch word is written before it is read
     if (cudaMemsetAsync(W.counters, 0, kCounterDoubles * sizeof(double), s) != cudaSuccess) return MHFEM_ERR_CUDA;
     if (width > 0) {
         const int64_t count = (int64_t)width * rows;
         const unsigned grid = (unsigned)std::min<int64_t>((count + 255) / 256, 1024);
-        k_check_cols<<<grid, 256, 0, s>>>(cols, count, rows, W.counters + 2);
+        k_check_cols<<<grid, 256, 0, s>>>(cols, count, rows, W.counters + kBadColumns);
         if (cudaGetLastError() != cudaSuccess) return MHFEM_ERR_CUDA;
         uint32_t bad = 0;
-        if (cudaMemcpyAsync(&bad, W.counters + 2, sizeof(bad), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        if (cudaMemcpyAsync(&bad, W.counters + kBadColumns, sizeof(bad), cudaMemcpyDeviceToHost, s) != cudaSuccess)
             return MHFEM_ERR_CUDA;
         if (cudaStreamSynchronize(s) != cudaSuccess) return MHFEM_ERR_CUDA;
         if (bad != 0) return MHFEM_ERR_INVALID_ARGUMENT;  // a column outside [0, rows): nothing else was queued
     }
     mhfem::krylov_init_fp64(A, rhs, x, W, tol, max_iter, s);
     if (cudaGetLastError() != cudaSuccess) return MHFEM_ERR_CUDA;
+    const bool small = rows <= mhfem::krylov_small_rows();  // always, at this size limit
     mhfem::KrylovScalars hs{};
+    int32_t barrier_failed = 0;
     for (;;) {
         if (cudaMemcpyAsync(&hs, W.sc, sizeof(hs), cudaMemcpyDeviceToHost, s) != cudaSuccess) return MHFEM_ERR_CUDA;
+        if (small && cudaMemcpyAsync(&barrier_failed, W.counters + 3, sizeof(barrier_failed), cudaMemcpyDeviceToHost,
+                                     s) != cudaSuccess)
+            return MHFEM_ERR_CUDA;
         if (cudaStreamSynchronize(s) != cudaSuccess) return MHFEM_ERR_CUDA;
+        if (barrier_failed) return MHFEM_ERR_CUDA;  // a grid barrier wait ran out (the context stays usable)
         if (hs.done) break;
         // the stream has drained here, so the shared scratch is idle when the limit ends the call
         if (timeout_s > 0 && elapsed_s(t0) > timeout_s) {
@@ -140,7 +154,11 @@ extern "C" mhfem_status mhfem_bicgstab_noalloc(const int32_t* cols, const double
             if (residual) *residual = hs.res;
             return MHFEM_ERR_TIMEOUT;
         }
-        mhfem::krylov_iterate_fp64(A, x, W, 8, s);
+        if (small) {
+            if (mhfem::krylov_small_fp64(A, x, W, 256, s) != cudaSuccess) return MHFEM_ERR_CUDA;
+        }
+        else
+            mhfem::krylov_iterate_fp64(A, x, W, 8, s);
         if (cudaGetLastError() != cudaSuccess) return MHFEM_ERR_CUDA;
     }
     if (iterations) *iterations = hs.it;
