@@ -748,13 +748,23 @@ mhfem_status mhfem::run_fp64(mhfem_t h, double tol, int max_iter, int* iters, do
     if (h->opts.linear_solver == MHFEM_SOLVER_GMRES) return run_gmres(h, tol, max_iter, iters, res);
     const auto t0 = std::chrono::steady_clock::now();
     krylov_init_fp64(h->A, h->rhs, h->Z_iF, h->W, tol, max_iter, h->stream);
-    if (h->A.rows <= krylov_small_rows() && h->W.p2 && h->W.v2) {
+    bool small = h->A.rows <= krylov_small_rows() && h->W.p2 && h->W.v2;
+    if (small) {
         // small system: chunks of iterations in one persistent launch each
         // (k_bicgstab_small), one host round trip per chunk
         constexpr int kChunk = 256;
         h->launches += 1;
-        for (;;) {
-            CK(krylov_small_fp64(h->A, h->Z_iF, h->W, kChunk, h->stream));
+        for (bool first = true;; first = false) {
+            const cudaError_t e = krylov_small_fp64(h->A, h->Z_iF, h->W, kChunk, h->stream);
+            if (first && e == cudaErrorCooperativeLaunchTooLarge) {
+                // the device cannot hold the grid at once (a partitioned or
+                // shared GPU): nothing ran, so the five-kernel iteration
+                // below starts from the same initial state
+                cudaGetLastError();
+                small = false;
+                break;
+            }
+            CK(e);
             h->launches += 1;
             CK(cudaMemcpyAsync(h->W.host_sc, h->W.sc, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, h->stream));
             CK(cudaMemcpyAsync(h->host_err, h->W.counters + 3, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
@@ -765,9 +775,11 @@ mhfem_status mhfem::run_fp64(mhfem_t h, double tol, int max_iter, int* iters, do
             if (h->opts.timeout_s > 0 && elapsed_s(t0) > h->opts.timeout_s)
                 return fail(h, MHFEM_ERR_TIMEOUT, "Krylov solve exceeded %.1f s", h->opts.timeout_s);
         }
-        *iters = h->W.host_sc->it;
-        *res = h->W.host_sc->res;
-        return status_from_krylov(h, *h->W.host_sc, "FP64 BiCGStab");
+        if (small) {
+            *iters = h->W.host_sc->it;
+            *res = h->W.host_sc->res;
+            return status_from_krylov(h, *h->W.host_sc, "FP64 BiCGStab");
+        }
     }
     CK(cudaMemcpyAsync(h->W.host_sc, h->W.sc, sizeof(KrylovScalars), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));

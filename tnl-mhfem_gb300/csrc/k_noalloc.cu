@@ -137,10 +137,10 @@ extern "C" mhfem_status mhfem_bicgstab_noalloc(const int32_t* cols, const double
     }
     mhfem::krylov_init_fp64(A, rhs, x, W, tol, max_iter, s);
     if (cudaGetLastError() != cudaSuccess) return MHFEM_ERR_CUDA;
-    const bool small = rows <= mhfem::krylov_small_rows();  // always, at this size limit
+    bool small = rows <= mhfem::krylov_small_rows();  // always, at this size limit
     mhfem::KrylovScalars hs{};
     int32_t barrier_failed = 0;
-    for (;;) {
+    for (bool first = true;; first = false) {
         if (cudaMemcpyAsync(&hs, W.sc, sizeof(hs), cudaMemcpyDeviceToHost, s) != cudaSuccess) return MHFEM_ERR_CUDA;
         if (small && cudaMemcpyAsync(&barrier_failed, W.counters + 3, sizeof(barrier_failed), cudaMemcpyDeviceToHost,
                                      s) != cudaSuccess)
@@ -155,10 +155,17 @@ extern "C" mhfem_status mhfem_bicgstab_noalloc(const int32_t* cols, const double
             return MHFEM_ERR_TIMEOUT;
         }
         if (small) {
-            if (mhfem::krylov_small_fp64(A, x, W, 256, s) != cudaSuccess) return MHFEM_ERR_CUDA;
+            const cudaError_t e = mhfem::krylov_small_fp64(A, x, W, 256, s);
+            if (first && e == cudaErrorCooperativeLaunchTooLarge) {
+                // the device cannot hold the grid at once (a partitioned or
+                // shared GPU): nothing ran, the five-kernel iteration goes on
+                cudaGetLastError();
+                small = false;
+            }
+            else if (e != cudaSuccess)
+                return MHFEM_ERR_CUDA;
         }
-        else
-            mhfem::krylov_iterate_fp64(A, x, W, 8, s);
+        if (!small) mhfem::krylov_iterate_fp64(A, x, W, 8, s);
         if (cudaGetLastError() != cudaSuccess) return MHFEM_ERR_CUDA;
     }
     if (iterations) *iterations = hs.it;
