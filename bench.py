@@ -179,7 +179,7 @@ def step_bytes(n, nf, S, C, F, V, W, iters, d_full=True):
         + 8 * n * n * S * C + 8 * n * n * nf * C + 8 * n * C + rec
     assemble = 15 * F + rec + 8 * W * R + 8 * R
     init = R * (12 * W + 8 + 8 + 8 + 24)
-    per_iter = R * (24 * W + 160)
+    per_iter = R * (24 * W + 152)  # SpMVs 12W + 24 and 12W + 16, updates 24 + 56 + 32
     recon = 4 * nf * C + 8 * n * F + 8 * n * n * nf * C + 16 * n * C
     return cell + assemble + init + iters * per_iter + recon
 

@@ -1,6 +1,8 @@
 """The benchmark's JSON line, on the CPU: the reference arm (the oracle port,
 OpenMP on the host's cores) on a small grid prints the keys the contract
-asks for."""
+asks for; the roofline's DRAM traffic comes from the committed ncu summary
+with the commit it was captured on; the per-iteration byte model is the
+documented one."""
 import json
 import os
 import subprocess
@@ -28,3 +30,30 @@ def test_reference_arm_json_line():
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] == len(os.sched_getaffinity(0))
     assert "8^3" in d["cpu_baseline"]["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def _bench():
+    sys.path.insert(0, str(REPO))
+    import bench
+    return bench
+
+
+def test_roofline_traffic_names_its_capture():
+    bench = _bench()
+    summary = (REPO / "profiles" / "iteration_kernels_fp64_diffusion3d64.txt").read_text()
+    for name in ("spmv_dot", "spmv_dots2"):
+        value, source = bench.ncu_traffic(name, 64)
+        line = [l.split() for l in summary.splitlines() if l.startswith(f"traffic {name} ")][0]
+        assert value == float(line[2]) and source.endswith(f"ncu capture of commit {line[3]}")
+        assert f"captured on commit {line[3]}" in summary
+    assert bench.ncu_traffic("spmv_dots2", 32) == (None, None)  # captured at 64^3 only
+
+
+def test_iteration_bytes_model():
+    """One FP64 BiCGStab iteration moves R (24 W + 160) bytes: the two SpMVs
+    (12 W + 24 and 12 W + 16 per row) and the s, x / r and p updates (24, 56
+    and 32 per row); 296 bytes per row at width 6."""
+    bench = _bench()
+    n, nf, S, C, F, V, W = 1, 4, 14, 1572864, 3170304, 274625, 6
+    per_iter = bench.step_bytes(n, nf, S, C, F, V, W, 1) - bench.step_bytes(n, nf, S, C, F, V, W, 0)
+    assert per_iter == F * ((12 * W + 24) + (12 * W + 16) + 24 + 56 + 32) == F * 296

@@ -31,6 +31,14 @@ def test_library_exports_every_declared_symbol():
     assert set(declared) == bound, "ctypes signatures out of sync with the header"
 
 
+def test_integration_table_names_every_entry_point():
+    """INTEGRATION.md's entry-point table (the reference interface each call
+    replaces) lists every function the header declares."""
+    text = (REPO / "INTEGRATION.md").read_text()
+    missing = [name for name in _declared_symbols() if f"`{name}" not in text]
+    assert not missing, f"entry points missing from INTEGRATION.md: {missing}"
+
+
 def test_create_without_device_fails_loudly():
     import torch
 
