@@ -690,6 +690,12 @@ mhfem_status run_gmres(mhfem_t h, double tol, int max_iter, int* iters, double* 
     init.tol = tol;
     init.m = m;
     init.max_iter = max_iter;
+    init.m_min = rule.m_min;
+    init.m_max = rule.m_max;
+    init.step_min = rule.step_min;
+    init.step_max = rule.step_max;
+    init.max_cr = restart_max_cr();
+    init.min_cr = restart_min_cr();
     CK(cudaMemcpyAsync(G.st, &init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
     gmres_init(h->A, h->rhs, h->Z_iF, G, h->W, true, h->stream);
     h->launches += 1;
@@ -698,6 +704,38 @@ mhfem_status run_gmres(mhfem_t h, double tol, int max_iter, int* iters, double* 
     CK(cudaGetLastError());
     double res_prev = G.host->res;
     const bool reorth = h->opts.gmres_variant == MHFEM_GMRES_CGSR;
+    if (rows <= krylov_small_rows() && !G.host->done) {
+        // small system: chunks of iterations, restarts included, in one
+        // persistent launch each (k_gmres_small), one host round trip per
+        // chunk; the device applies the restart rule
+        CK(cudaMemcpyAsync(&G.st->res_prev, &res_prev, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        constexpr int kChunk = 256;
+        bool small = true;
+        for (bool first = true;; first = false) {
+            const cudaError_t e = gmres_small(h->A, h->rhs, h->Z_iF, G, h->W, reorth, kChunk, h->stream);
+            if (first && e == cudaErrorCooperativeLaunchTooLarge) {
+                // the device cannot hold the grid at once: nothing ran, the
+                // graph of iterations below goes on from the same state
+                cudaGetLastError();
+                small = false;
+                break;
+            }
+            CK(e);
+            h->launches += 1;
+            CK(cudaMemcpyAsync(G.host, &G.st->ctl, sizeof(GmresCtl), cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaMemcpyAsync(h->host_err, h->W.counters + 3, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+            if (*h->host_err) return fail(h, MHFEM_ERR_CUDA, "GMRES (small system): a grid barrier wait gave up");
+            if (G.host->done) break;
+            if (h->opts.timeout_s > 0 && elapsed_s(t0) > h->opts.timeout_s)
+                return fail(h, MHFEM_ERR_TIMEOUT, "Krylov solve exceeded %.1f s", h->opts.timeout_s);
+        }
+        if (small) {
+            *iters = G.host->it;
+            *res = G.host->res;
+            return status_from_gmres(h, *G.host);
+        }
+    }
     if (!h->ggm) {
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));

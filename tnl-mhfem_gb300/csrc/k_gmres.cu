@@ -30,8 +30,10 @@
 //  - every iteration kernel returns at once when the cycle has ended or the
 //    solve is done, so the host replays a CUDA graph of several iterations
 //    between checks.
+#include <algorithm>
 #include <initializer_list>
 
+#include "gmres_restart.h"
 #include "krylov_common.cuh"
 
 namespace mhfem {
@@ -272,6 +274,218 @@ __global__ void __launch_bounds__(KB) k_gm_update_x(int64_t rows, const double* 
     }
 }
 
+// ---- small systems: one persistent launch per chunk of iterations ----------------
+//
+// On a system of a few ten thousand rows the two kernels of an Arnoldi
+// iteration are bound by launch, drain and last-block latency (53 us per
+// iteration on the 128^2 heat-equation system).  Here one cooperative
+// launch runs up to `max_its` iterations, restarts included:
+//  A. z = A u_j -> u_{j+1} and the dot products (z, u_i), i <= j, in chunks
+//     of kGmChunk basis vectors (with the reorthogonalization, A2: u_{j+1}
+//     -= sum c_i u_i and the dot products again, into a second partials
+//     region);
+//  B. u_{j+1} -= sum c_i u_i and ||u_{j+1}||^2;
+//  then, at the end of a cycle: x += sum_i y_i inv_i u_i, a barrier (the
+//  residual gathers other CTAs' x), r = b - A x -> u_0 and ||r||^2, and the
+//  next cycle's length by the adaptive rule (gmres_restart.h).
+// Every CTA sums the partials in CTA order and keeps its own copy of the
+// solve state (Hessenberg column rotations, least-squares solve) in shared
+// memory, applying the same operations to the same values, so all copies
+// stay identical and the result is deterministic.  Barrier waits are
+// bounded as in k_bicgstab_small.
+template <int WW, bool REORTH>
+__global__ void __launch_bounds__(KB) k_gmres_small(const int32_t* __restrict__ cols,
+                                                    const double* __restrict__ vals, int W, int64_t rows,
+                                                    const double* __restrict__ b, double* x, double* U,
+                                                    GmresState* st, double* pdots, double* pnorm,
+                                                    unsigned int* bar, int* bar_err, int max_its)
+{
+    __shared__ GmresState S;
+    __shared__ double d[kGmDots];
+    {
+        // the state, copied word by word
+        const unsigned long long* src = reinterpret_cast<const unsigned long long*>(st);
+        unsigned long long* dst = reinterpret_cast<unsigned long long*>(&S);
+        for (int k = threadIdx.x; k < (int)(sizeof(GmresState) / 8); k += KB) dst[k] = src[k];
+    }
+    __syncthreads();
+    if (S.ctl.done) return;
+    const int64_t gstride = (int64_t)gridDim.x * KB;
+    const int64_t gtid = (int64_t)blockIdx.x * KB + threadIdx.x;
+    const unsigned int nb = gridDim.x;
+    unsigned int target = 0;
+    double* pd0 = pdots;
+    double* pd1 = pdots + (int64_t)nb * kGmStride;
+    // the dot products (w, u_i), i <= j, of the own rows into partials pd
+    // (w = u_{j+1}, formed first as A u_j when SPMV)
+    auto dots = [&](int j, bool spmv, double* pd) {
+        const double* uj = U + (int64_t)j * rows;
+        double* un = U + (int64_t)(j + 1) * rows;
+        for (int c0 = 0; c0 <= j; c0 += kGmChunk) {
+            const int n = (j + 1 - c0 < kGmChunk) ? j + 1 - c0 : kGmChunk;
+            double acc[kGmChunk];
+#pragma unroll
+            for (int k = 0; k < kGmChunk; ++k) acc[k] = 0;
+            for (int64_t q = gtid; q < rows; q += gstride) {
+                double z;
+                if (spmv && c0 == 0) {
+                    z = small_row<WW>(cols, vals, W, rows, q, uj[q], [&](int64_t c) { return __ldcg(uj + c); });
+                    un[q] = z;
+                }
+                else
+                    z = un[q];
+                if (n == kGmChunk) {
+#pragma unroll
+                    for (int k = 0; k < kGmChunk; ++k) acc[k] = fma(z, U[(int64_t)(c0 + k) * rows + q], acc[k]);
+                }
+                else
+                    for (int k = 0; k < n; ++k) acc[k] = fma(z, U[(int64_t)(c0 + k) * rows + q], acc[k]);
+            }
+            gm_block_dots(acc, c0, n, pd);
+        }
+    };
+    // u_{j+1} -= sum_{i <= j} c_i u_i over the own rows; returns sum t^2 when NORM
+    auto orth = [&](int j, bool norm) {
+        double* un = U + (int64_t)(j + 1) * rows;
+        double acc = 0;
+        for (int64_t q = gtid; q < rows; q += gstride) {
+            double t = un[q];
+#pragma unroll 4
+            for (int i = 0; i <= j; ++i) t = fma(-S.c[i], U[(int64_t)i * rows + q], t);
+            un[q] = t;
+            if (norm) acc = fma(t, t, acc);
+        }
+        return acc;
+    };
+    for (int it = 0; it < max_its; ++it) {
+        const int j = S.j;
+        // A. z = A u_j, h_ij, c_i
+        dots(j, true, pd0);
+        if (!grid_barrier(bar, bar_err, target += nb)) return;
+        gm_final_dots(pd0, j, d);
+        if (threadIdx.x == 0) {
+            const double invj = S.inv[j];
+            for (int i = 0; i <= j; ++i) {
+                const double invi = S.inv[i];
+                S.H[i][j] = invj * invi * d[i];
+                S.c[i] = invi * invi * d[i];
+            }
+        }
+        __syncthreads();
+        if constexpr (REORTH) {
+            // A2. u_{j+1} -= sum c_i u_i, then the dot products again
+            orth(j, false);
+            dots(j, false, pd1);
+            if (!grid_barrier(bar, bar_err, target += nb)) return;
+            gm_final_dots(pd1, j, d);
+            if (threadIdx.x == 0) {
+                const double invj = S.inv[j];
+                for (int i = 0; i <= j; ++i) {
+                    const double invi = S.inv[i];
+                    S.H[i][j] += invj * invi * d[i];
+                    S.c[i] = invi * invi * d[i];
+                }
+            }
+            __syncthreads();
+        }
+        // B. u_{j+1} -= sum c_i u_i, ||u_{j+1}||, the rotations, the cycle's end
+        {
+            double acc[1] = {orth(j, true)};
+            block_reduce_store<double, 1>(acc, pnorm);
+            if (!grid_barrier(bar, bar_err, target += nb)) return;
+            double sum[1];
+            grid_sums<1>(pnorm, sum);
+            if (threadIdx.x == 0) {
+                GmresCtl& C = S.ctl;
+                const double nrm = sqrt(sum[0]);
+                const double hn = S.inv[j] * nrm;  // h_{j+1,j}
+                for (int k = 0; k < j; ++k) {
+                    const double a = S.H[k][j], bb = S.H[k + 1][j];
+                    S.H[k][j] = S.cs[k] * a + S.sn[k] * bb;
+                    S.H[k + 1][j] = -S.sn[k] * a + S.cs[k] * bb;
+                }
+                const double a = S.H[j][j];
+                const double den = sqrt(a * a + hn * hn);
+                const double cs = den > 0 ? a / den : 1.0, sn = den > 0 ? hn / den : 0.0;
+                S.cs[j] = cs;
+                S.sn[j] = sn;
+                S.H[j][j] = den;
+                S.g[j + 1] = -sn * S.g[j];
+                S.g[j] = cs * S.g[j];
+                S.inv[j + 1] = nrm > 0 ? 1.0 / nrm : 0.0;
+                const double res = fabs(S.g[j + 1]) / C.bnorm;
+                C.res = res;
+                C.it += 1;
+                S.j = j + 1;
+                if (!finite(res) || !finite(den)) { C.status = KS_NOTFINITE; C.done = 1; }
+                else if (res < S.tol || j + 1 >= S.m || nrm == 0 || C.it >= S.max_iter) C.cycle_end = 1;
+            }
+            __syncthreads();
+        }
+        if (S.ctl.done) break;
+        if (!S.ctl.cycle_end) continue;
+        // the end of the cycle: y from R y = g, x += sum_i y_i inv_i u_i
+        if (threadIdx.x == 0) {
+            const int k = S.j;
+            double y[kGmresMaxM];
+            for (int i = k - 1; i >= 0; --i) {
+                double sacc = S.g[i];
+                for (int l = i + 1; l < k; ++l) sacc -= S.H[i][l] * y[l];
+                y[i] = sacc / S.H[i][i];
+            }
+            for (int i = 0; i < kGmDots; ++i) S.c[i] = (i < k) ? y[i] * S.inv[i] : 0.0;
+        }
+        __syncthreads();
+        {
+            const int k = S.j;
+            for (int64_t q = gtid; q < rows; q += gstride) {
+                double t = x[q];
+#pragma unroll 4
+                for (int i = 0; i < k; ++i) t = fma(S.c[i], U[(int64_t)i * rows + q], t);
+                x[q] = t;
+            }
+        }
+        if (!grid_barrier(bar, bar_err, target += nb)) return;
+        // the restart: r = b - A x -> u_0, the true residual, the next length
+        {
+            double acc[1] = {0};
+            for (int64_t q = gtid; q < rows; q += gstride) {
+                const double r = b[q] - small_row<WW>(cols, vals, W, rows, q, x[q], [&](int64_t c) { return __ldcg(x + c); });
+                U[q] = r;
+                acc[0] = fma(r, r, acc[0]);
+            }
+            block_reduce_store<double, 1>(acc, pnorm);
+            if (!grid_barrier(bar, bar_err, target += nb)) return;
+            double sum[1];
+            grid_sums<1>(pnorm, sum);
+            if (threadIdx.x == 0) {
+                GmresCtl& C = S.ctl;
+                const double beta = sqrt(sum[0]);
+                C.res = beta / C.bnorm;
+                S.g[0] = beta;
+                S.inv[0] = beta > 0 ? 1.0 / beta : 0.0;
+                S.j = 0;
+                C.cycle_end = 0;
+                if (!finite(C.res)) { C.status = KS_NOTFINITE; C.done = 1; }
+                else if (C.res < S.tol) { C.status = KS_CONVERGED; C.done = 1; }
+                else if (C.it >= S.max_iter) { C.status = KS_MAXITER; C.done = 1; }
+                else {
+                    const RestartRule R{S.m_min, S.m_max, S.step_min, S.step_max};
+                    S.m = next_restart_with(S.m, S.res_prev > 0 ? C.res / S.res_prev : 0.0, R, S.max_cr, S.min_cr);
+                }
+                S.res_prev = C.res;
+            }
+            __syncthreads();
+            if (S.ctl.done) break;
+        }
+    }
+    if (blockIdx.x == 0) {
+        const unsigned long long* src = reinterpret_cast<const unsigned long long*>(&S);
+        unsigned long long* dst = reinterpret_cast<unsigned long long*>(st);
+        for (int k = threadIdx.x; k < (int)(sizeof(GmresState) / 8); k += KB) dst[k] = src[k];
+    }
+}
+
 // ---- launchers --------------------------------------------------------------
 
 void gmres_init(const EllMatrix& A, const double* b, const double* x, GmresWork& G, KrylovWork& W, bool first,
@@ -301,6 +515,48 @@ void gmres_update(double* x, GmresWork& G, int64_t rows, cudaStream_t s)
 {
     k_gm_solve<<<1, 32, 0, s>>>(G.st);
     k_gm_update_x<<<row_grid(k_gm_update_x, rows), KB, 0, s>>>(rows, G.U, x, G.st);
+}
+
+cudaError_t gmres_small(const EllMatrix& A, const double* b, double* x, GmresWork& G, KrylovWork& W, bool reorth,
+                        int iters, cudaStream_t s)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const int sms = sm_count(dev);
+    int nb = 0;
+    auto occ = [&](auto kern) { return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, KB, 0); };
+    if (reorth) MHFEM_WIDTH_DISPATCH(A.width, e = occ(k_gmres_small<WW, true>));
+    else MHFEM_WIDTH_DISPATCH(A.width, e = occ(k_gmres_small<WW, false>));
+    if (e != cudaSuccess) return e;
+    if (nb < 1) return cudaErrorCooperativeLaunchTooLarge;
+    // about two rows per thread, every CTA resident, at most one per SM, and
+    // at most as many CTAs as the partials regions hold
+    const int64_t want = (A.rows + 2 * (int64_t)KB - 1) / (2 * (int64_t)KB);
+    int grid = (int)std::min<int64_t>(std::min<int64_t>(want, (int64_t)sms), (int64_t)nb * sms);
+    grid = std::max(1, std::min(grid, std::min(krylov_grid() / 2, W.grid)));
+    unsigned int* bar = W.counters + 2;
+    int* bar_err = reinterpret_cast<int*>(W.counters + 3);
+    e = cudaMemsetAsync(bar, 0, 2 * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+    const int32_t* cols = A.cols;
+    const double* vals = A.vals;
+    int W_ = A.width;
+    int64_t rows = A.rows;
+    double* U = G.U;
+    GmresState* st = G.st;
+    double* pdots = G.partials;
+    double* pnorm = W.partials;
+    int its = iters;
+    void* args[] = {(void*)&cols, (void*)&vals, (void*)&W_, (void*)&rows, (void*)&b, (void*)&x, (void*)&U,
+                    (void*)&st, (void*)&pdots, (void*)&pnorm, (void*)&bar, (void*)&bar_err, (void*)&its};
+    if (reorth)
+        MHFEM_WIDTH_DISPATCH(A.width, e = cudaLaunchCooperativeKernel((const void*)k_gmres_small<WW, true>, dim3(grid),
+                                                                     dim3(KB), args, 0, s));
+    else
+        MHFEM_WIDTH_DISPATCH(A.width, e = cudaLaunchCooperativeKernel((const void*)k_gmres_small<WW, false>, dim3(grid),
+                                                                     dim3(KB), args, 0, s));
+    return e;
 }
 
 }  // namespace mhfem

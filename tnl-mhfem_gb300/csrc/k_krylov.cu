@@ -809,46 +809,6 @@ __global__ void __launch_bounds__(KB) k_update_p(int64_t rows, T* p, const T* r,
 // records the failure in *bar_err and returns, and the others then fail
 // their next wait at once.
 
-constexpr unsigned int kBarrierPolls = 1u << 22;  // seconds, far beyond any barrier of a working launch
-
-__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p)
-{
-    unsigned int v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// Arrive at the grid barrier whose cumulative arrival count is `target`
-// (the count starts at 0 for a launch and grows by gridDim.x per barrier)
-// and wait for every CTA.  False (in every thread of the CTA) when the wait
-// gave up.
-__device__ __forceinline__ bool grid_barrier(unsigned int* count, int* err, unsigned int target,
-                                             unsigned int max_polls = kBarrierPolls)
-{
-    __shared__ int ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int good = 1;
-        __threadfence();
-        // the last CTA to arrive sees the target in its own add and does not
-        // poll: it is the one the others wait for in the next phase too
-        const unsigned int seen = atomicAdd(count, 1u) + 1u;
-        unsigned int polls = 0;
-        while (seen < target && ld_acquire_u32(count) < target) {
-            if (++polls > max_polls || *(volatile int*)err != 0) {
-                good = 0;
-                atomicExch(err, 1);
-                break;
-            }
-            __nanosleep(32);
-        }
-        __threadfence();
-        ok = good;
-    }
-    __syncthreads();
-    return ok != 0;
-}
-
 // Check of the bounded barrier: every CTA but `skip` (none if negative)
 // arrives once and reports 1 (passed) or 0 (gave up); CTA `skip` never
 // arrives and reports -1, so the others' waits run out after max_polls.
@@ -863,63 +823,6 @@ __global__ void __launch_bounds__(KB) k_grid_barrier_check(unsigned int* count, 
     if (threadIdx.x == 0) result[blockIdx.x] = ok ? 1 : 0;
 }
 
-// Sum of the per-CTA partials [cta][kPartStride] in CTA order, identical in
-// every CTA (same loads, same order); the result is in out[] of every thread.
-template <int NV>
-__device__ __forceinline__ void grid_sums(const double* partials, double (&out)[NV])
-{
-    __shared__ double col[NV][KB];
-    __shared__ double tot[NV];
-    const int nb = (int)gridDim.x;
-#pragma unroll
-    for (int q = 0; q < NV; ++q)
-        col[q][threadIdx.x] = threadIdx.x < nb ? __ldcg(partials + (int64_t)threadIdx.x * kPartStride + q) : 0.0;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
-#pragma unroll
-        for (int q = 0; q < NV; ++q) {
-            double v = col[q][lane];
-#pragma unroll
-            for (int w = 1; w < KB / 32; ++w) v += col[q][lane + 32 * w];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-            if (lane == 0) tot[q] = v;
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < NV; ++q) out[q] = tot[q];
-}
-
-// y = self + sum_k a_k g(c_k), where g(j) forms the gathered vector's value
-// at row j (loaded past L1); same operation order as spmv_rows, so the
-// products match the five-kernel path's.
-template <int WW, typename G>
-__device__ __forceinline__ double small_row(const int32_t* __restrict__ cols, const double* __restrict__ vals, int W,
-                                            int64_t rows, int64_t q, double self, G&& g)
-{
-    double acc = self;
-    if constexpr (WW > 0) {
-        int32_t c[WW];
-        double a[WW], xg[WW];
-#pragma unroll
-        for (int k = 0; k < WW; ++k) {
-            c[k] = __ldg(cols + (int64_t)k * rows + q);
-            a[k] = __ldg(vals + (int64_t)k * rows + q);
-        }
-#pragma unroll
-        for (int k = 0; k < WW; ++k) xg[k] = g(c[k]);
-#pragma unroll
-        for (int k = 0; k < WW; ++k) acc = fma(a[k], xg[k], acc);
-    }
-    else
-        for (int k = 0; k < W; ++k) {
-            const int64_t o = (int64_t)k * rows + q;
-            acc = fma(__ldg(vals + o), g(__ldg(cols + o)), acc);
-        }
-    return acc;
-}
 
 // The ELL words of one row held in registers for a whole launch (the
 // matrix does not change during a solve).

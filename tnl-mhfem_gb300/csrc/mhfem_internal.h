@@ -185,6 +185,12 @@ struct GmresState {
     double H[kGmresMaxM + 1][kGmresMaxM];
     double cs[kGmresMaxM], sn[kGmresMaxM];
     double g[kGmresMaxM + 1];
+    // restarts inside the persistent small-system solve: the true relative
+    // residual at the last restart, and the adaptive restart rule
+    // (gmres_restart.h) with its two thresholds
+    double res_prev;
+    double max_cr, min_cr;
+    int32_t m_min, m_max, step_min, step_max;
 };
 
 struct GmresWork {
@@ -203,6 +209,11 @@ void gmres_init(const EllMatrix& A, const double* b, const double* x, GmresWork&
 void gmres_iterate(const EllMatrix& A, GmresWork& G, KrylovWork& W, int iters, bool reorth, cudaStream_t s);
 // end of a cycle: solve the triangular system and update x
 void gmres_update(double* x, GmresWork& G, int64_t rows, cudaStream_t s);
+// Small systems (at most krylov_small_rows() rows): up to `iters` Arnoldi
+// iterations, restarts included, in one cooperative launch (bounded grid
+// barriers; W.counters + 2 and + 3 are its barrier count and failure flag).
+cudaError_t gmres_small(const EllMatrix& A, const double* b, double* x, GmresWork& G, KrylovWork& W, bool reorth,
+                        int iters, cudaStream_t s);
 void krylov_iterate_fp64(const EllMatrix& A, double* x, KrylovWork& W, int iters, cudaStream_t s);
 // Small systems (rows <= krylov_small_rows()): up to `iters` FP64 BiCGStab
 // iterations in one cooperative launch on a solve set up by krylov_init_fp64
