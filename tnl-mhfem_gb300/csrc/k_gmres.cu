@@ -12,8 +12,9 @@
 // of a cycle and restarts from the true residual.  The restart length is
 // gmres-restarting-max, or, with gmres-restarting-min and the steps set,
 // varies between the two from cycle to cycle (gmres_restart.h: Baker,
-// Jessup and Kolev's rule, applied by the host between cycles; the device
-// reads the cycle length from its state in every iteration).
+// Jessup and Kolev's rule, applied by the host between cycles, or by the
+// device inside the persistent small-system solve; the device reads the
+// cycle length from its state in every iteration).
 //
 // Design for GB300:
 //  - the basis is stored unnormalized (v_i = inv_i u_i), so no pass only
@@ -29,7 +30,9 @@
 //    last block sums them in a fixed order);
 //  - every iteration kernel returns at once when the cycle has ended or the
 //    solve is done, so the host replays a CUDA graph of several iterations
-//    between checks.
+//    between checks;
+//  - systems of at most 2^18 rows run k_gmres_small instead: a persistent
+//    cooperative launch per chunk of iterations, restarts included (below).
 #include <algorithm>
 #include <initializer_list>
 
